@@ -1,0 +1,285 @@
+"""nsgb: GB300-native morphological reconstruction and union-find labelling.
+
+Thin Python mirror of the reference's `nscale::` / `nscale::gpu::` interface
+(fastIA-master/src/segment/MorphologicOperations.h:21-190) over the C ABI in libnsgb.so.
+Same names, argument order and meaning; images are 2-D CUDA tensors (uint8, uint16, int32,
+float32) instead of cv::Mat / cv::gpu::GpuMat, and results are new tensors.  Errors raise
+`NsgbError` (the reference raised cv::Exception on bad arguments); there is no CPU fallback:
+CPU tensors are rejected.
+
+Every call runs on torch's current CUDA stream and synchronizes it at the end to report the
+device-side status, matching the reference's blocking calls.  For asynchronous use call the
+C ABI directly (opts.sync = 0).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Dict, Optional, Tuple
+
+import torch
+
+from . import _ffi
+from ._ffi import NsgbError, lib
+
+__all__ = [
+    "imreconstruct", "imreconstructBinary", "imfillHoles", "imhmin", "bwselect", "bwlabel", "bwlabel2",
+    "bwareaopen2", "threshold", "invert", "chain", "NsgbError", "workspace",
+]
+
+_DT = {torch.uint8: _ffi.U8, torch.int32: _ffi.I32, torch.float32: _ffi.F32}
+if hasattr(torch, "uint16"):
+    _DT[torch.uint16] = _ffi.U16
+
+
+def _dtype_code(t: torch.Tensor) -> int:
+    if t.dtype not in _DT:
+        raise NsgbError(2, f"dtype {t.dtype}")
+    return _DT[t.dtype]
+
+
+def _check_image(t: torch.Tensor, name: str) -> None:
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise NsgbError(1, f"{name} must be a CUDA tensor (no CPU path)")
+    if t.dim() != 2:
+        raise NsgbError(1, f"{name} must be 2-D (single channel)")
+    if t.stride(1) != 1:
+        raise NsgbError(1, f"{name} must have unit column stride")
+
+
+def _pitch(t: torch.Tensor) -> int:
+    return t.stride(0) * t.element_size()
+
+
+def _stream() -> C.c_void_p:
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class _Workspace:
+    """Per-device cached workspace (a uint8 tensor grown on demand)."""
+
+    def __init__(self) -> None:
+        self._buf: Dict[int, torch.Tensor] = {}
+
+    def get(self, nbytes: int, device: torch.device) -> Tuple[int, int]:
+        idx = device.index if device.index is not None else torch.cuda.current_device()
+        buf = self._buf.get(idx)
+        if buf is None or buf.numel() < nbytes:
+            buf = torch.empty(max(nbytes, 1 << 20) + 256, dtype=torch.uint8, device=device)
+            self._buf[idx] = buf
+        ptr = buf.data_ptr()
+        aligned = (ptr + 255) & ~255
+        return aligned, buf.numel() - (aligned - ptr)
+
+
+workspace = _Workspace()
+
+
+def _ws(op: int, dtype: int, rows: int, cols: int, device: torch.device) -> Tuple[int, int]:
+    need = lib.nsgb_workspace_size(op, dtype, rows, cols)
+    return workspace.get(need, device)
+
+
+def _same_shape(a: torch.Tensor, b: torch.Tensor, what: str) -> None:
+    if a.shape != b.shape or a.dtype != b.dtype or a.device != b.device:
+        raise NsgbError(1, f"{what}: shape/dtype/device mismatch")
+
+
+def _dense_like(t: torch.Tensor, dtype: Optional[torch.dtype] = None) -> torch.Tensor:
+    return torch.empty(t.shape, dtype=dtype or t.dtype, device=t.device)
+
+
+def _contig(t: torch.Tensor) -> torch.Tensor:
+    return t if t.is_contiguous() else t.contiguous()
+
+
+def imreconstruct(seeds: torch.Tensor, image: torch.Tensor, connectivity: int, erode: bool = False,
+                  max_rounds: int = 0, max_visit_iters: int = 0) -> torch.Tensor:
+    """nscale::imreconstruct<T>(seeds, image, connectivity) (MorphologicOperations.cpp:665-838) /
+    nscale::gpu::imreconstruct<T> (MorphologicOperationsGPU.cpp:172-200): reconstruction by
+    dilation of `seeds` under `image`.  `erode=True` gives the dual (reconstruction by erosion)."""
+    _check_image(seeds, "seeds")
+    _check_image(image, "image")
+    _same_shape(seeds, image, "imreconstruct")
+    dt = _dtype_code(image)
+    out = _contig(seeds).clone()
+    mask = _contig(image)
+    rows, cols = out.shape
+    ws, nb = _ws(_ffi.OP_IMRECONSTRUCT, dt, rows, cols, out.device)
+    opts = _ffi.Opts(1, max_rounds, max_visit_iters)
+    st = lib.nsgb_imreconstruct(dt, out.data_ptr(), mask.data_ptr(), rows, cols, _pitch(out), connectivity,
+                                1 if erode else 0, ws, nb, _stream(), C.byref(opts))
+    _ffi.check(st, "imreconstruct")
+    return out
+
+
+def imreconstructBinary(seeds: torch.Tensor, binaryImage: torch.Tensor, connectivity: int) -> torch.Tensor:
+    """nscale::imreconstructBinary<T> (MorphologicOperations.cpp:1688-1829)."""
+    _check_image(seeds, "seeds")
+    _check_image(binaryImage, "binaryImage")
+    _same_shape(seeds, binaryImage, "imreconstructBinary")
+    dt = _dtype_code(binaryImage)
+    out = _contig(seeds).clone()
+    mask = _contig(binaryImage)
+    rows, cols = out.shape
+    ws, nb = _ws(_ffi.OP_IMRECONSTRUCT_BINARY, dt, rows, cols, out.device)
+    st = lib.nsgb_imreconstruct_binary(dt, out.data_ptr(), mask.data_ptr(), rows, cols, _pitch(out), connectivity,
+                                       ws, nb, _stream(), None)
+    _ffi.check(st, "imreconstructBinary")
+    return out
+
+
+def imfillHoles(image: torch.Tensor, binary: bool, connectivity: int) -> torch.Tensor:
+    """nscale::imfillHoles<T>(image, binary, connectivity) (MorphologicOperations.cpp:1859-1926)."""
+    _check_image(image, "image")
+    dt = _dtype_code(image)
+    img = _contig(image)
+    out = _dense_like(img)
+    rows, cols = img.shape
+    ws, nb = _ws(_ffi.OP_FILL_HOLES, dt, rows, cols, img.device)
+    st = lib.nsgb_imfill_holes(dt, img.data_ptr(), out.data_ptr(), rows, cols, _pitch(img), 1 if binary else 0,
+                               connectivity, ws, nb, _stream(), None)
+    _ffi.check(st, "imfillHoles")
+    return out
+
+
+def imhmin(image: torch.Tensor, h: float, connectivity: int) -> torch.Tensor:
+    """nscale::imhmin<T>(image, h, connectivity) (MorphologicOperations.cpp:2260-2282)."""
+    _check_image(image, "image")
+    dt = _dtype_code(image)
+    img = _contig(image)
+    out = _dense_like(img)
+    rows, cols = img.shape
+    ws, nb = _ws(_ffi.OP_HMIN, dt, rows, cols, img.device)
+    st = lib.nsgb_imhmin(dt, img.data_ptr(), out.data_ptr(), rows, cols, _pitch(img), float(h), connectivity, ws,
+                         nb, _stream(), None)
+    _ffi.check(st, "imhmin")
+    return out
+
+
+def bwselect(binaryImage: torch.Tensor, seeds: torch.Tensor, connectivity: int) -> torch.Tensor:
+    """nscale::bwselect<T>(binaryImage, seeds, connectivity) (MorphologicOperations.cpp:1929-1951)."""
+    _check_image(binaryImage, "binaryImage")
+    _check_image(seeds, "seeds")
+    _same_shape(binaryImage, seeds, "bwselect")
+    dt = _dtype_code(binaryImage)
+    img = _contig(binaryImage)
+    sd = _contig(seeds)
+    out = _dense_like(img)
+    rows, cols = img.shape
+    ws, nb = _ws(_ffi.OP_BWSELECT, dt, rows, cols, img.device)
+    st = lib.nsgb_bwselect(dt, img.data_ptr(), sd.data_ptr(), out.data_ptr(), rows, cols, _pitch(img), connectivity,
+                           ws, nb, _stream(), None)
+    _ffi.check(st, "bwselect")
+    return out
+
+
+def bwlabel2(binaryImage: torch.Tensor, connectivity: int, relab: bool) -> torch.Tensor:
+    """nscale::bwlabel2(binaryImage, connectivity, relab) (MorphologicOperations.cpp:2012-2035).
+    relab=True: labels 1..n in raster order, background 0; relab=False: smallest raster
+    index of the component, background -1."""
+    lab, _ = _bwlabel(binaryImage, connectivity, relab)
+    return lab
+
+
+def bwlabel(binaryImage: torch.Tensor, connectivity: int, relab: bool) -> torch.Tensor:
+    """nscale::gpu::bwlabel(binaryImage, connectivity, relab) (MorphologicOperationsGPU.cpp:878-900)."""
+    return bwlabel2(binaryImage, connectivity, relab)
+
+
+def _bwlabel(binaryImage: torch.Tensor, connectivity: int, relab: bool) -> Tuple[torch.Tensor, int]:
+    _check_image(binaryImage, "binaryImage")
+    if binaryImage.dtype != torch.uint8:
+        raise NsgbError(2, "bwlabel2 takes a uint8 image")
+    img = _contig(binaryImage)
+    rows, cols = img.shape
+    lab = torch.empty((rows, cols), dtype=torch.int32, device=img.device)
+    ws, nb = _ws(_ffi.OP_BWLABEL, _ffi.U8, rows, cols, img.device)
+    n = C.c_int32(0)
+    st = lib.nsgb_bwlabel(img.data_ptr(), lab.data_ptr(), rows, cols, _pitch(img), _pitch(lab), connectivity,
+                          1 if relab else 0, C.byref(n), ws, nb, _stream(), None)
+    _ffi.check(st, "bwlabel2")
+    return lab, int(n.value)
+
+
+def bwlabel2_count(binaryImage: torch.Tensor, connectivity: int) -> Tuple[torch.Tensor, int]:
+    """bwlabel2 with relabelling, also returning the number of components
+    (ConnComponents::relabel's return value)."""
+    return _bwlabel(binaryImage, connectivity, True)
+
+
+def bwareaopen2(image: torch.Tensor, labeled: bool, flatten: bool, minSize: int, maxSize: int,
+                connectivity: int) -> Tuple[torch.Tensor, int]:
+    """nscale::bwareaopen2(image, labeled, flatten, minSize, maxSize, connectivity, count)
+    (MorphologicOperations.cpp:2199-2232).  Returns (result, count): result is uint8 255/0 when
+    `flatten`, else int32 kept labels (background -1); count = components kept."""
+    _check_image(image, "image")
+    if labeled and image.dtype != torch.int32:
+        raise NsgbError(2, "labeled input must be int32")
+    if not labeled and image.dtype != torch.uint8:
+        raise NsgbError(2, "unlabeled input must be uint8")
+    img = _contig(image)
+    rows, cols = img.shape
+    ws, nb = _ws(_ffi.OP_BWAREAOPEN, _ffi.U8, rows, cols, img.device)
+    cnt = C.c_int32(0)
+    if flatten:
+        out = torch.empty((rows, cols), dtype=torch.uint8, device=img.device)
+        st = lib.nsgb_bwareaopen(img.data_ptr(), 1 if labeled else 0, None, out.data_ptr(), rows, cols, _pitch(img),
+                                 0, _pitch(out), int(minSize), int(maxSize), connectivity, C.byref(cnt), ws, nb,
+                                 _stream(), None)
+    else:
+        out = torch.empty((rows, cols), dtype=torch.int32, device=img.device)
+        st = lib.nsgb_bwareaopen(img.data_ptr(), 1 if labeled else 0, out.data_ptr(), None, rows, cols, _pitch(img),
+                                 _pitch(out), 0, int(minSize), int(maxSize), connectivity, C.byref(cnt), ws, nb,
+                                 _stream(), None)
+    _ffi.check(st, "bwareaopen2")
+    return out, int(cnt.value)
+
+
+def threshold(image: torch.Tensor, thr: float) -> torch.Tensor:
+    """`image > thr` as 255 / 0 uint8 (OpenCV `Mat > k`, HistologicalEntities.cpp:214)."""
+    _check_image(image, "image")
+    dt = _dtype_code(image)
+    img = _contig(image)
+    out = _dense_like(img, torch.uint8)
+    rows, cols = img.shape
+    st = lib.nsgb_threshold(dt, img.data_ptr(), out.data_ptr(), rows, cols, _pitch(img), _pitch(out), float(thr),
+                            _stream())
+    _ffi.check(st, "threshold")
+    return out
+
+
+def invert(image: torch.Tensor) -> torch.Tensor:
+    """nscale::PixelOperations::invert<T> (PixelOperations.cpp:18-39)."""
+    _check_image(image, "image")
+    dt = _dtype_code(image)
+    img = _contig(image)
+    out = _dense_like(img)
+    rows, cols = img.shape
+    st = lib.nsgb_invert(dt, img.data_ptr(), out.data_ptr(), rows, cols, _pitch(img), _stream())
+    _ffi.check(st, "invert")
+    return out
+
+
+def chain(marker: torch.Tensor, mask: torch.Tensor, recon_conn: int = 8, thr: float = 128, fill_conn: int = 4,
+          label_conn: int = 8, area_min: int = 11, area_max: int = 1000) -> Dict[str, object]:
+    """The device-resident segmentation chain of HistologicalEntities.cpp:195-246:
+    reconstruction, threshold, binary hole fill, bwlabel2 (relabelled) and bwareaopen2."""
+    _check_image(marker, "marker")
+    _check_image(mask, "mask")
+    _same_shape(marker, mask, "chain")
+    dt = _dtype_code(mask)
+    rec = _contig(marker).clone()
+    msk = _contig(mask)
+    rows, cols = rec.shape
+    dev = rec.device
+    fill = torch.empty((rows, cols), dtype=torch.uint8, device=dev)
+    labels = torch.empty((rows, cols), dtype=torch.int32, device=dev)
+    area = torch.empty((rows, cols), dtype=torch.uint8, device=dev)
+    ws, nb = _ws(_ffi.OP_CHAIN, dt, rows, cols, dev)
+    nl, nk = C.c_int32(0), C.c_int32(0)
+    st = lib.nsgb_chain(dt, rec.data_ptr(), msk.data_ptr(), rows, cols, _pitch(rec), recon_conn, float(thr),
+                        fill_conn, label_conn, int(area_min), int(area_max), fill.data_ptr(), labels.data_ptr(),
+                        area.data_ptr(), C.byref(nl), C.byref(nk), ws, nb, _stream(), None)
+    _ffi.check(st, "chain")
+    return {"recon": rec, "fill": fill, "labels": labels, "area": area, "n_labels": int(nl.value),
+            "n_kept": int(nk.value)}

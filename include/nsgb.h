@@ -1,0 +1,178 @@
+/* nsgb — GB300-native morphological reconstruction and union-find labelling.
+ *
+ * C ABI of the device library (libnsgb.so).  Every entry point:
+ *   - takes DEVICE pointers for images (row pitch in bytes, pitch >= cols * element size,
+ *     pitch a multiple of the element size), a caller-provided device workspace of at least
+ *     nsgb_workspace_size(op, ...) bytes, and a CUDA stream;
+ *   - enqueues its kernels on that stream and never allocates device memory;
+ *   - returns an nsgb_status and never throws.  With opts == NULL or opts->sync != 0 the
+ *     call synchronizes the stream and also reports errors detected on the device (iteration
+ *     budget exhausted, wait timeout); with opts->sync == 0 it returns after enqueueing and
+ *     nsgb_device_status() reads the device-side status later.
+ *   - calls on different streams with different workspaces are independent (no global state).
+ *
+ * Semantics follow the reference's serial CPU implementation (nscale::, fastIA-master/src/
+ * segment/MorphologicOperations.cpp and ConnComponents.cpp), which is also what its GPU path
+ * computes; each function names the reference interface it replaces.
+ */
+#ifndef NSGB_H_
+#define NSGB_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* nsgb_stream_t; /* == cudaStream_t */
+
+typedef enum {
+  NSGB_OK = 0,
+  NSGB_ERR_BAD_ARG = 1,           /* null pointer, bad size, pitch, connectivity ... */
+  NSGB_ERR_UNSUPPORTED_DTYPE = 2, /* dtype not defined for this operation */
+  NSGB_ERR_WORKSPACE = 3,         /* workspace missing or smaller than required */
+  NSGB_ERR_NOT_CONVERGED = 4,     /* iteration / round budget exhausted on the device */
+  NSGB_ERR_TIMEOUT = 5,           /* a bounded device-side wait gave up */
+  NSGB_ERR_CUDA = 6,              /* a CUDA runtime call failed */
+  NSGB_ERR_QUEUE_OVERFLOW = 7     /* a device work list ran out of capacity */
+} nsgb_status;
+
+typedef enum { NSGB_U8 = 0, NSGB_U16 = 1, NSGB_I32 = 2, NSGB_F32 = 3 } nsgb_dtype;
+
+typedef enum {
+  NSGB_OP_IMRECONSTRUCT = 0,
+  NSGB_OP_IMRECONSTRUCT_BINARY = 1,
+  NSGB_OP_FILL_HOLES = 2,
+  NSGB_OP_HMIN = 3,
+  NSGB_OP_BWSELECT = 4,
+  NSGB_OP_BWLABEL = 5,
+  NSGB_OP_BWAREAOPEN = 6,
+  NSGB_OP_CHAIN = 7
+} nsgb_op;
+
+typedef struct {
+  int sync;       /* 1: synchronize and return the device status (default when opts == NULL) */
+  int max_rounds; /* reconstruction: cap on work-list rounds (0 = default) */
+  int max_visit_iters; /* reconstruction: cap on row/column sweeps per tile visit (0 = default) */
+  int reserved[5];
+  /* Optional CUDA events (cudaEvent_t) recorded on the call's stream immediately before and
+   * after the reconstruction kernel (nsgb_imreconstruct, nsgb_chain), for timing it alone. */
+  void* recon_event_begin;
+  void* recon_event_end;
+} nsgb_opts;
+
+/* Bytes of device workspace needed by `op` on an image of rows x cols of `dtype`. */
+size_t nsgb_workspace_size(int op, int dtype, int64_t rows, int64_t cols);
+
+const char* nsgb_status_string(int status);
+
+/* Reads (synchronously) the device-side status word of the last call that used `ws`. */
+nsgb_status nsgb_device_status(const void* ws, nsgb_stream_t stream);
+
+/* Grayscale morphological reconstruction, in place on `marker` (read-only `mask`).
+ *   erode = 0: reconstruction by dilation of marker under mask -- nscale::imreconstruct<T>
+ *              (MorphologicOperations.cpp:665-838; GPU: nscale::gpu::imreconstruct<T>
+ *              MorphologicOperationsGPU.cpp:172-200, imreconstructIntCaller<T> /
+ *              imreconstructFloatCaller<T> imreconstruct_int_kernel.cuh:7-9,
+ *              imreconstruct_float_kernel.cuh, and the queue variants
+ *              imreconstructQueueSpeedup<T> MorphologicOperationsGPU.cpp:286-360 /
+ *              morphReconSpeedup global_queue.cuh:48-50).  Includes the reference's
+ *              0-valued padding ring (visible only for negative signed / float data).
+ *   erode = 1: reconstruction by erosion of marker above mask (the dual), with no padding
+ *              ring; the hole-filling building block.
+ * dtypes: u8, u16, i32, f32.  conn: 4 or 8. */
+nsgb_status nsgb_imreconstruct(int dtype, void* marker, const void* mask, int64_t rows, int64_t cols,
+                               int64_t pitch, int conn, int erode, void* ws, size_t ws_bytes,
+                               nsgb_stream_t stream, const nsgb_opts* opts);
+
+/* Binary reconstruction in place on `marker`: every zero marker pixel whose mask is non-zero
+ * and that is connected through non-zero mask pixels to a pixel with marker != 0 and
+ * mask != 0 becomes max<T>; other pixels keep their marker value (the marker is not
+ * clamped by the mask).  nscale::imreconstructBinary<T> (MorphologicOperations.cpp:1688-
+ * 1829); GPU nscale::gpu::imreconstructBinary<T> (MorphologicOperationsGPU.cpp:686-721),
+ * imreconstructBinaryCaller<T> (imreconstruct_binary_kernel.cuh).  dtypes: u8, u16, i32. */
+nsgb_status nsgb_imreconstruct_binary(int dtype, void* marker, const void* mask, int64_t rows,
+                                      int64_t cols, int64_t pitch, int conn, void* ws,
+                                      size_t ws_bytes, nsgb_stream_t stream, const nsgb_opts* opts);
+
+/* Hole filling: nscale::imfillHoles<T>(image, binary, conn) (MorphologicOperations.cpp:
+ * 1859-1926); GPU nscale::gpu::imfillHoles<T> (MorphologicOperationsGPU.cpp:751-836).
+ * binary = 1: u8/u16 -> 0 where the pixel is not max<T> and is connected to the image
+ *             border through pixels that are not max<T>, else max<T> (0/max input gives the
+ *             usual fill); i32 -> INT_MAX everywhere (the reference's result for int, whose
+ *             padding value min<int> is non-zero).
+ * binary = 0: grayscale fill, the erosion reconstruction of (image on the border, max<T>
+ *             inside) above the image.  dtypes u8, u16, i32, f32.  out must not alias image. */
+nsgb_status nsgb_imfill_holes(int dtype, const void* image, void* out, int64_t rows, int64_t cols,
+                              int64_t pitch, int binary, int conn, void* ws, size_t ws_bytes,
+                              nsgb_stream_t stream, const nsgb_opts* opts);
+
+/* h-minima transform: nscale::imhmin<T>(image, h, conn) (MorphologicOperations.cpp:2260-2282;
+ * GPU MorphologicOperationsGPU.cpp:1059-1098) = invert(imreconstruct(invert(I) - h,
+ * invert(I))) with saturating subtraction.  dtypes u8, u16, f32. */
+nsgb_status nsgb_imhmin(int dtype, const void* image, void* out, int64_t rows, int64_t cols,
+                        int64_t pitch, double h, int conn, void* ws, size_t ws_bytes,
+                        nsgb_stream_t stream, const nsgb_opts* opts);
+
+/* nscale::bwselect<T>(binaryImage, seeds, conn) (MorphologicOperations.cpp:1929-1951; GPU
+ * MorphologicOperationsGPU.cpp:839-868): keeps the image's non-zero pixels whose component
+ * (non-zero adjacency) contains a pixel with seeds != 0.  dtypes u8, u16, i32. */
+nsgb_status nsgb_bwselect(int dtype, const void* image, const void* seeds, void* out, int64_t rows,
+                          int64_t cols, int64_t pitch, int conn, void* ws, size_t ws_bytes,
+                          nsgb_stream_t stream, const nsgb_opts* opts);
+
+/* Union-find labelling of a u8 image: equal-valued non-zero neighbours are joined.
+ * relabel = 1: labels 1..n in raster order of each component's first pixel, background 0
+ *              (nscale::bwlabel2(bin, conn, true), MorphologicOperations.cpp:2012-2035 ->
+ *              ConnComponents::label + relabel, ConnComponents.cpp:52-118; GPU
+ *              nscale::gpu::bwlabel MorphologicOperationsGPU.cpp:878-900 -> CCL + relabel,
+ *              ccl_uf.cuh:11-16).
+ * relabel = 0: each pixel gets the smallest raster index (row*cols + col) of its component,
+ *              background -1 (bwlabel2(bin, conn, false)).
+ * `count` (host pointer, optional) receives n; it forces a stream synchronization. */
+nsgb_status nsgb_bwlabel(const uint8_t* bin, int32_t* labels, int64_t rows, int64_t cols,
+                         int64_t pitch_in, int64_t pitch_labels, int conn, int relabel,
+                         int32_t* count, void* ws, size_t ws_bytes, nsgb_stream_t stream,
+                         const nsgb_opts* opts);
+
+/* Area opening: nscale::bwareaopen2(image, labeled, flatten, minSize, maxSize, conn, count)
+ * (MorphologicOperations.cpp:2199-2232 -> ConnComponents::areaThresholdLabeled,
+ * ConnComponents.cpp:205-239; GPU nscale::gpu::bwareaopen2 MorphologicOperationsGPU.cpp:
+ * 1024-1057 -> areaThreshold2 ccl_uf.cuh).  Keeps components whose pixel count is in
+ * [min_size, max_size).  labeled = 0: `in` is a u8 image labelled first (conn);
+ * labeled = 1: `in` is an int32 label image (background -1).  Outputs (each optional):
+ * labels_out = kept label (the input label / smallest raster index), -1 elsewhere;
+ * flat_out = 255 where kept, else 0.  `count` (host, optional) = components kept. */
+nsgb_status nsgb_bwareaopen(const void* in, int labeled, int32_t* labels_out, uint8_t* flat_out,
+                            int64_t rows, int64_t cols, int64_t pitch_in, int64_t pitch_labels,
+                            int64_t pitch_flat, int32_t min_size, int32_t max_size, int conn,
+                            int32_t* count, void* ws, size_t ws_bytes, nsgb_stream_t stream,
+                            const nsgb_opts* opts);
+
+/* Elementwise helpers of the path: `in > thr` -> 255 / 0 (u8 out; OpenCV `Mat > k` as used at
+ * HistologicalEntities.cpp:214; GPU thresholdCaller pixel-ops.cu:349-381), and invert
+ * (PixelOperations::invert<T>, PixelOperations.cpp:18-39; GPU invertKernel* pixel-ops.cu:
+ * 15-48): unsigned max - x, signed -x (INT_MIN -> INT_MAX), float -x. */
+nsgb_status nsgb_threshold(int dtype, const void* in, uint8_t* out, int64_t rows, int64_t cols,
+                           int64_t pitch_in, int64_t pitch_out, double thr, nsgb_stream_t stream);
+nsgb_status nsgb_invert(int dtype, const void* in, void* out, int64_t rows, int64_t cols,
+                        int64_t pitch, nsgb_stream_t stream);
+
+/* The single-tile segmentation chain of HistologicalEntities.cpp:195-246, kept on the
+ * device: R = imreconstruct(marker, mask, recon_conn) in place on `marker`;
+ * B = R > thr; F = imfillHoles(B, binary, fill_conn); L = bwlabel2(F, label_conn, relabel);
+ * A = bwareaopen2(F, unlabeled, flatten, area_min, area_max, label_conn).  Outputs fill,
+ * labels, area (each optional).  n_labels / n_kept: host pointers (optional; synchronize).
+ * dtypes of marker/mask: u8, u16, i32 (threshold in the same units). */
+nsgb_status nsgb_chain(int dtype, void* marker, const void* mask, int64_t rows, int64_t cols,
+                       int64_t pitch, int recon_conn, double thr, int fill_conn, int label_conn,
+                       int32_t area_min, int32_t area_max, uint8_t* fill_out, int32_t* labels_out,
+                       uint8_t* area_out, int32_t* n_labels, int32_t* n_kept, void* ws,
+                       size_t ws_bytes, nsgb_stream_t stream, const nsgb_opts* opts);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NSGB_H_ */

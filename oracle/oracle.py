@@ -1,0 +1,176 @@
+"""Python view of the CPU oracle (liboracle.so).  TEST INFRASTRUCTURE ONLY.
+
+Restates the reference's serial algorithms (recon_oracle.hpp cites each one).  Used by
+tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, never by the product.
+`ref` (optional) is the reference's own ConnComponents.cpp compiled from its sources into
+oracle/_ref/ (oracle/build_ref.sh); it exists only where the reference tree was available.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libconncomp_ref.so")
+
+DT = {np.dtype(np.uint8): 0, np.dtype(np.uint16): 1, np.dtype(np.int32): 2, np.dtype(np.float32): 3}
+
+
+def build() -> None:
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    subprocess.run([os.path.join(HERE, "build_ref.sh")], check=True, capture_output=True)
+
+
+def _load() -> C.CDLL:
+    if not os.path.exists(LIB):
+        build()
+    lib = C.CDLL(LIB)
+    vp, i64, i32 = C.c_void_p, C.c_int64, C.c_int32
+    lib.orc_imreconstruct.argtypes = [C.c_int, vp, vp, i64, i64, C.c_int, vp]
+    lib.orc_imreconstruct_binary.argtypes = [C.c_int, vp, vp, i64, i64, C.c_int, vp]
+    lib.orc_imfill_holes.argtypes = [C.c_int, vp, i64, i64, C.c_int, C.c_int, vp]
+    lib.orc_imhmin.argtypes = [C.c_int, vp, i64, i64, C.c_double, C.c_int, vp]
+    lib.orc_bwselect.argtypes = [C.c_int, vp, vp, i64, i64, C.c_int, vp]
+    lib.orc_threshold_gt.argtypes = [C.c_int, vp, i64, C.c_double, vp]
+    lib.orc_bwlabel2.argtypes = [vp, i64, i64, C.c_int, C.c_int, vp]
+    lib.orc_bwlabel2.restype = i32
+    lib.orc_bwareaopen2.argtypes = [vp, C.c_int, C.c_int, i32, i32, C.c_int, i64, i64, vp, vp]
+    lib.orc_bwareaopen2.restype = i32
+    lib.orc_chain.argtypes = [C.c_int, vp, vp, i64, i64, C.c_int, C.c_double, C.c_int, C.c_int, i32, i32,
+                              vp, vp, vp, vp, C.POINTER(i32), vp]
+    lib.orc_chain.restype = i32
+    lib.orc_chain_replicas_seconds.argtypes = [vp, vp, i64, i64, C.c_int, C.c_int]
+    lib.orc_chain_replicas_seconds.restype = C.c_double
+    return lib
+
+
+lib = _load()
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _c(a: np.ndarray) -> np.ndarray:
+    return np.ascontiguousarray(a)
+
+
+def imreconstruct(seeds: np.ndarray, image: np.ndarray, conn: int) -> np.ndarray:
+    seeds, image = _c(seeds), _c(image)
+    out = np.empty_like(image)
+    assert lib.orc_imreconstruct(DT[image.dtype], _p(seeds), _p(image), image.shape[0], image.shape[1], conn,
+                                 _p(out)) == 0
+    return out
+
+
+def imreconstruct_binary(seeds: np.ndarray, image: np.ndarray, conn: int) -> np.ndarray:
+    seeds, image = _c(seeds), _c(image)
+    out = np.empty_like(image)
+    assert lib.orc_imreconstruct_binary(DT[image.dtype], _p(seeds), _p(image), image.shape[0], image.shape[1],
+                                        conn, _p(out)) == 0
+    return out
+
+
+def imfill_holes(image: np.ndarray, binary: bool, conn: int) -> np.ndarray:
+    image = _c(image)
+    out = np.empty_like(image)
+    assert lib.orc_imfill_holes(DT[image.dtype], _p(image), image.shape[0], image.shape[1], int(binary), conn,
+                                _p(out)) == 0
+    return out
+
+
+def imhmin(image: np.ndarray, h: float, conn: int) -> np.ndarray:
+    image = _c(image)
+    out = np.empty_like(image)
+    assert lib.orc_imhmin(DT[image.dtype], _p(image), image.shape[0], image.shape[1], float(h), conn, _p(out)) == 0
+    return out
+
+
+def bwselect(image: np.ndarray, seeds: np.ndarray, conn: int) -> np.ndarray:
+    image, seeds = _c(image), _c(seeds)
+    out = np.empty_like(image)
+    assert lib.orc_bwselect(DT[image.dtype], _p(image), _p(seeds), image.shape[0], image.shape[1], conn,
+                            _p(out)) == 0
+    return out
+
+
+def threshold_gt(image: np.ndarray, thr: float) -> np.ndarray:
+    image = _c(image)
+    out = np.empty(image.shape, np.uint8)
+    assert lib.orc_threshold_gt(DT[image.dtype], _p(image), image.size, float(thr), _p(out)) == 0
+    return out
+
+
+def bwlabel2(binary: np.ndarray, conn: int, relab: bool):
+    binary = _c(binary).astype(np.uint8, copy=False)
+    out = np.empty(binary.shape, np.int32)
+    n = lib.orc_bwlabel2(_p(binary), binary.shape[0], binary.shape[1], conn, int(relab), _p(out))
+    return out, int(n)
+
+
+def bwareaopen2(image: np.ndarray, labeled: bool, flatten: bool, lo: int, hi: int, conn: int):
+    image = _c(image)
+    H, W = image.shape
+    labels = np.empty((H, W), np.int32)
+    flat = np.empty((H, W), np.uint8)
+    cnt = lib.orc_bwareaopen2(_p(image), int(labeled), int(flatten), lo, hi, conn, H, W, _p(labels), _p(flat))
+    return (flat if flatten else labels), int(cnt)
+
+
+def chain(marker: np.ndarray, mask: np.ndarray, recon_conn=8, thr=128.0, fill_conn=4, label_conn=8, lo=11,
+          hi=1000):
+    marker, mask = _c(marker), _c(mask)
+    H, W = mask.shape
+    rec = np.empty_like(mask)
+    b = np.empty((H, W), np.uint8)
+    f = np.empty((H, W), np.uint8)
+    lab = np.empty((H, W), np.int32)
+    a = np.empty((H, W), np.uint8)
+    nl = C.c_int32(0)
+    kept = lib.orc_chain(DT[mask.dtype], _p(marker), _p(mask), H, W, recon_conn, float(thr), fill_conn, label_conn,
+                         lo, hi, _p(rec), _p(b), _p(f), _p(lab), C.byref(nl), _p(a))
+    return {"recon": rec, "thr": b, "fill": f, "labels": lab, "n_labels": int(nl.value), "area": a,
+            "n_kept": int(kept)}
+
+
+def chain_replicas_seconds(marker: np.ndarray, mask: np.ndarray, threads: int, reps: int) -> float:
+    marker, mask = _c(marker), _c(mask)
+    return float(lib.orc_chain_replicas_seconds(_p(marker), _p(mask), mask.shape[0], mask.shape[1], threads, reps))
+
+
+# -- the reference's own ConnComponents (only where it was built) ---------------------------
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def _ref() -> C.CDLL:
+    r = C.CDLL(REF_LIB)
+    r.ref_cc_label.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int]
+    r.ref_cc_relabel.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int]
+    r.ref_cc_relabel.restype = C.c_int
+    r.ref_cc_area_threshold_labeled.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int]
+    r.ref_cc_area_threshold_labeled.restype = C.c_int
+    return r
+
+
+def ref_label(img: np.ndarray, conn: int, relab: bool):
+    r = _ref()
+    img = _c(img).astype(np.uint8).copy()
+    H, W = img.shape
+    out = np.empty((H, W), np.int32)
+    r.ref_cc_label(_p(img), W, H, _p(out), -1, conn)
+    n = r.ref_cc_relabel(W, H, _p(out), -1) if relab else 0
+    return out, int(n)
+
+
+def ref_area_threshold_labeled(labels: np.ndarray, lo: int, hi: int):
+    r = _ref()
+    labels = _c(labels).astype(np.int32)
+    H, W = labels.shape
+    out = np.empty((H, W), np.int32)
+    n = r.ref_cc_area_threshold_labeled(_p(labels), W, H, _p(out), -1, lo, hi)
+    return out, int(n)

@@ -1,0 +1,424 @@
+// CPU oracle for the reconstruction / labelling path.  TEST INFRASTRUCTURE ONLY.
+//
+// This file restates, on plain arrays, the reference's serial CPU algorithms.  It is the
+// checker that the CUDA path is compared against; the product never links or calls it.
+// Only tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py use it.
+//
+// Every function cites the reference function it follows (paths relative to the
+// reference project root, fastIA-master/).  The restatement keeps the reference's
+// semantics: 0-padding of marker and mask, the raster / anti-raster / FIFO order of
+// Vincent's hybrid algorithm, numeric_limits-based padding values, and the union-find
+// root = smallest raster index rule.  It is written from the algorithm, not copied.
+//
+// Parity pins: the union-find part is checked against the reference's own
+// src/segment/ConnComponents.cpp compiled from source (oracle/build_ref.sh); the
+// reconstruction part has no reference golden output (the reference's test data is not
+// distributed), so it is pinned by the uniqueness of the reconstruction fixed point, by
+// property checks, and by the reference's inline 32x32 fixture
+// (test/segment/cuda/globalQueueTest.cu:446-583).
+#pragma once
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <deque>
+#include <limits>
+#include <type_traits>
+#include <vector>
+
+namespace orc {
+
+// src/common/TypeUtils.h:34-41: lowest value used for padding ("-inf").
+template <typename T>
+inline T type_min() {
+  if constexpr (std::numeric_limits<T>::is_integer) return std::numeric_limits<T>::min();
+  else return -std::numeric_limits<T>::max();
+}
+
+// src/segment/PixelOperations.cpp:18-39.  Unsigned: max - x.  Signed: bitwise_not(x) + 1
+// through OpenCV arithmetic; the one value where that overflows (INT_MIN) is taken with
+// OpenCV's saturating semantics, i.e. invert(INT_MIN) = INT_MAX.  Float: -x.
+template <typename T>
+inline T invert_px(T x) {
+  if constexpr (std::numeric_limits<T>::is_integer) {
+    if constexpr (std::numeric_limits<T>::is_signed) {
+      if (x == std::numeric_limits<T>::min()) return std::numeric_limits<T>::max();
+      return (T)(-x);
+    } else {
+      return (T)(std::numeric_limits<T>::max() - x);
+    }
+  } else {
+    return -x;
+  }
+}
+
+// std::min / std::max as the reference uses them (ties keep the first argument for max
+// when !(a < b), and the first argument for min when !(b < a)).
+template <typename T>
+inline T vmax(T a, T b) { return (a < b) ? b : a; }
+template <typename T>
+inline T vmin(T a, T b) { return (b < a) ? b : a; }
+
+// A (rows x cols) row-major plane.
+template <typename T>
+struct Plane {
+  int64_t rows = 0, cols = 0;
+  std::vector<T> d;
+  Plane() = default;
+  Plane(int64_t r, int64_t c, T v) : rows(r), cols(c), d((size_t)(r * c), v) {}
+  T* row(int64_t y) { return d.data() + y * cols; }
+  const T* row(int64_t y) const { return d.data() + y * cols; }
+};
+
+// copyMakeBorder(src, dst, 1, 1, 1, 1, BORDER_CONSTANT, v)
+template <typename T>
+Plane<T> pad1(const T* src, int64_t H, int64_t W, T v) {
+  Plane<T> p(H + 2, W + 2, v);
+  for (int64_t y = 0; y < H; ++y) std::memcpy(p.row(y + 1) + 1, src + y * W, (size_t)W * sizeof(T));
+  return p;
+}
+
+template <typename T>
+void crop1(const Plane<T>& p, T* dst) {
+  const int64_t H = p.rows - 2, W = p.cols - 2;
+  for (int64_t y = 0; y < H; ++y) std::memcpy(dst + y * W, p.row(y + 1) + 1, (size_t)W * sizeof(T));
+}
+
+// Grayscale reconstruction by dilation of `seeds` under `image`.
+// src/segment/MorphologicOperations.cpp:665-838 (imreconstruct<T>) with the propagation
+// step of MorphologicOperations.cpp:428-439 (propagate<T>).
+template <typename T>
+void imreconstruct(const T* seeds, const T* image, int64_t H, int64_t W, int conn, T* out) {
+  Plane<T> o = pad1<T>(seeds, H, W, (T)0);
+  Plane<T> in = pad1<T>(image, H, W, (T)0);
+  const int64_t C = o.cols;
+  const int64_t maxx = o.cols - 1, maxy = o.rows - 1;
+  T* O = o.d.data();
+  const T* I = in.d.data();
+  std::deque<int64_t> fifo;
+
+  // Raster scan: N+(p) = left, up (and up-left, up-right for 8-connectivity).
+  for (int64_t y = 1; y < maxy; ++y) {
+    T* r = O + y * C;
+    const T* ru = r - C;
+    const T* ir = I + y * C;
+    T left = r[0];
+    for (int64_t x = 1; x < maxx; ++x) {
+      T v = vmax(r[x], vmax(left, ru[x]));
+      if (conn == 8) v = vmax(v, vmax(ru[x + 1], ru[x - 1]));
+      left = vmin(v, ir[x]);
+      r[x] = left;
+    }
+  }
+  // Anti-raster scan: N-(p) = right, down (and down-right, down-left), then seed the FIFO
+  // with every p that could still raise one of its N-(p) neighbours.
+  for (int64_t y = maxy - 1; y > 0; --y) {
+    T* r = O + y * C;
+    T* rd = r + C;
+    const T* ir = I + y * C;
+    const T* ird = ir + C;
+    T right = r[maxx];
+    for (int64_t x = maxx - 1; x > 0; --x) {
+      T v = vmax(r[x], vmax(right, rd[x]));
+      if (conn == 8) v = vmax(v, vmax(rd[x + 1], rd[x - 1]));
+      right = vmin(v, ir[x]);
+      r[x] = right;
+      const T p = r[x];
+      if (r[x + 1] < vmin(p, ir[x + 1]) || rd[x] < vmin(p, ird[x])) {
+        fifo.push_back(y * C + x);
+        continue;
+      }
+      if (conn == 8 && (rd[x + 1] < vmin(p, ird[x + 1]) || rd[x - 1] < vmin(p, ird[x - 1]))) {
+        fifo.push_back(y * C + x);
+      }
+    }
+  }
+  // FIFO propagation.
+  auto propagate = [&](int64_t q, T p) {
+    const T qv = O[q], iv = I[q];
+    if (qv < p && iv != qv) {
+      O[q] = vmin(p, iv);
+      fifo.push_back(q);
+    }
+  };
+  while (!fifo.empty()) {
+    const int64_t i = fifo.front();
+    fifo.pop_front();
+    const int64_t y = i / C, x = i % C;
+    const T p = O[i];
+    if (y > 0) propagate(i - C, p);
+    if (y < maxy) propagate(i + C, p);
+    if (x > 0) propagate(i - 1, p);
+    if (x < maxx) propagate(i + 1, p);
+    if (conn == 8) {
+      if (y > 0) {
+        if (x > 0) propagate(i - C - 1, p);
+        if (x < maxx) propagate(i - C + 1, p);
+      }
+      if (y < maxy) {
+        if (x > 0) propagate(i + C - 1, p);
+        if (x < maxx) propagate(i + C + 1, p);
+      }
+    }
+  }
+  crop1(o, out);
+}
+
+// Binary reconstruction (background 0, foreground != 0; filled pixels get max<T>).
+// src/segment/MorphologicOperations.cpp:1688-1829 (imreconstructBinary<T>) with
+// propagateBinary<T> at 1665-1673.  The marker is not clamped by the mask.
+template <typename T>
+void imreconstruct_binary(const T* seeds, const T* image, int64_t H, int64_t W, int conn, T* out) {
+  Plane<T> o = pad1<T>(seeds, H, W, (T)0);
+  Plane<T> in = pad1<T>(image, H, W, (T)0);
+  const int64_t C = o.cols;
+  const int64_t maxx = o.cols - 1, maxy = o.rows - 1;
+  T* O = o.d.data();
+  const T* I = in.d.data();
+  std::deque<int64_t> fifo;
+  // Contour pixels: marker and mask both non-zero with a zero neighbour in the marker.
+  for (int64_t y = 1; y < maxy; ++y) {
+    for (int64_t x = 1; x < maxx; ++x) {
+      const int64_t i = y * C + x;
+      if (O[i] != 0 && I[i] != 0) {
+        if (O[i - C] == 0 || O[i + C] == 0 || O[i + 1] == 0 || O[i - 1] == 0) {
+          fifo.push_back(i);
+          continue;
+        }
+        if (conn == 8 && (O[i - C - 1] == 0 || O[i - C + 1] == 0 || O[i + C - 1] == 0 || O[i + C + 1] == 0)) {
+          fifo.push_back(i);
+        }
+      }
+    }
+  }
+  const T fg = std::numeric_limits<T>::max();
+  auto propagate = [&](int64_t q) {
+    if (O[q] == 0 && I[q] != 0) {
+      O[q] = fg;
+      fifo.push_back(q);
+    }
+  };
+  while (!fifo.empty()) {
+    const int64_t i = fifo.front();
+    fifo.pop_front();
+    const int64_t y = i / C, x = i % C;
+    if (y > 0) propagate(i - C);
+    if (y < maxy) propagate(i + C);
+    if (x > 0) propagate(i - 1);
+    if (x < maxx) propagate(i + 1);
+    if (conn == 8) {
+      if (y > 0) {
+        if (x > 0) propagate(i - C - 1);
+        if (x < maxx) propagate(i - C + 1);
+      }
+      if (y < maxy) {
+        if (x > 0) propagate(i + C - 1);
+        if (x < maxx) propagate(i + C + 1);
+      }
+    }
+  }
+  crop1(o, out);
+}
+
+// Hole filling.  src/segment/MorphologicOperations.cpp:1859-1926 (imfillHoles<T>): the
+// image is padded with min<T>, the marker is min<T> inside and max<T> on the padding ring,
+// the mask is inverted, reconstructed (binary or grayscale), inverted back and cropped.
+template <typename T>
+void imfill_holes(const T* image, int64_t H, int64_t W, bool binary, int conn, T* out) {
+  const T mn = type_min<T>();
+  const T mx = std::numeric_limits<T>::max();
+  Plane<T> mask = pad1<T>(image, H, W, mn);
+  Plane<T> marker(H + 2, W + 2, mx);
+  for (int64_t y = 1; y <= H; ++y)
+    for (int64_t x = 1; x <= W; ++x) marker.row(y)[x] = mn;
+  for (auto& v : mask.d) v = invert_px(v);
+  Plane<T> rec(H + 2, W + 2, (T)0);
+  if (binary)
+    imreconstruct_binary<T>(marker.d.data(), mask.d.data(), H + 2, W + 2, conn, rec.d.data());
+  else
+    imreconstruct<T>(marker.d.data(), mask.d.data(), H + 2, W + 2, conn, rec.d.data());
+  for (auto& v : rec.d) v = invert_px(v);
+  crop1(rec, out);
+}
+
+// Saturating subtraction as OpenCV's `Mat - scalar` does for 8/16-bit types; for 32-bit
+// integers the result is clamped as well; float is plain subtraction.
+template <typename T>
+inline T sub_sat(T a, T h) {
+  if constexpr (std::numeric_limits<T>::is_integer) {
+    const int64_t r = (int64_t)a - (int64_t)h;
+    if (r < (int64_t)std::numeric_limits<T>::min()) return std::numeric_limits<T>::min();
+    if (r > (int64_t)std::numeric_limits<T>::max()) return std::numeric_limits<T>::max();
+    return (T)r;
+  } else {
+    return a - h;
+  }
+}
+
+// h-minima transform.  src/segment/MorphologicOperations.cpp:2260-2282 (imhmin<T>):
+// invert(imreconstruct(invert(I) - h, invert(I))).
+template <typename T>
+void imhmin(const T* image, int64_t H, int64_t W, T h, int conn, T* out) {
+  const int64_t n = H * W;
+  std::vector<T> mask((size_t)n), marker((size_t)n);
+  for (int64_t i = 0; i < n; ++i) {
+    mask[i] = invert_px(image[i]);
+    marker[i] = sub_sat(mask[i], h);
+  }
+  imreconstruct<T>(marker.data(), mask.data(), H, W, conn, out);
+  for (int64_t i = 0; i < n; ++i) out[i] = invert_px(out[i]);
+}
+
+// src/segment/MorphologicOperations.cpp:1929-1951 (bwselect<T>): binary reconstruction
+// of the image restricted to the seed pixels, ANDed with the image.
+template <typename T>
+void bwselect(const T* image, const T* seeds, int64_t H, int64_t W, int conn, T* out) {
+  const int64_t n = H * W;
+  std::vector<T> marker((size_t)n);
+  for (int64_t i = 0; i < n; ++i) marker[i] = seeds[i] != 0 ? image[i] : (T)0;
+  imreconstruct_binary<T>(marker.data(), image, H, W, conn, out);
+  for (int64_t i = 0; i < n; ++i) out[i] = (T)(out[i] & image[i]);
+}
+
+// ---------------------------------------------------------------------------------------
+// Union-find labelling.  src/segment/ConnComponents.cpp.
+
+// ConnComponents::find (24-32) with path compression, written iteratively.
+inline int32_t uf_find(int32_t* L, int32_t x) {
+  int32_t r = x;
+  while (L[r] != r) r = L[r];
+  while (L[x] != r) {
+    int32_t n = L[x];
+    L[x] = r;
+    x = n;
+  }
+  return r;
+}
+
+// ConnComponents::merge (34-43): the root with the smaller index wins.
+inline void uf_merge(int32_t* L, int32_t a, int32_t b) {
+  a = uf_find(L, a);
+  b = uf_find(L, b);
+  if (a < b) L[b] = a;
+  else if (a > b) L[a] = b;
+}
+
+// ConnComponents::label (52-86): equal-valued non-zero neighbours are joined; background
+// gets bgval; every foreground pixel ends with the smallest raster index of its component
+// (ConnComponents::flatten, 137-148).
+inline void cc_label(const uint8_t* img, int64_t W, int64_t H, int32_t* L, int32_t bgval, int conn) {
+  const int64_t n = W * H;
+  for (int64_t i = 0; i < n; ++i) L[i] = (int32_t)i;
+  for (int64_t y = 0; y < H; ++y) {
+    for (int64_t x = 0; x < W; ++x) {
+      const int64_t i = y * W + x;
+      const uint8_t p = img[i];
+      if (p == 0) {
+        L[i] = bgval;
+        continue;
+      }
+      if (x > 0 && p == img[i - 1]) uf_merge(L, (int32_t)i, (int32_t)(i - 1));
+      if (y > 0 && p == img[i - W]) uf_merge(L, (int32_t)i, (int32_t)(i - W));
+      if (conn == 8) {
+        if (y > 0 && x > 0 && p == img[i - W - 1]) uf_merge(L, (int32_t)i, (int32_t)(i - W - 1));
+        if (y > 0 && x < W - 1 && p == img[i - W + 1]) uf_merge(L, (int32_t)i, (int32_t)(i - W + 1));
+      }
+    }
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    if (L[i] == bgval) continue;
+    int32_t r = (int32_t)i;
+    while (L[r] != r) r = L[r];
+    L[i] = r;
+  }
+}
+
+// ConnComponents::relabel (89-118): roots numbered 1..n in raster order, bgval -> 0.
+inline int32_t cc_relabel(int64_t W, int64_t H, int32_t* L, int32_t bgval) {
+  const int64_t n = W * H;
+  std::vector<int32_t> id((size_t)n, 0);
+  int32_t j = 1;
+  for (int64_t i = 0; i < n; ++i)
+    if (L[i] == (int32_t)i) id[i] = j++;
+  for (int64_t i = 0; i < n; ++i) L[i] = (L[i] == bgval) ? 0 : id[L[i]];
+  return j - 1;
+}
+
+// ConnComponents::areaThresholdLabeled (205-239): keep labels whose pixel count is in
+// [lower, upper); the rest become bgval.  Returns the number kept.
+inline int32_t cc_area_threshold_labeled(const int32_t* L, int64_t W, int64_t H, int32_t* out,
+                                         int32_t bgval, int32_t lower, int32_t upper) {
+  const int64_t n = W * H;
+  // Labels are raster indices here (or any value < n); count with a dense array where
+  // possible, otherwise sort.
+  std::vector<int64_t> keys;
+  keys.reserve(1024);
+  std::vector<int32_t> area;
+  bool dense = true;
+  for (int64_t i = 0; i < n; ++i)
+    if (L[i] != bgval && (L[i] < 0 || L[i] >= n)) dense = false;
+  int32_t kept = 0;
+  if (dense) {
+    area.assign((size_t)n, 0);
+    for (int64_t i = 0; i < n; ++i)
+      if (L[i] != bgval) ++area[L[i]];
+    for (int64_t i = 0; i < n; ++i)
+      if (area[i] > 0 && area[i] >= lower && area[i] < upper) ++kept;
+    for (int64_t i = 0; i < n; ++i) {
+      const int32_t l = L[i];
+      out[i] = (l != bgval && area[l] >= lower && area[l] < upper) ? l : bgval;
+    }
+    return kept;
+  }
+  std::vector<int32_t> s;
+  for (int64_t i = 0; i < n; ++i)
+    if (L[i] != bgval) s.push_back(L[i]);
+  std::sort(s.begin(), s.end());
+  std::vector<std::pair<int32_t, int32_t>> runs;
+  for (size_t a = 0; a < s.size();) {
+    size_t b = a;
+    while (b < s.size() && s[b] == s[a]) ++b;
+    runs.push_back({s[a], (int32_t)(b - a)});
+    if ((int32_t)(b - a) >= lower && (int32_t)(b - a) < upper) ++kept;
+    a = b;
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    out[i] = bgval;
+    if (L[i] == bgval) continue;
+    auto it = std::lower_bound(runs.begin(), runs.end(), std::make_pair(L[i], (int32_t)-1));
+    if (it->second >= lower && it->second < upper) out[i] = L[i];
+  }
+  return kept;
+}
+
+// src/segment/MorphologicOperations.cpp:2012-2035 (bwlabel2).
+inline int32_t bwlabel2(const uint8_t* bin, int64_t H, int64_t W, int conn, bool relab, int32_t* out) {
+  cc_label(bin, W, H, out, -1, conn);
+  if (relab) return cc_relabel(W, H, out, -1);
+  return 0;
+}
+
+// src/segment/MorphologicOperations.cpp:2199-2232 (bwareaopen2): label (unless already
+// labelled), keep areas in [minSize, maxSize), optionally flatten to 255 / 0 (`> -1`).
+inline int32_t bwareaopen2(const void* image, bool labeled, bool flatten, int32_t minSize,
+                           int32_t maxSize, int conn, int64_t H, int64_t W, int32_t* labels_out,
+                           uint8_t* flat_out) {
+  const int64_t n = H * W;
+  std::vector<int32_t> lab((size_t)n);
+  if (!labeled) cc_label((const uint8_t*)image, W, H, lab.data(), -1, conn);
+  else std::memcpy(lab.data(), image, (size_t)n * sizeof(int32_t));
+  std::vector<int32_t> kept((size_t)n);
+  int32_t count = cc_area_threshold_labeled(lab.data(), W, H, kept.data(), -1, minSize, maxSize);
+  if (labels_out) std::memcpy(labels_out, kept.data(), (size_t)n * sizeof(int32_t));
+  if (flatten && flat_out)
+    for (int64_t i = 0; i < n; ++i) flat_out[i] = kept[i] > -1 ? 255 : 0;
+  return count;
+}
+
+// `Mat > k` (HistologicalEntities.cpp:214): 255 where strictly greater, else 0.
+template <typename T>
+inline void threshold_gt(const T* in, int64_t n, T k, uint8_t* out) {
+  for (int64_t i = 0; i < n; ++i) out[i] = in[i] > k ? 255 : 0;
+}
+
+}  // namespace orc

@@ -1,0 +1,38 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "emory-cci-fast-ia-gsoc_gb300")
+for p in (ROOT, PKG, os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); runs the device library")
+    config.addinivalue_line("markers", "slow: large full-size cases")
+
+
+@pytest.fixture(scope="session")
+def nsgb():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.fail("GPU test collected without a CUDA device")
+    import nsgb as m
+
+    return m
+
+
+@pytest.fixture(scope="session")
+def oracle():
+    import oracle as o
+
+    return o
+
+
+@pytest.fixture(scope="session")
+def golden_dir():
+    return os.path.join(ROOT, "tests", "golden")

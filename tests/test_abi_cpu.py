@@ -1,0 +1,62 @@
+"""CPU-only checks of the device library boundary: it loads without a GPU, exports every
+entry point declared in include/*.h, and its host-only helpers behave."""
+import ctypes
+import glob
+import os
+import re
+
+from conftest import ROOT
+
+LIB = os.path.join(ROOT, "emory-cci-fast-ia-gsoc_gb300", "lib", "libnsgb.so")
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        txt = open(h).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        for m in re.finditer(r"\b(nsgb_[a-z0-9_]+)\s*\(", txt):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(LIB)
+    names = declared_symbols()
+    assert len(names) >= 15
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_declares_every_symbol():
+    import nsgb._ffi as ffi
+
+    assert declared_symbols() <= set(ffi.EXPORTED) | {"nsgb_stream_t"}
+
+
+def test_status_strings_and_workspace_sizes():
+    import nsgb._ffi as ffi
+
+    lib = ffi.lib
+    assert lib.nsgb_status_string(0) == b"ok"
+    assert b"workspace" in lib.nsgb_status_string(3)
+    for op in range(8):
+        for dt in range(4):
+            assert lib.nsgb_workspace_size(op, dt, 64, 64) > 0
+    assert lib.nsgb_workspace_size(0, 0, 0, 10) == 0
+    big = lib.nsgb_workspace_size(7, 0, 4096, 4096)
+    assert big > 3 * 4 * 4096 * 4096
+
+
+def test_argument_errors_need_no_gpu():
+    import nsgb._ffi as ffi
+
+    lib = ffi.lib
+    # Invalid dtype / null pointers / bad connectivity are rejected before any CUDA call.
+    assert lib.nsgb_imreconstruct(9, 1, 1, 4, 4, 4, 8, 0, 1, 1 << 20, None, None) == 2
+    assert lib.nsgb_imreconstruct(0, None, 1, 4, 4, 4, 8, 0, 1, 1 << 20, None, None) == 1
+    assert lib.nsgb_imreconstruct(0, 1, 1, 4, 4, 4, 6, 0, 1, 1 << 20, None, None) == 1
+    assert lib.nsgb_imreconstruct(0, 1, 1, 4, 4, 3, 8, 0, 1, 1 << 20, None, None) == 1
+    assert lib.nsgb_imreconstruct(0, 1, 1, 4, 4, 4, 8, 0, None, 0, None, None) == 3
+    assert lib.nsgb_bwlabel(None, 1, 4, 4, 4, 16, 8, 1, None, 1, 1 << 20, None, None) == 1
+    assert lib.nsgb_imhmin(2, 1, 2, 4, 4, 16, 1.0, 8, 1, 1 << 20, None, None) == 2

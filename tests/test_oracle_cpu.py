@@ -1,0 +1,221 @@
+"""Pins the CPU oracle (oracle/) before it is trusted as the checker of the GPU path.
+
+* union-find labelling: exact match with the reference's own ConnComponents.cpp, through the
+  committed fixtures (tests/golden/ref_ccl_cases.npz) and, where oracle/_ref was built, live;
+* reconstruction: the reference's inline 32x32 queue fixture, and an independent numpy
+  fixed-point definition (Jacobi iteration to convergence) on random small images, including
+  the 0-valued padding ring and odd / non-square sizes;
+* hole filling, bwselect, binary reconstruction, h-minima: independent scipy / numpy
+  formulations.
+"""
+import os
+
+import numpy as np
+import pytest
+import scipy.ndimage as ndi
+
+from conftest import ROOT  # noqa: F401
+
+
+# ---------------------------------------------------------------------------------------
+# Independent definitions (numpy), small sizes only.
+def struct(conn):
+    return ndi.generate_binary_structure(2, 1 if conn == 4 else 2)
+
+
+def np_recon(marker, mask, conn, erode=False, ring=True):
+    """Fixed point of R = max(R, min(nbr_max(R), mask)) over the image padded with a fixed
+    0 ring (the reference's copyMakeBorder(..., 0)); erode = the dual without a ring."""
+    if erode:
+        if np.issubdtype(mask.dtype, np.floating):
+            return -np_recon(-marker, -mask, conn, False, ring)
+        if np.issubdtype(mask.dtype, np.signedinteger):
+            return ~np_recon(~marker, ~mask, conn, False, ring)
+        mx = np.iinfo(mask.dtype).max
+        return (mx - np_recon((mx - marker).astype(mask.dtype), (mx - mask).astype(mask.dtype), conn, False,
+                              ring)).astype(mask.dtype)
+    H, W = mask.shape
+    low = np.finfo(mask.dtype).min if np.issubdtype(mask.dtype, np.floating) else np.iinfo(mask.dtype).min
+    pad_v = 0 if ring else low
+    K = np.full((H + 2, W + 2), pad_v, mask.dtype)
+    K[1:-1, 1:-1] = mask
+    R = np.full((H + 2, W + 2), pad_v, mask.dtype)
+    R[1:-1, 1:-1] = np.minimum(marker, mask)
+    fp = struct(conn)
+    while True:
+        D = ndi.grey_dilation(R, footprint=fp, mode="constant", cval=low)
+        N = R.copy()
+        N[1:-1, 1:-1] = np.maximum(R[1:-1, 1:-1], np.minimum(D[1:-1, 1:-1], K[1:-1, 1:-1]))
+        if np.array_equal(N, R):
+            return R[1:-1, 1:-1]
+        R = N
+
+
+def np_binary_recon(marker, mask, conn):
+    lab, _ = ndi.label(mask != 0, structure=struct(conn))
+    seeded = np.unique(lab[(marker != 0) & (mask != 0)])
+    seeded = seeded[seeded > 0]
+    filled = np.isin(lab, seeded) & (mask != 0) & (marker == 0)
+    out = marker.copy()
+    out[filled] = np.iinfo(mask.dtype).max
+    return out
+
+
+def np_fill_binary(img, conn):
+    mx = np.iinfo(img.dtype).max
+    cls = img != mx
+    lab, _ = ndi.label(cls, structure=struct(conn))
+    border = np.unique(np.concatenate([lab[0], lab[-1], lab[:, 0], lab[:, -1]]))
+    border = border[border > 0]
+    reach = np.isin(lab, border)
+    return np.where(reach, 0, mx).astype(img.dtype)
+
+
+def rand_gray(rng, h, w, dtype, levels=6):
+    if dtype == np.float32:
+        return rng.random((h, w)).astype(np.float32)
+    base = rng.integers(0, levels, (h, w))
+    if dtype == np.uint8:
+        return (base * 40).astype(np.uint8)
+    if dtype == np.uint16:
+        return (base * 10000).astype(np.uint16)
+    return (base * 1000 - 1500).astype(np.int32)  # includes negatives: exercises the ring
+
+
+SHAPES = [(1, 1), (1, 9), (9, 1), (5, 7), (13, 31), (33, 17), (40, 40)]
+
+
+# ---------------------------------------------------------------------------------------
+def test_labels_match_reference_fixtures(oracle, golden_dir):
+    d = np.load(os.path.join(golden_dir, "ref_ccl_cases.npz"))
+    k = 0
+    while f"img{k}" in d:
+        img = d[f"img{k}"]
+        for conn in (4, 8):
+            lab, _ = oracle.bwlabel2(img, conn, relab=False)
+            rel, n = oracle.bwlabel2(img, conn, relab=True)
+            assert np.array_equal(lab, d[f"lab{k}_{conn}"]), (k, conn)
+            assert np.array_equal(rel, d[f"rel{k}_{conn}"]), (k, conn)
+            assert n == int(d[f"n{k}_{conn}"])
+            kept, nk = oracle.bwareaopen2(lab, True, False, 3, 40, conn)
+            assert np.array_equal(kept, d[f"kept{k}_{conn}"]) and nk == int(d[f"nk{k}_{conn}"])
+        k += 1
+    assert k >= 30
+
+
+def test_labels_match_reference_live(oracle):
+    if not oracle.ref_available():
+        pytest.skip("reference ConnComponents not built here (oracle/_ref)")
+    rng = np.random.default_rng(7)
+    for trial in range(40):
+        h, w = rng.integers(1, 90, 2)
+        img = (rng.integers(0, 3, (h, w)) * 100).astype(np.uint8)
+        for conn in (4, 8):
+            a, n = oracle.bwlabel2(img, conn, True)
+            b, m = oracle.ref_label(img, conn, True)
+            assert n == m and np.array_equal(a, b)
+
+
+def test_recon_reference_queue_fixture(oracle, golden_dir):
+    d = np.load(os.path.join(golden_dir, "ref_fixture_32.npz"))
+    image = d["image"].astype(np.int32)
+    seeds = d["seeds"].astype(np.int32)
+    assert sorted(int(v) for v in d["seed_list"]) == sorted(int(v) for v in np.flatnonzero(seeds))
+    for conn in (4, 8):
+        out = oracle.imreconstruct(seeds, image, conn)
+        assert np.array_equal(out, d[f"expected{conn}"])
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.uint16, np.int32, np.float32])
+@pytest.mark.parametrize("conn", [4, 8])
+def test_recon_matches_fixed_point_definition(oracle, dtype, conn):
+    rng = np.random.default_rng(11 + conn)
+    for (h, w) in SHAPES:
+        mask = rand_gray(rng, h, w, dtype)
+        marker = rand_gray(rng, h, w, dtype)  # not <= mask: exercises min(marker, mask)
+        got = oracle.imreconstruct(marker, mask, conn)
+        exp = np_recon(marker, mask, conn)
+        assert np.array_equal(got, exp), (h, w)
+        assert (got <= mask).all() and (got >= np.minimum(marker, mask)).all()
+        assert np.array_equal(oracle.imreconstruct(got, mask, conn), got)  # idempotent
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.uint16, np.int32])
+@pytest.mark.parametrize("conn", [4, 8])
+def test_binary_recon_and_bwselect(oracle, dtype, conn):
+    rng = np.random.default_rng(5)
+    mx = np.iinfo(dtype).max
+    for (h, w) in SHAPES:
+        mask = (rng.random((h, w)) < 0.55).astype(dtype) * mx
+        marker = (rng.random((h, w)) < 0.08).astype(dtype) * 7
+        assert np.array_equal(oracle.imreconstruct_binary(marker, mask, conn), np_binary_recon(marker, mask, conn))
+        seeds = (rng.random((h, w)) < 0.1).astype(dtype)
+        sel = oracle.bwselect(mask, seeds, conn)
+        exp = np_binary_recon(np.where(seeds != 0, mask, 0).astype(dtype), mask, conn) & mask
+        assert np.array_equal(sel, exp)
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.uint16])
+@pytest.mark.parametrize("conn", [4, 8])
+def test_fill_holes_binary(oracle, dtype, conn):
+    rng = np.random.default_rng(3)
+    mx = np.iinfo(dtype).max
+    for (h, w) in SHAPES:
+        img = (rng.random((h, w)) < 0.5).astype(dtype) * mx
+        got = oracle.imfill_holes(img, True, conn)
+        assert np.array_equal(got, np_fill_binary(img, conn))
+        # 0/max input: the usual scipy hole filling (background connectivity = conn)
+        exp = ndi.binary_fill_holes(img != 0, structure=struct(conn)).astype(dtype) * mx
+        assert np.array_equal(got, exp)
+
+
+def test_fill_holes_binary_int32_is_constant(oracle):
+    img = (np.random.default_rng(0).random((9, 11)) < 0.5).astype(np.int32) * 255
+    got = oracle.imfill_holes(img, True, 4)
+    assert (got == np.iinfo(np.int32).max).all()
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.uint16, np.int32, np.float32])
+@pytest.mark.parametrize("conn", [4, 8])
+def test_fill_holes_gray_is_border_erosion(oracle, dtype, conn):
+    rng = np.random.default_rng(9)
+    for (h, w) in SHAPES:
+        img = rand_gray(rng, h, w, dtype)
+        if dtype == np.int32:
+            img = np.abs(img).astype(np.int32)
+        got = oracle.imfill_holes(img, False, conn)
+        top = np.finfo(dtype).max if dtype == np.float32 else np.iinfo(dtype).max
+        marker = np.full_like(img, top)
+        marker[0], marker[-1], marker[:, 0], marker[:, -1] = img[0], img[-1], img[:, 0], img[:, -1]
+        exp = np_recon(marker, img, conn, erode=True, ring=False)
+        assert np.array_equal(got, exp), (h, w)
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.float32])
+def test_hmin(oracle, dtype):
+    rng = np.random.default_rng(4)
+    for (h, w) in SHAPES:
+        img = rand_gray(rng, h, w, dtype)
+        hv = 30 if dtype == np.uint8 else 0.25
+        got = oracle.imhmin(img, hv, 8)
+        if dtype == np.uint8:
+            inv = (255 - img).astype(np.uint8)
+            mk = np.maximum(inv.astype(int) - hv, 0).astype(np.uint8)
+            exp = (255 - np_recon(mk, inv, 8)).astype(np.uint8)
+        else:
+            exp = -np_recon((-img - np.float32(hv)).astype(np.float32), -img, 8)
+        assert np.array_equal(got, exp)
+
+
+def test_chain_small(oracle):
+    from nsgb import synth
+
+    mask, marker = synth.tile_u8(96, 80, 12, 1)
+    r = oracle.chain(marker, mask)
+    assert np.array_equal(r["recon"], oracle.imreconstruct(marker, mask, 8))
+    assert np.array_equal(r["thr"], np.where(r["recon"] > 128, 255, 0))
+    assert np.array_equal(r["fill"], oracle.imfill_holes(r["thr"], True, 4))
+    lab, n = oracle.bwlabel2(r["fill"], 8, True)
+    assert np.array_equal(r["labels"], lab) and n == r["n_labels"]
+    a, k = oracle.bwareaopen2(r["fill"], False, True, 11, 1000, 8)
+    assert np.array_equal(r["area"], a) and k == r["n_kept"]
