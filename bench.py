@@ -224,8 +224,6 @@ def run_nsgb(args):
     ev_rb = torch.cuda.Event(enable_timing=True)
     ev_re = torch.cuda.Event(enable_timing=True)
     opts = _ffi.Opts(0, 0, 0)
-    opts.recon_event_begin = C.c_void_p(ev_rb.cuda_event)
-    opts.recon_event_end = C.c_void_p(ev_re.cuda_event)
 
     def chain_call(o):
         st = lib.nsgb_chain(_ffi.U8, work.data_ptr(), mask.data_ptr(), H, W, W, 8, 128.0, 4, 8, 11, 1000,
@@ -241,8 +239,23 @@ def run_nsgb(args):
         chain_call(opts)
         ev1.record(stream)
 
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    rec = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    def new_events(n):
+        # torch creates the CUDA event on first record(); record once so the handle exists
+        # before it is handed to the C ABI.
+        out = []
+        for _ in range(n):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            b.record(stream)
+            out.append((a, b))
+        return out
+
+    evs = new_events(args.steps)
+    rec = new_events(args.steps)
+    ev_rb.record(stream)
+    ev_re.record(stream)
+    opts.recon_event_begin = C.c_void_p(ev_rb.cuda_event)
+    opts.recon_event_end = C.c_void_p(ev_re.cuda_event)
     w0, w1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     for _ in range(max(args.warmup, 3)):
         step(w0, w1)

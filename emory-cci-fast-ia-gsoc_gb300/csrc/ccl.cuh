@@ -30,11 +30,17 @@ namespace ccl {
 constexpr int kTile = 32;      // tile edge (pixels)
 constexpr int kThreads = 256;  // 32 x 8 threads, 4 rows each
 
+// Root of x in a shared-memory forest, halving the path on the way (every node on it is
+// re-pointed to its grandparent; a concurrent hook of a root is never overwritten because
+// roots are not written here).
 __device__ __forceinline__ int s_find(volatile int* s, int x) {
   for (;;) {
     const int p = s[x];
     if (p == x) return x;
-    x = p;
+    const int g = s[p];
+    if (g == p) return p;
+    s[x] = g;
+    x = g;
   }
 }
 
@@ -54,11 +60,17 @@ __device__ __forceinline__ void s_union(int* s, int a, int b) {
   }
 }
 
-__device__ __forceinline__ int g_find(const int* L, int x) {
+// Root of x in the global forest with path halving.  The halving write is an atomicMin: a
+// parent link only ever moves to a smaller index (an ancestor), so it can never undo another
+// thread's write of the root itself (the smallest index on the path).
+__device__ __forceinline__ int g_find(int* L, int x) {
   for (;;) {
     const int p = ld_relaxed(L + x);
     if (p == x) return x;
-    x = p;
+    const int g = ld_relaxed(L + p);
+    if (g == p) return p;
+    atomicMin(L + x, g);
+    x = g;
   }
 }
 
@@ -80,6 +92,12 @@ __device__ __forceinline__ void g_union(int* L, int a, int b) {
 
 // L: dense H x W int32 (index y*W + x).  A (optional): dense int32, receives each local root's
 // pixel count at the root and 0 elsewhere.
+//
+// Each warp owns tile rows (lane = column).  Runs of equal class along a row are found with a
+// ballot and start out joined (label = run start), so unions are only needed where runs of
+// adjacent rows touch: at a pixel that starts its run or sits under the start of a run above
+// (and, for 8-connectivity, diagonally past the two ends of the run).  That is one union per
+// touching pair of runs instead of one per pixel pair.
 template <class Cls, int CONN>
 __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, int H, int W, int* __restrict__ L,
                                                       int* __restrict__ A) {
@@ -88,26 +106,42 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, int H, int W, int
   __shared__ uint8_t s_c[kTile * kTile];
   const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  uint8_t c[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int ly = ty + 8 * k, i = ly * kTile + tx;
     const int gy = y0 + ly, gx = x0 + tx;
-    const uint32_t c = (gy < H && gx < W) ? cls(gy, gx) : 0u;
-    s_c[i] = (uint8_t)c;
-    s_lab[i] = c ? i : -1;
+    c[k] = (uint8_t)((gy < H && gx < W) ? cls(gy, gx) : 0u);
+    s_c[i] = c[k];
     s_cnt[i] = 0;
+  }
+  __syncwarp();
+  unsigned same_left[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int ly = ty + 8 * k, i = ly * kTile + tx;
+    const uint8_t left = __shfl_up_sync(NSGB_FULL, c[k], 1);
+    same_left[k] = __ballot_sync(NSGB_FULL, tx > 0 && c[k] != 0 && left == c[k]);
+    // run start: highest lane <= tx whose pixel does not continue a run from the left
+    const unsigned starts = ~same_left[k] & (0xFFFFFFFFu >> (31 - tx));
+    const int rs = 31 - __clz(starts);
+    s_lab[i] = c[k] ? ly * kTile + rs : -1;
   }
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int ly = ty + 8 * k, i = ly * kTile + tx;
-    const uint8_t c = s_c[i];
-    if (!c) continue;
-    if (tx > 0 && s_c[i - 1] == c) s_union(s_lab, i, i - 1);
-    if (ly > 0 && s_c[i - kTile] == c) s_union(s_lab, i, i - kTile);
-    if (CONN == 8 && ly > 0) {
-      if (tx > 0 && s_c[i - kTile - 1] == c) s_union(s_lab, i, i - kTile - 1);
-      if (tx < kTile - 1 && s_c[i - kTile + 1] == c) s_union(s_lab, i, i - kTile + 1);
+    const uint8_t v = c[k];
+    if (!v || ly == 0) continue;
+    const bool run_start = !((same_left[k] >> tx) & 1u);
+    const int u = i - kTile;
+    const uint8_t up = s_c[u];
+    const bool up_start = up != 0 && !(tx > 0 && s_c[u - 1] == up);
+    if (up == v && (run_start || up_start)) s_union(s_lab, i, u);
+    if (CONN == 8) {
+      if (run_start && tx > 0 && s_c[u - 1] == v) s_union(s_lab, i, u - 1);
+      const bool run_end = (tx == kTile - 1) || s_c[i + 1] != v;
+      if (run_end && tx < kTile - 1 && s_c[u + 1] == v) s_union(s_lab, i, u + 1);
     }
   }
   __syncthreads();
@@ -115,7 +149,7 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, int H, int W, int
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int ly = ty + 8 * k, i = ly * kTile + tx;
-    root[k] = s_c[i] ? s_find(s_lab, i) : -1;
+    root[k] = c[k] ? s_find(s_lab, i) : -1;
   }
   if (A) {
 #pragma unroll
@@ -190,10 +224,10 @@ __global__ void ccl_flatten(int H, int W, int* __restrict__ L, int* __restrict__
                             unsigned* __restrict__ bits) {
   const int64_t n = (int64_t)H * W;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int l = L[i];
+    const int l = ld_relaxed(L + i);
     if (l < 0) continue;
     const int r = g_find(L, l);
-    if (r != l) L[i] = r;
+    if (r != l) atomicMin(L + i, r);
     if (A) {
       const int a = A[i];
       if (a > 0 && r != (int)i) atomicAdd(&A[r], a);
@@ -208,8 +242,10 @@ __global__ void ccl_flatten(int H, int W, int* __restrict__ L, int* __restrict__
   }
 }
 
+// Read-only in the kernels that call it, so the L1-cached path is used: a giant component's
+// root word is read by every pixel and would otherwise hammer one L2 line.
 __device__ __forceinline__ bool test_bit(const unsigned* bits, int r) {
-  return (__ldcg(&bits[r >> 5]) >> (r & 31)) & 1u;
+  return (__ldg(&bits[r >> 5]) >> (r & 31)) & 1u;
 }
 
 // Host helpers (ccl.cu).

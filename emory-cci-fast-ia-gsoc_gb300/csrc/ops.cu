@@ -130,9 +130,12 @@ __global__ void label_out_kernel(int H, int W, const int* __restrict__ L, const 
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
     const int l = __ldcg(&L[i]);
-    if (labels) *pxp(labels, pitch_labels, y, x) = relabel ? (l < 0 ? 0 : __ldcg(&rank[l]) + 1) : l;
+    // rank / A are read-only here: L1-cached loads (a giant component's root is read by
+    // every one of its pixels).
+    if (labels) *pxp(labels, pitch_labels, y, x) = relabel ? (l < 0 ? 0 : __ldg(&rank[l]) + 1) : l;
     if (A) {
-      const bool keep = l >= 0 && __ldcg(&A[l]) >= lo && __ldcg(&A[l]) < hi;
+      const int a = l >= 0 ? __ldg(&A[l]) : 0;
+      const bool keep = l >= 0 && a >= lo && a < hi;
       if (kept_labels) *pxp(kept_labels, pitch_kept, y, x) = keep ? l : -1;
       if (flat) *pxp(flat, pitch_flat, y, x) = keep ? 255 : 0;
     }
@@ -161,7 +164,8 @@ __global__ void labeled_area_out_kernel(const int32_t* lab, int64_t pitch, int H
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
     const int l = px(lab, pitch, y, x);
-    const bool keep = l >= 0 && (int64_t)l < n && __ldcg(&A[l]) >= lo && __ldcg(&A[l]) < hi;
+    const int a = (l >= 0 && (int64_t)l < n) ? __ldg(&A[l]) : 0;
+    const bool keep = l >= 0 && (int64_t)l < n && a >= lo && a < hi;
     if (kept_labels) *pxp(kept_labels, pitch_kept, y, x) = keep ? l : -1;
     if (flat) *pxp(flat, pitch_flat, y, x) = keep ? 255 : 0;
   }
@@ -338,7 +342,7 @@ cudaError_t recon_timed(const nsgb_opts* o, int dtype, void* out, const void* ma
                         int64_t W, int64_t pitch, int conn, bool erode, bool ring, void* ws, cudaStream_t s) {
   cudaError_t e = record(o, true, s);
   if (e != cudaSuccess) return e;
-  e = recon_launch(dtype, out, marker, mask, H, W, pitch, conn, erode, ring, ws, s, o ? o->max_rounds : 0,
+  e = recon_launch(dtype, out, marker, mask, H, W, pitch, conn, erode, ring, ws, s, o ? o->max_visits_per_tile : 0,
                    o ? o->max_visit_iters : 0);
   if (e != cudaSuccess) return e;
   return record(o, false, s);
@@ -502,7 +506,7 @@ nsgb_status nsgb_imfill_holes(int dtype, const void* image, void* out, int64_t r
     case NSGB_I32: fill_marker_kernel<int32_t><<<grid1d(rows * cols), 256, 0, s>>>((const int32_t*)image, (int32_t*)out, pitch, H, W); break;
     case NSGB_F32: fill_marker_kernel<float><<<grid1d(rows * cols), 256, 0, s>>>((const float*)image, (float*)out, pitch, H, W); break;
   }
-  e = recon_launch(dtype, out, out, image, rows, cols, pitch, conn, true, false, ws, s, opts ? opts->max_rounds : 0,
+  e = recon_launch(dtype, out, out, image, rows, cols, pitch, conn, true, false, ws, s, opts ? opts->max_visits_per_tile : 0,
                    opts ? opts->max_visit_iters : 0);
   return finish(e, ws, s, opts);
 }
@@ -526,7 +530,7 @@ nsgb_status nsgb_imhmin(int dtype, const void* image, void* out, int64_t rows, i
   // invert(recon(invert(I) - h, invert(I))): the order-reversed reconstruction with the
   // reference's 0-valued padding ring taken in the inverted domain.
   cudaError_t e = recon_launch(dtype, out, out, image, rows, cols, pitch, conn, true, true, ws, s,
-                               opts ? opts->max_rounds : 0, opts ? opts->max_visit_iters : 0);
+                               opts ? opts->max_visits_per_tile : 0, opts ? opts->max_visit_iters : 0);
   return finish(e, ws, s, opts);
 }
 

@@ -15,16 +15,22 @@
 //     right and back, a clamp-composition scan) on a transposed copy, then a column pass (down
 //     and up, with the diagonals for 8-connectivity), repeated until a column pass changes
 //     nothing.  min/max run as max.u16x2 / min.u16x2 on pairs of pixels.
-//   * One persistent cooperative kernel runs all visits.  Round 0 visits every tile; a visit
-//     that could raise a pixel of a neighbouring tile puts that tile on the next round's work
-//     list (deduplicated with round stamps); a neighbour already queued for the current round
-//     and not yet started is skipped because it will read the new values.  Rounds are
-//     separated by a bounded grid barrier; the kernel ends when a round queues nothing.
+//   * One persistent cooperative kernel runs all visits from a device work queue (a bounded
+//     multi-producer / multi-consumer ring with per-slot sequence numbers).  Every tile starts
+//     queued in raster order.  Each tile has a state IDLE / QUEUED / RUNNING / RUNNING_DIRTY:
+//     a visit that could raise a pixel of a neighbouring tile queues it if it is idle, marks
+//     it dirty if it is running (its owner re-runs it before releasing it), and leaves it
+//     alone if it is already queued (it has not loaded its halo yet and will read the new
+//     values).  A tile is therefore processed by one warp at a time and as soon as it can
+//     change; `pending` counts queued and running tiles and the kernel ends when it reaches 0.
+//     Stores and state reads / writes are separated by SC fences on both sides, so a neighbour
+//     either sees the new values or is re-run.
 //
 // Every wait is bounded (status NSGB_ERR_TIMEOUT), and the per-visit sweep count and the
-// number of rounds are capped (status NSGB_ERR_NOT_CONVERGED).
+// total number of visits are capped (status NSGB_ERR_NOT_CONVERGED).
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include "common.cuh"
 #include "recon.cuh"
@@ -45,28 +51,35 @@ struct alignas(16) WarpBuf {
   uint32_t c0[32], c1[32];  // final first / last tile column, for the neighbour test
 };
 
+enum TileState : int { kIdle = 0, kQueued = 1, kRunning = 2, kRunningDirty = 3 };
+
+struct Slot {
+  int val;
+  unsigned seq;
+};
+
 struct Ctl {
-  int* enq;     // [ntiles] round in which the tile is next scheduled
-  int* start;   // [ntiles] last round in which the tile was started
-  int* list0;   // [ntiles]
-  int* list1;   // [ntiles]
-  int* claim;   // [3] per-round claim counters (slot = round % 3)
-  int* count;   // [3] per-round list lengths
-  unsigned* bar;  // [2] grid barrier
+  int* state;         // [ntiles] TileState
+  Slot* slots;        // [cap] work ring
+  unsigned* head;     // consumer ticket counter
+  unsigned* tail;     // producer ticket counter
+  int* pending;       // queued + running tiles
   int* status;
-  int* stats;   // [0] rounds, [1] visits, [2] sweeps
+  int* stats;         // [0] visits, [1] sweeps, [2] re-runs
+  unsigned long long* visit_count;  // budget counter
+  unsigned cap;       // ring capacity (power of two >= ntiles)
+  long long max_visits;
 };
 
 template <typename T>
 struct Args {
-  T* out;
-  const T* marker;
+  T* out;          // reconstructed in place (holds the marker on entry)
   const T* mask;
-  int64_t pitch;  // bytes, shared by the three planes
+  int64_t pitch;   // bytes, shared by both planes
   int H, W;
   int tiles_x, tiles_y, ntiles;
   int flip, ring, aligned;
-  int max_rounds, max_iters;
+  int max_iters;
   Ctl c;
 };
 
@@ -327,20 +340,72 @@ __device__ __forceinline__ uint32_t col_pass(uint32_t (&O)[32], const WarpBuf& B
   return acc;
 }
 
-__device__ __forceinline__ void mark_tile(const Ctl& c, int nt, int round) {
-  if (round > 0) {
-    // Queued for this round and not started: it will read the values just written.
-    if (ld_relaxed(&c.enq[nt]) == round && ld_relaxed(&c.start[nt]) < round) return;
+__device__ __forceinline__ void st_release_u(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Producer side of the ring (Vyukov's bounded queue): wait until slot `p` is free for this
+// lap, fill it, publish it.
+__device__ __forceinline__ bool queue_push(const Ctl& c, int t) {
+  const unsigned p = atomicAdd(c.tail, 1u);
+  Slot* sl = &c.slots[p & (c.cap - 1)];
+  long long spins = 0;
+  while (ld_acquire_u(&sl->seq) != p) {
+    if (++spins > kSpinLimit || ld_relaxed(c.status) != 0) {
+      set_status(c.status, kDevTimeout);
+      return false;
+    }
+    __nanosleep(64);
   }
-  if (atomicMax(&c.enq[nt], round + 1) < round + 1) {
-    int* next = ((round + 1) & 1) ? c.list1 : c.list0;
-    const int idx = atomicAdd(&c.count[(round + 1) % 3], 1);
-    next[idx] = nt;
+  sl->val = t;
+  st_release_u(&sl->seq, p + 1u);
+  return true;
+}
+
+// Consumer side: claim a ticket and wait for its item; returns -1 when no tile is queued or
+// running any more (pending == 0: nothing can be pushed again) or after an error.
+__device__ __forceinline__ int queue_pop(const Ctl& c) {
+  const unsigned tk = atomicAdd(c.head, 1u);
+  Slot* sl = &c.slots[tk & (c.cap - 1)];
+  long long spins = 0;
+  unsigned ns = 32;
+  for (;;) {
+    if (ld_acquire_u(&sl->seq) == tk + 1u) {
+      const int t = *(volatile int*)&sl->val;
+      st_release_u(&sl->seq, tk + c.cap);
+      return t;
+    }
+    if (ld_acquire(c.pending) == 0 || ld_relaxed(c.status) != 0) return -1;
+    if (++spins > kSpinLimit) {
+      set_status(c.status, kDevTimeout);
+      return -1;
+    }
+    __nanosleep(ns);
+    if (ns < 1024) ns <<= 1;
   }
 }
 
+// A neighbour's values may have become stale: make sure it (re)reads them.
+__device__ __forceinline__ void mark_tile(const Ctl& c, int nt) {
+  int s = ld_relaxed(&c.state[nt]);
+  for (int guard = 0; guard < 1024; ++guard) {
+    if (s == kQueued || s == kRunningDirty) return;  // will load after our stores
+    const int want = (s == kIdle) ? kQueued : kRunningDirty;
+    const int old = atomicCAS(&c.state[nt], s, want);
+    if (old == s) {
+      if (want == kQueued) {
+        atomicAdd(c.pending, 1);
+        queue_push(c, nt);
+      }
+      return;
+    }
+    s = old;
+  }
+  set_status(c.status, kDevTimeout);
+}
+
 template <typename T, int CONN>
-__device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int round, int lane) {
+__device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int lane) {
   using P = Px<T>;
   constexpr int E = P::E;
   constexpr int TW = 32 * E;
@@ -349,13 +414,12 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int r
   const int H = a.H, W = a.W;
   const bool flip = a.flip != 0, ring = a.ring != 0;
 
-  if (lane == 0) atomicExch(&a.c.start[t], round);
+  // The caller has set the tile RUNNING; order that before reading the neighbours' pixels.
   __syncwarp();
   __threadfence();
 
-  const bool first = (round == 0);
-  const T* src = first ? a.marker : a.out;
-  const bool coh = !first || (a.marker == a.out);
+  const T* src = a.out;
+  const bool coh = true;
   const bool interior = (y0 + kRows <= H) && (x0 + TW <= W);
   const bool fast = interior && a.aligned;
   const int xl = x0 + E * lane;
@@ -418,8 +482,8 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int r
     }
   }
   if (lane == 0) {
-    atomicAdd(&a.c.stats[1], 1);
-    atomicAdd(&a.c.stats[2], it);
+    atomicAdd(&a.c.stats[0], 1);
+    atomicAdd(&a.c.stats[1], it);
   }
 
   // Write the tile back.
@@ -489,7 +553,7 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int r
       if (!((dirs >> d) & 1u)) continue;
       const int ny = ty + d / 3 - 1, nx = tx + d % 3 - 1;
       if (ny < 0 || ny >= a.tiles_y || nx < 0 || nx >= a.tiles_x) continue;
-      mark_tile(a.c, ny * a.tiles_x + nx, round);
+      mark_tile(a.c, ny * a.tiles_x + nx);
     }
   }
   __syncwarp();
@@ -500,47 +564,103 @@ __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   WarpBuf& B = reinterpret_cast<WarpBuf*>(smem_raw)[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
-  int round = 0;
   for (;;) {
-    const int n_cur = (round == 0) ? a.ntiles : ld_acquire(&a.c.count[round % 3]);
-    const int* list = (round & 1) ? a.c.list1 : a.c.list0;
-    for (;;) {
-      int idx = 0;
-      if (lane == 0) idx = atomicAdd(&a.c.claim[round % 3], 1);
-      idx = __shfl_sync(NSGB_FULL, idx, 0);
-      if (idx >= n_cur) break;
-      const int t = (round == 0) ? idx : __ldcg(&list[idx]);
-      visit<T, CONN>(a, B, t, round, lane);
-      if (ld_relaxed(a.c.status) != 0) break;
+    int t = 0;
+    if (lane == 0) t = queue_pop(a.c);
+    t = __shfl_sync(NSGB_FULL, t, 0);
+    if (t < 0) break;
+    if (lane == 0) atomicExch(&a.c.state[t], kRunning);
+    visit<T, CONN>(a, B, t, lane);
+    if (lane == 0) {
+      if (atomicCAS(&a.c.state[t], kRunning, kIdle) == kRunning) {
+        atomicSub(a.c.pending, 1);
+      } else {
+        // A neighbour changed while this tile ran: queue it again at the back, so the
+        // neighbours still running finish first (it stays counted in `pending`).
+        atomicExch(&a.c.state[t], kQueued);
+        atomicAdd(&a.c.stats[2], 1);
+        queue_push(a.c, t);
+      }
+      if (atomicAdd(a.c.visit_count, 1ull) >= (unsigned long long)a.c.max_visits)
+        set_status(a.c.status, kDevNotConverged);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      a.c.claim[(round + 2) % 3] = 0;
-      a.c.count[(round + 2) % 3] = 0;
-    }
-    if (!grid_barrier(a.c.bar, gridDim.x, a.c.status)) break;
-    const int nn = ld_acquire(&a.c.count[(round + 1) % 3]);
-    if (nn == 0 || ld_relaxed(a.c.status) != 0) break;
-    if (++round >= a.max_rounds) {
-      if (blockIdx.x == 0 && threadIdx.x == 0) set_status(a.c.status, kDevNotConverged);
-      break;
-    }
+    __syncwarp();
+    if (ld_relaxed(a.c.status) != 0) break;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) a.c.stats[0] = round + 1;
 }
 
-// Workspace layout (ints): status, stats[3], claim[3], count[3], bar[2] (unsigned), pad to 32;
-// then enq, start, list0, list1 (ntiles each).
-constexpr int kHdrInts = 32;
+// Initial queue: every tile, in raster order (order 0) or as a checkerboard, even tiles first
+// (order 1), so that tiles processed at the same time are rarely neighbours.
+__global__ void recon_init_kernel(Ctl c, int ntiles, int tiles_x, int order) {
+  const int half = (ntiles + 1) / 2;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < c.cap; i += gridDim.x * blockDim.x) {
+    if ((int)i < ntiles) {
+      int t = (int)i;
+      if (order == 1) {
+        // i-th even tile for i < #even, else the (i - #even)-th odd tile
+        const int ty_n = (ntiles + tiles_x - 1) / tiles_x;
+        int even = 0;
+        for (int ty = 0; ty < ty_n; ++ty) even += (tiles_x + ((ty & 1) ? 0 : 1)) / 2;
+        (void)half;
+        int k = (int)i, parity = 0;
+        if (k >= even) {
+          k -= even;
+          parity = 1;
+        }
+        // walk rows: row ty holds ceil/floor(tiles_x/2) tiles of this parity
+        int ty = 0;
+        for (;; ++ty) {
+          const int cnt = (tiles_x + (((ty & 1) ^ parity) ? 0 : 1)) / 2;
+          if (k < cnt) break;
+          k -= cnt;
+        }
+        const int first = ((ty & 1) ^ parity) ? 1 : 0;
+        t = ty * tiles_x + first + 2 * k;
+      }
+      c.slots[i].val = t;
+      c.slots[i].seq = i + 1u;
+      c.state[i] = kQueued;
+    } else {
+      c.slots[i].val = -1;
+      c.slots[i].seq = i;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *c.head = 0u;
+    *c.tail = (unsigned)ntiles;
+    *c.pending = ntiles;
+  }
+}
+
+// Workspace layout (ints): [0] status, [1..3] stats (visits, sweeps, re-runs), [6..7] visit
+// counter (64-bit), [8] head, [9] tail, [10] pending; from int kHdrInts: state[ntiles], then
+// the ring (2 ints per slot, cap slots).
+constexpr int kHdrInts = 64;
 
 template <typename T>
 int tiles_x_for(int64_t W) { return (int)((W + 32 * Px<T>::E - 1) / (32 * Px<T>::E)); }
 
+// Initial queue order (0 raster, 1 checkerboard); NSGB_RECON_ORDER overrides for experiments.
+inline int recon_order() {
+  static int order = -1;
+  if (order < 0) {
+    const char* e = getenv("NSGB_RECON_ORDER");
+    order = (e && *e) ? atoi(e) : 1;
+  }
+  return order;
+}
+
+inline unsigned ring_cap(int64_t ntiles) {
+  unsigned c = 32;
+  while ((int64_t)c < ntiles) c <<= 1;
+  return c;
+}
+
 template <typename T, int CONN>
-cudaError_t launch_typed(void* out, const void* marker, const void* mask, int64_t H, int64_t W, int64_t pitch,
-                         bool erode, bool ring, void* ws, cudaStream_t s, int max_rounds, int max_iters) {
+cudaError_t launch_typed(void* out, const void* mask, int64_t H, int64_t W, int64_t pitch, bool erode, bool ring,
+                         void* ws, cudaStream_t s, int max_visits_per_tile, int max_iters) {
   Args<T> a;
   a.out = (T*)out;
-  a.marker = (const T*)marker;
   a.mask = (const T*)mask;
   a.pitch = pitch;
   a.H = (int)H;
@@ -551,35 +671,31 @@ cudaError_t launch_typed(void* out, const void* marker, const void* mask, int64_
   a.flip = erode ? 1 : 0;
   a.ring = ring ? 1 : 0;
   const int vec = Px<T>::E == 2 ? 2 * (int)sizeof(T) : (int)sizeof(T);
-  a.aligned = (((uintptr_t)out % vec) == 0 && ((uintptr_t)marker % vec) == 0 && ((uintptr_t)mask % vec) == 0 &&
-               (pitch % vec) == 0)
-                  ? 1
-                  : 0;
-  a.max_rounds = max_rounds > 0 ? max_rounds : (1 << 24);
+  a.aligned = (((uintptr_t)out % vec) == 0 && ((uintptr_t)mask % vec) == 0 && (pitch % vec) == 0) ? 1 : 0;
   a.max_iters = max_iters > 0 ? max_iters : 4096;
   int* wi = (int*)ws;
   a.c.status = wi + 0;
   a.c.stats = wi + 1;
-  a.c.claim = wi + 4;
-  a.c.count = wi + 7;
-  a.c.bar = (unsigned*)(wi + 10);
-  a.c.enq = wi + kHdrInts;
-  a.c.start = a.c.enq + a.ntiles;
-  a.c.list0 = a.c.start + a.ntiles;
-  a.c.list1 = a.c.list0 + a.ntiles;
+  a.c.visit_count = (unsigned long long*)(wi + 6);
+  a.c.head = (unsigned*)(wi + 8);
+  a.c.tail = (unsigned*)(wi + 9);
+  a.c.pending = wi + 10;
+  a.c.state = wi + kHdrInts;
+  a.c.cap = ring_cap(a.ntiles);
+  a.c.slots = (Slot*)(a.c.state + ((a.ntiles + 1) & ~1));
+  a.c.max_visits = (long long)(max_visits_per_tile > 0 ? max_visits_per_tile : 1 << 20) * a.ntiles;
 
-  cudaError_t e;
-  // Header and enq = 0; start = -1.
-  e = cudaMemsetAsync(wi, 0, sizeof(int) * (kHdrInts + (size_t)a.ntiles), s);
+  cudaError_t e = cudaMemsetAsync(wi, 0, sizeof(int) * kHdrInts, s);
   if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(a.c.start, 0xFF, sizeof(int) * (size_t)a.ntiles, s);
+  recon_init_kernel<<<(a.c.cap + 255) / 256, 256, 0, s>>>(a.c, a.ntiles, a.tiles_x, recon_order());
+  e = cudaGetLastError();
   if (e != cudaSuccess) return e;
 
   const size_t smem = sizeof(WarpBuf) * kWarps;
-  static int occ_cache[8][2] = {{0}};  // per device, per instantiation set below
+  static int occ_cache[8] = {0};  // per device, for this instantiation
   int dev = 0;
   cudaGetDevice(&dev);
-  int& occ = occ_cache[dev & 7][0];
+  int& occ = occ_cache[dev & 7];
   if (occ == 0) {
     e = cudaFuncSetAttribute(recon_kernel<T, CONN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -595,6 +711,8 @@ cudaError_t launch_typed(void* out, const void* marker, const void* mask, int64_
   if (grid > occ) grid = occ;
   if (grid < 1) grid = 1;
   void* args[] = {&a};
+  // Cooperative launch: all CTAs are co-resident, so warps waiting on the queue never block
+  // warps that still have to be scheduled.
   return cudaLaunchCooperativeKernel((const void*)recon_kernel<T, CONN>, dim3(grid), dim3(kWarps * 32), args, smem,
                                      s);
 }
@@ -611,19 +729,24 @@ size_t recon_workspace_bytes(int dtype, int64_t H, int64_t W) {
     default: return 0;
   }
   const int64_t ty = (H + kRows - 1) / kRows;
-  return sizeof(int) * (size_t)(kHdrInts + 4 * tx * ty);
+  const int64_t nt = tx * ty;
+  return sizeof(int) * (size_t)(kHdrInts + ((nt + 1) & ~1) + 2 * (int64_t)ring_cap(nt));
 }
 
 cudaError_t recon_launch(int dtype, void* out, const void* marker, const void* mask, int64_t H, int64_t W,
-                         int64_t pitch, int conn, bool erode, bool ring, void* ws, cudaStream_t s, int max_rounds,
+                         int64_t pitch, int conn, bool erode, bool ring, void* ws, cudaStream_t s, int max_visits,
                          int max_iters) {
+  if (marker != out) {
+    // The kernel works in place; start from a copy of the marker.
+    const int esz = elem_size(dtype);
+    cudaError_t e = cudaMemcpy2DAsync(out, pitch, marker, pitch, (size_t)W * esz, (size_t)H, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+  }
   switch (dtype) {
-#define NSGB_RECON_CASE(CODE, TYPE)                                                                         \
-  case CODE:                                                                                                 \
-    return conn == 8 ? launch_typed<TYPE, 8>(out, marker, mask, H, W, pitch, erode, ring, ws, s, max_rounds, \
-                                             max_iters)                                                      \
-                     : launch_typed<TYPE, 4>(out, marker, mask, H, W, pitch, erode, ring, ws, s, max_rounds, \
-                                             max_iters);
+#define NSGB_RECON_CASE(CODE, TYPE)                                                                           \
+  case CODE:                                                                                                   \
+    return conn == 8 ? launch_typed<TYPE, 8>(out, mask, H, W, pitch, erode, ring, ws, s, max_visits, max_iters) \
+                     : launch_typed<TYPE, 4>(out, mask, H, W, pitch, erode, ring, ws, s, max_visits, max_iters);
     NSGB_RECON_CASE(NSGB_U8, uint8_t)
     NSGB_RECON_CASE(NSGB_U16, uint16_t)
     NSGB_RECON_CASE(NSGB_I32, int32_t)

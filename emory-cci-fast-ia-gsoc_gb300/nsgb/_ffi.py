@@ -33,7 +33,7 @@ class NsgbError(RuntimeError):
 
 
 class Opts(C.Structure):
-    _fields_ = [("sync", C.c_int), ("max_rounds", C.c_int), ("max_visit_iters", C.c_int),
+    _fields_ = [("sync", C.c_int), ("max_visits_per_tile", C.c_int), ("max_visit_iters", C.c_int),
                 ("reserved", C.c_int * 5), ("recon_event_begin", C.c_void_p), ("recon_event_end", C.c_void_p)]
 
 

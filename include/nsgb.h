@@ -53,7 +53,8 @@ typedef enum {
 
 typedef struct {
   int sync;       /* 1: synchronize and return the device status (default when opts == NULL) */
-  int max_rounds; /* reconstruction: cap on work-list rounds (0 = default) */
+  int max_visits_per_tile; /* reconstruction: cap on tile visits, in units of the number of
+                             tiles (0 = default, effectively unbounded) */
   int max_visit_iters; /* reconstruction: cap on row/column sweeps per tile visit (0 = default) */
   int reserved[5];
   /* Optional CUDA events (cudaEvent_t) recorded on the call's stream immediately before and

@@ -75,7 +75,7 @@ int orc_bwselect(int dtype, const void* image, const void* seeds, int64_t H, int
 int orc_threshold_gt(int dtype, const void* in, int64_t n, double k, uint8_t* out) {
   return dispatch(dtype, [&](auto* tag) {
     using T = std::remove_pointer_t<decltype(tag)>;
-    orc::threshold_gt<T>((const T*)in, n, (T)k, out);
+    orc::threshold_gt<T>((const T*)in, n, k, out);
   });
 }
 
@@ -103,7 +103,7 @@ int32_t orc_chain(int dtype, const void* marker, const void* mask, int64_t H, in
     std::vector<T> rec((size_t)n);
     orc::imreconstruct<T>((const T*)marker, (const T*)mask, H, W, recon_conn, rec.data());
     std::vector<uint8_t> b((size_t)n), f((size_t)n), a((size_t)n);
-    orc::threshold_gt<T>(rec.data(), n, (T)thr, b.data());
+    orc::threshold_gt<T>(rec.data(), n, thr, b.data());
     orc::imfill_holes<uint8_t>(b.data(), H, W, true, fill_conn, f.data());
     std::vector<int32_t> lab((size_t)n);
     int32_t nl = orc::bwlabel2(f.data(), H, W, label_conn, true, lab.data());

@@ -415,10 +415,12 @@ inline int32_t bwareaopen2(const void* image, bool labeled, bool flatten, int32_
   return count;
 }
 
-// `Mat > k` (HistologicalEntities.cpp:214): 255 where strictly greater, else 0.
+// `Mat > k` (HistologicalEntities.cpp:214): 255 where strictly greater, else 0.  The
+// comparison is against the double-valued scalar, as OpenCV's compare does (k is not
+// rounded to the pixel type: u8 `> -1` is true everywhere).
 template <typename T>
-inline void threshold_gt(const T* in, int64_t n, T k, uint8_t* out) {
-  for (int64_t i = 0; i < n; ++i) out[i] = in[i] > k ? 255 : 0;
+inline void threshold_gt(const T* in, int64_t n, double k, uint8_t* out) {
+  for (int64_t i = 0; i < n; ++i) out[i] = (double)in[i] > k ? 255 : 0;
 }
 
 }  // namespace orc

@@ -285,13 +285,13 @@ def test_chain_inverted_workload(nsgb, oracle):
 
 
 def test_device_budgets_report_status(nsgb):
-    """Failure detection without a fault: a one-round / one-sweep budget on an input that
-    needs more returns NOT_CONVERGED through the status word; the context stays usable."""
+    """Failure detection without a fault: a one-visit-per-tile / one-sweep budget on an input
+    that needs more returns NOT_CONVERGED through the status word; the context stays usable."""
     from nsgb import synth
 
     mask, marker = synth.tile_u8(512, 512, 60, 2)
     with pytest.raises(nsgb.NsgbError) as e:
-        nsgb.imreconstruct(to_dev(marker), to_dev(mask), 8, max_rounds=1)
+        nsgb.imreconstruct(to_dev(marker), to_dev(mask), 8, max_visits_per_tile=1)
     assert e.value.status == 4
     with pytest.raises(nsgb.NsgbError) as e:
         nsgb.imreconstruct(to_dev(marker), to_dev(mask), 8, max_visit_iters=1)
