@@ -7,12 +7,13 @@
 // reference (cuda/ccl_uf.cu:64-157, UF_local / UF_global / UF_final) uses the same
 // min-index rule with atomicMin.  This implementation keeps that rule (so labels are
 // bit-identical) with its own schedule:
-//   1. ccl_local: 32x32 tile per CTA; union-find in shared memory with atomicMin hooking;
-//      writes the tile-local root's global index and (optionally) each local root's area.
-//   2. ccl_merge: one thread per tile-perimeter pixel joins it with its forward neighbours
-//      in other tiles (global atomicMin hooking; a failed hook retries with the new parent).
-//   3. ccl_flatten: every foreground pixel points directly at its root; local-root areas are
-//      added into the root's area; optional "seed" pixels set a bit on their root.
+//   1. ccl_local: 32x32 tile per CTA; horizontal runs from warp ballots, union-find on run
+//      contacts in shared memory with atomicMin hooking; writes the tile-local root's global
+//      index, lists the local roots and (optionally) their areas.
+//   2. ccl_merge: one warp per tile edge joins runs that touch across the edge (global
+//      atomicMin hooking; a failed hook retries with the new parent).
+//   3. ccl_flatten_roots: every local root points directly at its global root and passes its
+//      area on, so any pixel's root is L[L[i]]; seed kernels set a bit on the roots.
 // Roots are exactly the pixels with L[i] == i.  Classifiers (the `Cls` template argument)
 // return a pixel's class (0 = background; equal non-zero classes are joined), so the same
 // kernels serve bwlabel (class = pixel value), hole filling (class = "not foreground"),
@@ -90,17 +91,30 @@ __device__ __forceinline__ void g_union(int* L, int a, int b) {
   }
 }
 
-// L: dense H x W int32 (index y*W + x).  A (optional): dense int32, receives each local root's
-// pixel count at the root and 0 elsewhere.
-//
+// Output of a labelling: L (dense H x W int32, index y*W + x; -1 = background) where every
+// foreground pixel points at its tile-local root and, after ccl_flatten_roots, every local
+// root points at the global root, so root(i) = L[L[i]] (one hop).  A (optional) holds the
+// pixel count of each local root, then of each global root.  `roots` lists the local roots
+// (global indices), `nroots` counts them.
+struct Forest {
+  int* L;
+  int* A;
+  int* roots;
+  int* nroots;
+};
+
+__device__ __forceinline__ int root_of(const int* L, int64_t i) {
+  const int l = __ldcg(L + i);
+  return l < 0 ? -1 : __ldcg(L + l);
+}
+
 // Each warp owns tile rows (lane = column).  Runs of equal class along a row are found with a
 // ballot and start out joined (label = run start), so unions are only needed where runs of
 // adjacent rows touch: at a pixel that starts its run or sits under the start of a run above
 // (and, for 8-connectivity, diagonally past the two ends of the run).  That is one union per
 // touching pair of runs instead of one per pixel pair.
 template <class Cls, int CONN>
-__global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, int H, int W, int* __restrict__ L,
-                                                      int* __restrict__ A) {
+__global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, int H, int W, Forest f) {
   __shared__ int s_lab[kTile * kTile];
   __shared__ int s_cnt[kTile * kTile];
   __shared__ uint8_t s_c[kTile * kTile];
@@ -115,7 +129,6 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, int H, int W, int
     s_c[i] = c[k];
     s_cnt[i] = 0;
   }
-  __syncwarp();
   unsigned same_left[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
@@ -151,7 +164,7 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, int H, int W, int
     const int ly = ty + 8 * k, i = ly * kTile + tx;
     root[k] = c[k] ? s_find(s_lab, i) : -1;
   }
-  if (A) {
+  if (f.A) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int r = root[k];
@@ -164,81 +177,129 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, int H, int W, int
   for (int k = 0; k < 4; ++k) {
     const int ly = ty + 8 * k, i = ly * kTile + tx;
     const int gy = y0 + ly, gx = x0 + tx;
-    if (gy >= H || gx >= W) continue;
-    const int64_t g = (int64_t)gy * W + gx;
+    const bool in = gy < H && gx < W;
     const int r = root[k];
-    L[g] = r < 0 ? -1 : (int)((int64_t)(y0 + r / kTile) * W + x0 + (r % kTile));
-    if (A) A[g] = (r == i) ? s_cnt[i] : 0;
-  }
-}
-
-// Joins tile-perimeter pixels with their forward neighbours (right, down-left, down,
-// down-right) that lie in another tile.  Grid: one CTA of 96 threads per tile.
-template <class Cls, int CONN>
-__global__ void __launch_bounds__(96) ccl_merge(Cls cls, int H, int W, int* __restrict__ L) {
-  const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile;
-  const int t = threadIdx.x & 31, part = threadIdx.x >> 5;
-  int y, x;
-  if (part == 0) {  // bottom row
-    y = y0 + kTile - 1;
-    x = x0 + t;
-  } else if (part == 1) {  // right column
-    y = y0 + t;
-    x = x0 + kTile - 1;
-  } else {  // left column
-    y = y0 + t;
-    x = x0;
-  }
-  if (y >= H || x >= W) return;
-  const uint32_t c = cls(y, x);
-  if (!c) return;
-  const int p = y * W + x;
-  auto join = [&](int qy, int qx) {
-    if (qy < 0 || qy >= H || qx < 0 || qx >= W) return;
-    if ((qy / kTile) == (y / kTile) && (qx / kTile) == (x / kTile)) return;
-    if (cls(qy, qx) != c) return;
-    g_union(L, p, qy * W + qx);
-  };
-  if (part == 0) {
-    join(y + 1, x);
-    if (CONN == 8) {
-      join(y + 1, x - 1);
-      join(y + 1, x + 1);
-    }
-  } else if (part == 1) {
-    join(y, x + 1);
-    if (CONN == 8) join(y + 1, x + 1);
-  } else {
-    if (CONN == 8) join(y + 1, x - 1);
-  }
-}
-
-// Seed policy used by ccl_flatten: `seed(y, x)` says whether the pixel marks its root.
-struct NoSeed {
-  __device__ bool operator()(int, int) const { return false; }
-};
-
-// L[i] <- root(L[i]); local-root areas move into the root; seed pixels set bit root in `bits`.
-template <class Seed>
-__global__ void ccl_flatten(int H, int W, int* __restrict__ L, int* __restrict__ A, Seed seed,
-                            unsigned* __restrict__ bits) {
-  const int64_t n = (int64_t)H * W;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int l = ld_relaxed(L + i);
-    if (l < 0) continue;
-    const int r = g_find(L, l);
-    if (r != l) atomicMin(L + i, r);
-    if (A) {
-      const int a = A[i];
-      if (a > 0 && r != (int)i) atomicAdd(&A[r], a);
-    }
-    if (bits) {
-      const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
-      if (seed(y, x)) {
-        const unsigned bit = 1u << (r & 31);
-        if (!(ld_relaxed((const int*)&bits[r >> 5]) & bit)) atomicOr(&bits[r >> 5], bit);
+    const int g = gy * W + gx;
+    if (in) f.L[g] = r < 0 ? -1 : (y0 + r / kTile) * W + x0 + (r % kTile);
+    const bool is_root = in && r == i;
+    const unsigned rb = __ballot_sync(NSGB_FULL, is_root);
+    if (rb) {
+      int base = 0;
+      if (tx == 0) base = atomicAdd(f.nroots, __popc(rb));
+      base = __shfl_sync(NSGB_FULL, base, 0);
+      if (is_root) {
+        f.roots[base + __popc(rb & ((1u << tx) - 1u))] = g;
+        if (f.A) f.A[g] = s_cnt[i];
       }
     }
+  }
+}
+
+// Joins runs across tile edges.  Two warps per tile: warp 0 takes the bottom edge (row
+// y0+31 against row y0+32), warp 1 the right edge (column x0+31 against column x0+32, the
+// same logic transposed).  With `a` = the pixel on this side and `b` its partner across the
+// edge, runs of equal class along the edge are found with ballots, and a union is made only
+// where a run on the far side starts or where a near-side run starts under a far-side run,
+// plus the two diagonal ends of each far-side run for 8-connectivity.
+template <class Cls, int CONN>
+__global__ void __launch_bounds__(64) ccl_merge(Cls cls, int H, int W, int* __restrict__ L) {
+  const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile;
+  const int lane = threadIdx.x & 31;
+  const bool bottom = (threadIdx.x >> 5) == 0;
+  // coordinates of the near pixel (a) and the far pixel (b) for this lane
+  int ay, ax, by, bx;
+  if (bottom) {
+    ay = y0 + kTile - 1;
+    ax = x0 + lane;
+    by = ay + 1;
+    bx = ax;
+    if (by >= H) return;  // whole warp: no tile below
+  } else {
+    ax = x0 + kTile - 1;
+    ay = y0 + lane;
+    bx = ax + 1;
+    by = ay;
+    if (bx >= W) return;
+  }
+  const bool in_a = ay < H && ax < W;
+  const bool in_b = by < H && bx < W;
+  const uint32_t ca = in_a ? cls(ay, ax) : 0u;
+  const uint32_t cb = in_b ? cls(by, bx) : 0u;
+  // runs along the edge (lane order) on each side
+  const uint32_t ca_prev = __shfl_up_sync(NSGB_FULL, ca, 1);
+  const uint32_t cb_prev = __shfl_up_sync(NSGB_FULL, cb, 1);
+  const uint32_t cb_next = __shfl_down_sync(NSGB_FULL, cb, 1);
+  const bool a_start = ca != 0 && !(lane > 0 && ca_prev == ca);
+  const bool b_start = cb != 0 && !(lane > 0 && cb_prev == cb);
+  const bool b_end = cb != 0 && !(lane < 31 && cb_next == cb);
+  if (cb == 0) return;
+  const int pb = by * W + bx;
+  if (ca == cb && (a_start || b_start)) g_union(L, pb, ay * W + ax);
+  if (CONN == 8) {
+    // diagonal partners one step before the start / after the end of the far-side run
+    if (b_start) {
+      const int dy = bottom ? ay : ay - 1, dx = bottom ? ax - 1 : ax;
+      if (dy >= 0 && dx >= 0 && dy < H && dx < W && cls(dy, dx) == cb) g_union(L, pb, dy * W + dx);
+    }
+    if (b_end) {
+      const int dy = bottom ? ay : ay + 1, dx = bottom ? ax + 1 : ax;
+      if (dy < H && dx < W && cls(dy, dx) == cb) g_union(L, pb, dy * W + dx);
+    }
+  }
+}
+
+// Every local root points directly at its global root; local-root areas move into the root.
+static __global__ void ccl_flatten_roots(Forest f, int max_roots) {
+  const int n = min(__ldcg(f.nroots), max_roots);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int lr = __ldcg(f.roots + k);
+    const int r = g_find(f.L, lr);
+    if (r != lr) {
+      atomicMin(f.L + lr, r);
+      if (f.A) atomicAdd(f.A + r, __ldcg(f.A + lr));
+    }
+  }
+}
+
+// Seed pixels set bit root(p) in `bits`.  One thread per pixel (row / column grid).
+template <class Seed>
+__global__ void ccl_seed_pixels(int H, int W, const int* __restrict__ L, Seed seed, unsigned* __restrict__ bits) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= W) return;
+  for (int y = blockIdx.y; y < H; y += gridDim.y) {
+    if (!seed(y, x)) continue;
+    const int r = root_of(L, (int64_t)y * W + x);
+    if (r < 0) continue;
+    const unsigned bit = 1u << (r & 31);
+    if (!(__ldcg(&bits[r >> 5]) & bit)) atomicOr(&bits[r >> 5], bit);
+  }
+}
+
+// Seed pixels on the image border only: thread k walks the border (top row, bottom row, left
+// column, right column).
+template <class Seed>
+__global__ void ccl_seed_border(int H, int W, const int* __restrict__ L, Seed seed, unsigned* __restrict__ bits) {
+  const int64_t per = 2 * (int64_t)W + 2 * (int64_t)H;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < per; k += (int64_t)gridDim.x * blockDim.x) {
+    int y, x;
+    if (k < W) {
+      y = 0;
+      x = (int)k;
+    } else if (k < 2 * (int64_t)W) {
+      y = H - 1;
+      x = (int)(k - W);
+    } else if (k < 2 * (int64_t)W + H) {
+      y = (int)(k - 2 * (int64_t)W);
+      x = 0;
+    } else {
+      y = (int)(k - 2 * (int64_t)W - H);
+      x = W - 1;
+    }
+    if (!seed(y, x)) continue;
+    const int r = root_of(L, (int64_t)y * W + x);
+    if (r < 0) continue;
+    const unsigned bit = 1u << (r & 31);
+    if (!(__ldcg(&bits[r >> 5]) & bit)) atomicOr(&bits[r >> 5], bit);
   }
 }
 
@@ -251,19 +312,25 @@ __device__ __forceinline__ bool test_bit(const unsigned* bits, int r) {
 // Host helpers (ccl.cu).
 inline dim3 tile_grid(int H, int W) { return dim3((W + kTile - 1) / kTile, (H + kTile - 1) / kTile); }
 int flat_grid(int64_t n);
+// Grid for the row / column kernels: x covers the columns (256 per block), y strides rows.
+inline dim3 rowcol_grid(int H, int W) {
+  return dim3((W + 255) / 256, (unsigned)(H < 65535 ? H : 65535));
+}
 
-template <class Cls, class Seed>
-cudaError_t label(const Cls& cls, int H, int W, int conn, int* L, int* A, const Seed& seed, unsigned* bits,
-                  cudaStream_t s) {
+// Labels the image: local pass, edge merge, root flattening.  Afterwards root(i) = L[L[i]].
+template <class Cls>
+cudaError_t label(const Cls& cls, int H, int W, int conn, const Forest& f, cudaStream_t s) {
   const dim3 g = tile_grid(H, W);
+  cudaError_t e = cudaMemsetAsync(f.nroots, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
   if (conn == 8) {
-    ccl_local<Cls, 8><<<g, kThreads, 0, s>>>(cls, H, W, L, A);
-    ccl_merge<Cls, 8><<<g, 96, 0, s>>>(cls, H, W, L);
+    ccl_local<Cls, 8><<<g, kThreads, 0, s>>>(cls, H, W, f);
+    ccl_merge<Cls, 8><<<g, 64, 0, s>>>(cls, H, W, f.L);
   } else {
-    ccl_local<Cls, 4><<<g, kThreads, 0, s>>>(cls, H, W, L, A);
-    ccl_merge<Cls, 4><<<g, 96, 0, s>>>(cls, H, W, L);
+    ccl_local<Cls, 4><<<g, kThreads, 0, s>>>(cls, H, W, f);
+    ccl_merge<Cls, 4><<<g, 64, 0, s>>>(cls, H, W, f.L);
   }
-  ccl_flatten<Seed><<<flat_grid((int64_t)H * W), 256, 0, s>>>(H, W, L, A, seed, bits);
+  ccl_flatten_roots<<<flat_grid((int64_t)H * W / 4 + 1), 256, 0, s>>>(f, H * W);
   return cudaGetLastError();
 }
 

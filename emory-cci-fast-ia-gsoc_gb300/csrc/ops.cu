@@ -80,63 +80,62 @@ struct SeedBoth {  // marker != 0 and mask != 0
 };
 
 // ------------------------------------------------------------------------------------------
-// Output kernels.
+// Output kernels.  Row / column grids (x = column, y strides rows); a pixel's root is
+// L[L[i]] after the labelling (ccl::root_of).
 
 // Binary hole filling: 0 where the non-foreground pixel's component touches the border.
-template <class Cls, typename TO>
-__global__ void fill_out_kernel(Cls cls, int H, int W, const int* __restrict__ L, const unsigned* __restrict__ bits,
-                                TO* out, int64_t pitch_out, TO fg) {
-  const int64_t n = (int64_t)H * W;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
-    const int l = __ldcg(&L[i]);
-    const bool hole_free = l >= 0 && ccl::test_bit(bits, l);
-    *pxp(out, pitch_out, y, x) = hole_free ? (TO)0 : fg;
+template <typename TO>
+__global__ void fill_out_kernel(int H, int W, const int* __restrict__ L, const unsigned* __restrict__ bits, TO* out,
+                                int64_t pitch_out, TO fg) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= W) return;
+  for (int y = blockIdx.y; y < H; y += gridDim.y) {
+    const int r = ccl::root_of(L, (int64_t)y * W + x);
+    *pxp(out, pitch_out, y, x) = (r >= 0 && ccl::test_bit(bits, r)) ? (TO)0 : fg;
   }
 }
 
 // Binary reconstruction output, in place on the marker.
 template <typename T>
-__global__ void binrecon_out_kernel(T* marker, const T* mask, int64_t pitch, int H, int W, const int* __restrict__ L,
+__global__ void binrecon_out_kernel(T* marker, int64_t pitch, int H, int W, const int* __restrict__ L,
                                     const unsigned* __restrict__ bits) {
-  const int64_t n = (int64_t)H * W;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= W) return;
+  for (int y = blockIdx.y; y < H; y += gridDim.y) {
     T* p = pxp(marker, pitch, y, x);
     if (*p != (T)0) continue;
-    const int l = __ldcg(&L[i]);
-    if (l >= 0 && ccl::test_bit(bits, l)) *p = std::numeric_limits<T>::max();
+    const int r = ccl::root_of(L, (int64_t)y * W + x);
+    if (r >= 0 && ccl::test_bit(bits, r)) *p = std::numeric_limits<T>::max();
   }
 }
 
 template <typename T>
 __global__ void bwselect_out_kernel(const T* image, T* out, int64_t pitch, int H, int W, const int* __restrict__ L,
                                     const unsigned* __restrict__ bits) {
-  const int64_t n = (int64_t)H * W;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= W) return;
+  for (int y = blockIdx.y; y < H; y += gridDim.y) {
     const T v = px(image, pitch, y, x);
-    const int l = __ldcg(&L[i]);
-    *pxp(out, pitch, y, x) = (v != (T)0 && l >= 0 && ccl::test_bit(bits, l)) ? v : (T)0;
+    const int r = ccl::root_of(L, (int64_t)y * W + x);
+    *pxp(out, pitch, y, x) = (v != (T)0 && r >= 0 && ccl::test_bit(bits, r)) ? v : (T)0;
   }
 }
 
-// Labels out: relabel ? (bg 0, roots' rank + 1) : root index / -1.  Optional area filter
-// outputs from the same pass.
+// Labels out: relabel ? (bg 0, root's rank + 1) : root index / -1.  Optional area-filter
+// outputs from the same pass.  rank / A are read-only here: L1-cached loads, because a giant
+// component's root is read by every one of its pixels.
 __global__ void label_out_kernel(int H, int W, const int* __restrict__ L, const int* __restrict__ rank, int relabel,
                                  int32_t* labels, int64_t pitch_labels, const int* __restrict__ A, int lo, int hi,
                                  int32_t* kept_labels, int64_t pitch_kept, uint8_t* flat, int64_t pitch_flat) {
-  const int64_t n = (int64_t)H * W;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
-    const int l = __ldcg(&L[i]);
-    // rank / A are read-only here: L1-cached loads (a giant component's root is read by
-    // every one of its pixels).
-    if (labels) *pxp(labels, pitch_labels, y, x) = relabel ? (l < 0 ? 0 : __ldg(&rank[l]) + 1) : l;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= W) return;
+  for (int y = blockIdx.y; y < H; y += gridDim.y) {
+    const int r = ccl::root_of(L, (int64_t)y * W + x);
+    if (labels) *pxp(labels, pitch_labels, y, x) = relabel ? (r < 0 ? 0 : __ldg(&rank[r]) + 1) : r;
     if (A) {
-      const int a = l >= 0 ? __ldg(&A[l]) : 0;
-      const bool keep = l >= 0 && a >= lo && a < hi;
-      if (kept_labels) *pxp(kept_labels, pitch_kept, y, x) = keep ? l : -1;
+      const int a = r >= 0 ? __ldg(&A[r]) : 0;
+      const bool keep = r >= 0 && a >= lo && a < hi;
+      if (kept_labels) *pxp(kept_labels, pitch_kept, y, x) = keep ? r : -1;
       if (flat) *pxp(flat, pitch_flat, y, x) = keep ? 255 : 0;
     }
   }
@@ -144,9 +143,10 @@ __global__ void label_out_kernel(int H, int W, const int* __restrict__ L, const 
 
 // Area of arbitrary int32 labels in [-1, n): dense histogram (background -1 skipped).
 __global__ void label_hist_kernel(const int32_t* lab, int64_t pitch, int H, int W, int* __restrict__ A, int* status) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= W) return;
   const int64_t n = (int64_t)H * W;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
+  for (int y = blockIdx.y; y < H; y += gridDim.y) {
     const int l = px(lab, pitch, y, x);
     if (l == -1) continue;
     if (l < -1 || (int64_t)l >= n) {
@@ -160,9 +160,10 @@ __global__ void label_hist_kernel(const int32_t* lab, int64_t pitch, int H, int 
 __global__ void labeled_area_out_kernel(const int32_t* lab, int64_t pitch, int H, int W, const int* __restrict__ A,
                                         int lo, int hi, int32_t* kept_labels, int64_t pitch_kept, uint8_t* flat,
                                         int64_t pitch_flat) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= W) return;
   const int64_t n = (int64_t)H * W;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
+  for (int y = blockIdx.y; y < H; y += gridDim.y) {
     const int l = px(lab, pitch, y, x);
     const int a = (l >= 0 && (int64_t)l < n) ? __ldg(&A[l]) : 0;
     const bool keep = l >= 0 && (int64_t)l < n && a >= lo && a < hi;
@@ -182,15 +183,16 @@ __global__ void count_labels_in_range_kernel(const int* __restrict__ A, int64_t 
 }
 
 // ------------------------------------------------------------------------------------------
-// Elementwise kernels.
+// Elementwise kernels (row / column grids).
+#define NSGB_FOR_PIXELS                                   \
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;    \
+  if (x >= W) return;                                     \
+  for (int y = blockIdx.y; y < H; y += gridDim.y)
+
 template <typename T>
 __global__ void threshold_kernel(const T* in, int64_t pitch_in, uint8_t* out, int64_t pitch_out, int H, int W,
                                  double thr) {
-  const int64_t n = (int64_t)H * W;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
-    *pxp(out, pitch_out, y, x) = (double)px(in, pitch_in, y, x) > thr ? 255 : 0;
-  }
+  NSGB_FOR_PIXELS { *pxp(out, pitch_out, y, x) = (double)px(in, pitch_in, y, x) > thr ? 255 : 0; }
 }
 
 template <typename T>
@@ -208,19 +210,13 @@ __device__ __forceinline__ T invert_value(T v) {
 
 template <typename T>
 __global__ void invert_kernel(const T* in, T* out, int64_t pitch, int H, int W) {
-  const int64_t n = (int64_t)H * W;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
-    *pxp(out, pitch, y, x) = invert_value(px(in, pitch, y, x));
-  }
+  NSGB_FOR_PIXELS { *pxp(out, pitch, y, x) = invert_value(px(in, pitch, y, x)); }
 }
 
 // Hole-filling marker: the image on the border, max<T> inside.
 template <typename T>
 __global__ void fill_marker_kernel(const T* image, T* out, int64_t pitch, int H, int W) {
-  const int64_t n = (int64_t)H * W;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
+  NSGB_FOR_PIXELS {
     const bool border = y == 0 || y == H - 1 || x == 0 || x == W - 1;
     *pxp(out, pitch, y, x) = border ? px(image, pitch, y, x) : std::numeric_limits<T>::max();
   }
@@ -229,9 +225,7 @@ __global__ void fill_marker_kernel(const T* image, T* out, int64_t pitch, int H,
 // h-minima marker: image + h, saturating for integers.
 template <typename T>
 __global__ void hmin_marker_kernel(const T* image, T* out, int64_t pitch, int H, int W, double h) {
-  const int64_t n = (int64_t)H * W;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
+  NSGB_FOR_PIXELS {
     const T v = px(image, pitch, y, x);
     T r;
     if constexpr (std::numeric_limits<T>::is_integer) {
@@ -246,11 +240,7 @@ __global__ void hmin_marker_kernel(const T* image, T* out, int64_t pitch, int H,
 
 template <typename T>
 __global__ void fill_const_kernel(T* out, int64_t pitch, int H, int W, T v) {
-  const int64_t n = (int64_t)H * W;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
-    *pxp(out, pitch, y, x) = v;
-  }
+  NSGB_FOR_PIXELS { *pxp(out, pitch, y, x) = v; }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -260,11 +250,13 @@ struct Ws {
   void* recon;
   int* L;
   int* A;
-  int* R;
+  int* R;        // root ranks; before ranking, the list of local roots
   unsigned* bits;
   int* tmp;
-  int* counts;  // [2]
+  int* counts;   // [2]
+  int* nroots;   // [1]
   uint8_t* F;
+  ccl::Forest forest(bool areas) const { return ccl::Forest{L, areas ? A : nullptr, R, nroots}; }
 };
 
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -282,7 +274,7 @@ WsSizes ws_sizes(int dtype, int64_t H, int64_t W) {
   z.A = z.L;
   z.R = z.L;
   z.bits = align256(sizeof(unsigned) * (size_t)((n + 31) / 32 + 1));
-  z.tmp = align256(sizeof(int) * (ccl::rank_tmp_ints(n) + 2));
+  z.tmp = align256(sizeof(int) * (ccl::rank_tmp_ints(n) + 4));
   z.F = align256((size_t)n);
   z.total = z.recon + z.L + z.A + z.R + z.bits + z.tmp + z.F;
   return z;
@@ -305,12 +297,14 @@ Ws carve(void* ws, int dtype, int64_t H, int64_t W) {
   p += z.bits;
   w.tmp = (int*)p;
   w.counts = w.tmp + (ccl::rank_tmp_ints(H * W));
+  w.nroots = w.counts + 2;
   p += z.tmp;
   w.F = (uint8_t*)p;
   return w;
 }
 
 inline int grid1d(int64_t n) { return ccl::flat_grid(n); }
+inline dim3 rc(int64_t rows, int64_t cols) { return ccl::rowcol_grid((int)rows, (int)cols); }
 
 }  // namespace
 }  // namespace nsgb
@@ -452,9 +446,10 @@ nsgb_status nsgb_imreconstruct_binary(int dtype, void* marker, const void* mask,
       using T = std::remove_pointer_t<decltype(tag)>;
       ClsNonZero<T> cls{(const T*)mask, pitch};
       SeedBoth<T> seed{(const T*)marker, (const T*)mask, pitch};
-      cudaError_t r = ccl::label(cls, H, W, conn, w.L, nullptr, seed, w.bits, s);
+      cudaError_t r = ccl::label(cls, H, W, conn, w.forest(false), s);
       if (r != cudaSuccess) return r;
-      binrecon_out_kernel<T><<<grid1d(rows * cols), 256, 0, s>>>((T*)marker, (const T*)mask, pitch, H, W, w.L, w.bits);
+      ccl::ccl_seed_pixels<SeedBoth<T>><<<rc(rows, cols), 256, 0, s>>>(H, W, w.L, seed, w.bits);
+      binrecon_out_kernel<T><<<rc(rows, cols), 256, 0, s>>>((T*)marker, pitch, H, W, w.L, w.bits);
       return cudaGetLastError();
     });
   }
@@ -480,7 +475,7 @@ nsgb_status nsgb_imfill_holes(int dtype, const void* image, void* out, int64_t r
     if (dtype == NSGB_I32) {
       // min<int> is non-zero, so the reference's binary reconstruction has no background to
       // grow into and every pixel comes back as invert(min<int>) = INT_MAX.
-      fill_const_kernel<int32_t><<<grid1d(rows * cols), 256, 0, s>>>((int32_t*)out, pitch, H, W, INT_MAX);
+      fill_const_kernel<int32_t><<<rc(rows, cols), 256, 0, s>>>((int32_t*)out, pitch, H, W, INT_MAX);
       return finish(cudaGetLastError(), ws, s, opts);
     }
     e = cudaMemsetAsync(w.bits, 0, sizeof(unsigned) * (size_t)((rows * cols + 31) / 32 + 1), s);
@@ -489,10 +484,12 @@ nsgb_status nsgb_imfill_holes(int dtype, const void* image, void* out, int64_t r
         using T = std::remove_pointer_t<decltype(tag)>;
         ClsNotMax<T> cls{(const T*)image, pitch};
         SeedBorder<ClsNotMax<T>> seed{cls, H, W};
-        cudaError_t r = ccl::label(cls, H, W, conn, w.L, nullptr, seed, w.bits, s);
+        cudaError_t r = ccl::label(cls, H, W, conn, w.forest(false), s);
         if (r != cudaSuccess) return r;
-        fill_out_kernel<ClsNotMax<T>, T><<<grid1d(rows * cols), 256, 0, s>>>(
-            cls, H, W, w.L, w.bits, (T*)out, pitch, std::numeric_limits<T>::max());
+        ccl::ccl_seed_border<SeedBorder<ClsNotMax<T>>><<<grid1d(2 * (rows + cols)), 256, 0, s>>>(H, W, w.L, seed,
+                                                                                                w.bits);
+        fill_out_kernel<T><<<rc(rows, cols), 256, 0, s>>>(H, W, w.L, w.bits, (T*)out, pitch,
+                                                          std::numeric_limits<T>::max());
         return cudaGetLastError();
       });
     }
@@ -501,10 +498,10 @@ nsgb_status nsgb_imfill_holes(int dtype, const void* image, void* out, int64_t r
   // Grayscale: erosion reconstruction of (image on the border, max inside) above the image.
   if (out == image) return NSGB_ERR_BAD_ARG;
   switch (dtype) {
-    case NSGB_U8: fill_marker_kernel<uint8_t><<<grid1d(rows * cols), 256, 0, s>>>((const uint8_t*)image, (uint8_t*)out, pitch, H, W); break;
-    case NSGB_U16: fill_marker_kernel<uint16_t><<<grid1d(rows * cols), 256, 0, s>>>((const uint16_t*)image, (uint16_t*)out, pitch, H, W); break;
-    case NSGB_I32: fill_marker_kernel<int32_t><<<grid1d(rows * cols), 256, 0, s>>>((const int32_t*)image, (int32_t*)out, pitch, H, W); break;
-    case NSGB_F32: fill_marker_kernel<float><<<grid1d(rows * cols), 256, 0, s>>>((const float*)image, (float*)out, pitch, H, W); break;
+    case NSGB_U8: fill_marker_kernel<uint8_t><<<rc(rows, cols), 256, 0, s>>>((const uint8_t*)image, (uint8_t*)out, pitch, H, W); break;
+    case NSGB_U16: fill_marker_kernel<uint16_t><<<rc(rows, cols), 256, 0, s>>>((const uint16_t*)image, (uint16_t*)out, pitch, H, W); break;
+    case NSGB_I32: fill_marker_kernel<int32_t><<<rc(rows, cols), 256, 0, s>>>((const int32_t*)image, (int32_t*)out, pitch, H, W); break;
+    case NSGB_F32: fill_marker_kernel<float><<<rc(rows, cols), 256, 0, s>>>((const float*)image, (float*)out, pitch, H, W); break;
   }
   e = recon_launch(dtype, out, out, image, rows, cols, pitch, conn, true, false, ws, s, opts ? opts->max_visits_per_tile : 0,
                    opts ? opts->max_visit_iters : 0);
@@ -523,9 +520,9 @@ nsgb_status nsgb_imhmin(int dtype, const void* image, void* out, int64_t rows, i
   cudaStream_t s = (cudaStream_t)stream;
   const int H = (int)rows, W = (int)cols;
   switch (dtype) {
-    case NSGB_U8: hmin_marker_kernel<uint8_t><<<grid1d(rows * cols), 256, 0, s>>>((const uint8_t*)image, (uint8_t*)out, pitch, H, W, h); break;
-    case NSGB_U16: hmin_marker_kernel<uint16_t><<<grid1d(rows * cols), 256, 0, s>>>((const uint16_t*)image, (uint16_t*)out, pitch, H, W, h); break;
-    case NSGB_F32: hmin_marker_kernel<float><<<grid1d(rows * cols), 256, 0, s>>>((const float*)image, (float*)out, pitch, H, W, h); break;
+    case NSGB_U8: hmin_marker_kernel<uint8_t><<<rc(rows, cols), 256, 0, s>>>((const uint8_t*)image, (uint8_t*)out, pitch, H, W, h); break;
+    case NSGB_U16: hmin_marker_kernel<uint16_t><<<rc(rows, cols), 256, 0, s>>>((const uint16_t*)image, (uint16_t*)out, pitch, H, W, h); break;
+    case NSGB_F32: hmin_marker_kernel<float><<<rc(rows, cols), 256, 0, s>>>((const float*)image, (float*)out, pitch, H, W, h); break;
   }
   // invert(recon(invert(I) - h, invert(I))): the order-reversed reconstruction with the
   // reference's 0-valued padding ring taken in the inverted domain.
@@ -553,9 +550,10 @@ nsgb_status nsgb_bwselect(int dtype, const void* image, const void* seeds, void*
       using T = std::remove_pointer_t<decltype(tag)>;
       ClsNonZero<T> cls{(const T*)image, pitch};
       SeedBoth<T> seed{(const T*)seeds, (const T*)image, pitch};
-      cudaError_t r = ccl::label(cls, H, W, conn, w.L, nullptr, seed, w.bits, s);
+      cudaError_t r = ccl::label(cls, H, W, conn, w.forest(false), s);
       if (r != cudaSuccess) return r;
-      bwselect_out_kernel<T><<<grid1d(rows * cols), 256, 0, s>>>((const T*)image, (T*)out, pitch, H, W, w.L, w.bits);
+      ccl::ccl_seed_pixels<SeedBoth<T>><<<rc(rows, cols), 256, 0, s>>>(H, W, w.L, seed, w.bits);
+      bwselect_out_kernel<T><<<rc(rows, cols), 256, 0, s>>>((const T*)image, (T*)out, pitch, H, W, w.L, w.bits);
       return cudaGetLastError();
     });
   }
@@ -577,10 +575,10 @@ nsgb_status nsgb_bwlabel(const uint8_t* bin, int32_t* labels, int64_t rows, int6
   cudaError_t e = cudaMemsetAsync(w.status, 0, sizeof(int), s);
   if (e != cudaSuccess) return NSGB_ERR_CUDA;
   ClsValueU8 cls{bin, pitch_in};
-  e = ccl::label(cls, H, W, conn, w.L, nullptr, ccl::NoSeed{}, nullptr, s);
+  e = ccl::label(cls, H, W, conn, w.forest(false), s);
   if (e == cudaSuccess) e = ccl::rank_roots(w.L, nullptr, n, 0, 0, w.R, w.tmp, w.counts, s);
   if (e == cudaSuccess) {
-    label_out_kernel<<<grid1d(n), 256, 0, s>>>(H, W, w.L, w.R, relabel, labels, pitch_labels, nullptr, 0, 0, nullptr,
+    label_out_kernel<<<rc(rows, cols), 256, 0, s>>>(H, W, w.L, w.R, relabel, labels, pitch_labels, nullptr, 0, 0, nullptr,
                                                0, nullptr, 0);
     e = cudaGetLastError();
   }
@@ -609,10 +607,10 @@ nsgb_status nsgb_bwareaopen(const void* in, int labeled, int32_t* labels_out, ui
   if (e != cudaSuccess) return NSGB_ERR_CUDA;
   if (!labeled) {
     ClsValueU8 cls{(const uint8_t*)in, pitch_in};
-    e = ccl::label(cls, H, W, conn, w.L, w.A, ccl::NoSeed{}, nullptr, s);
+    e = ccl::label(cls, H, W, conn, w.forest(true), s);
     if (e == cudaSuccess) e = ccl::rank_roots(w.L, w.A, n, min_size, max_size, w.R, w.tmp, w.counts, s);
     if (e == cudaSuccess) {
-      label_out_kernel<<<grid1d(n), 256, 0, s>>>(H, W, w.L, w.R, 0, nullptr, 0, w.A, min_size, max_size, labels_out,
+      label_out_kernel<<<rc(rows, cols), 256, 0, s>>>(H, W, w.L, w.R, 0, nullptr, 0, w.A, min_size, max_size, labels_out,
                                                  pitch_labels, flat_out, pitch_flat);
       e = cudaGetLastError();
     }
@@ -625,9 +623,9 @@ nsgb_status nsgb_bwareaopen(const void* in, int labeled, int32_t* labels_out, ui
   e = cudaMemsetAsync(w.A, 0, sizeof(int) * (size_t)n, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(w.counts, 0, 2 * sizeof(int), s);
   if (e == cudaSuccess) {
-    label_hist_kernel<<<grid1d(n), 256, 0, s>>>((const int32_t*)in, pitch_in, H, W, w.A, w.status);
+    label_hist_kernel<<<rc(rows, cols), 256, 0, s>>>((const int32_t*)in, pitch_in, H, W, w.A, w.status);
     count_labels_in_range_kernel<<<grid1d(n), 256, 0, s>>>(w.A, n, min_size, max_size, w.counts + 1);
-    labeled_area_out_kernel<<<grid1d(n), 256, 0, s>>>((const int32_t*)in, pitch_in, H, W, w.A, min_size, max_size,
+    labeled_area_out_kernel<<<rc(rows, cols), 256, 0, s>>>((const int32_t*)in, pitch_in, H, W, w.A, min_size, max_size,
                                                       labels_out, pitch_labels, flat_out, pitch_flat);
     e = cudaGetLastError();
   }
@@ -646,12 +644,11 @@ nsgb_status nsgb_threshold(int dtype, const void* in, uint8_t* out, int64_t rows
     return NSGB_ERR_BAD_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   const int H = (int)rows, W = (int)cols;
-  const int g = grid1d(rows * cols);
   switch (dtype) {
-    case NSGB_U8: threshold_kernel<uint8_t><<<g, 256, 0, s>>>((const uint8_t*)in, pitch_in, out, pitch_out, H, W, thr); break;
-    case NSGB_U16: threshold_kernel<uint16_t><<<g, 256, 0, s>>>((const uint16_t*)in, pitch_in, out, pitch_out, H, W, thr); break;
-    case NSGB_I32: threshold_kernel<int32_t><<<g, 256, 0, s>>>((const int32_t*)in, pitch_in, out, pitch_out, H, W, thr); break;
-    case NSGB_F32: threshold_kernel<float><<<g, 256, 0, s>>>((const float*)in, pitch_in, out, pitch_out, H, W, thr); break;
+    case NSGB_U8: threshold_kernel<uint8_t><<<rc(rows, cols), 256, 0, s>>>((const uint8_t*)in, pitch_in, out, pitch_out, H, W, thr); break;
+    case NSGB_U16: threshold_kernel<uint16_t><<<rc(rows, cols), 256, 0, s>>>((const uint16_t*)in, pitch_in, out, pitch_out, H, W, thr); break;
+    case NSGB_I32: threshold_kernel<int32_t><<<rc(rows, cols), 256, 0, s>>>((const int32_t*)in, pitch_in, out, pitch_out, H, W, thr); break;
+    case NSGB_F32: threshold_kernel<float><<<rc(rows, cols), 256, 0, s>>>((const float*)in, pitch_in, out, pitch_out, H, W, thr); break;
   }
   return cuda_status(cudaGetLastError());
 }
@@ -663,12 +660,11 @@ nsgb_status nsgb_invert(int dtype, const void* in, void* out, int64_t rows, int6
   if (!in || !out || !valid_dims(rows, cols) || !valid_pitch(pitch, cols, esz)) return NSGB_ERR_BAD_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   const int H = (int)rows, W = (int)cols;
-  const int g = grid1d(rows * cols);
   switch (dtype) {
-    case NSGB_U8: invert_kernel<uint8_t><<<g, 256, 0, s>>>((const uint8_t*)in, (uint8_t*)out, pitch, H, W); break;
-    case NSGB_U16: invert_kernel<uint16_t><<<g, 256, 0, s>>>((const uint16_t*)in, (uint16_t*)out, pitch, H, W); break;
-    case NSGB_I32: invert_kernel<int32_t><<<g, 256, 0, s>>>((const int32_t*)in, (int32_t*)out, pitch, H, W); break;
-    case NSGB_F32: invert_kernel<float><<<g, 256, 0, s>>>((const float*)in, (float*)out, pitch, H, W); break;
+    case NSGB_U8: invert_kernel<uint8_t><<<rc(rows, cols), 256, 0, s>>>((const uint8_t*)in, (uint8_t*)out, pitch, H, W); break;
+    case NSGB_U16: invert_kernel<uint16_t><<<rc(rows, cols), 256, 0, s>>>((const uint16_t*)in, (uint16_t*)out, pitch, H, W); break;
+    case NSGB_I32: invert_kernel<int32_t><<<rc(rows, cols), 256, 0, s>>>((const int32_t*)in, (int32_t*)out, pitch, H, W); break;
+    case NSGB_F32: invert_kernel<float><<<rc(rows, cols), 256, 0, s>>>((const float*)in, (float*)out, pitch, H, W); break;
   }
   return cuda_status(cudaGetLastError());
 }
@@ -701,21 +697,22 @@ nsgb_status nsgb_chain(int dtype, void* marker, const void* mask, int64_t rows, 
       using T = std::remove_pointer_t<decltype(tag)>;
       ClsNotAbove<T> cls{(const T*)marker, pitch, thr};
       SeedBorder<ClsNotAbove<T>> seed{cls, H, W};
-      cudaError_t r = ccl::label(cls, H, W, fill_conn, w.L, nullptr, seed, w.bits, s);
+      cudaError_t r = ccl::label(cls, H, W, fill_conn, w.forest(false), s);
       if (r != cudaSuccess) return r;
-      fill_out_kernel<ClsNotAbove<T>, uint8_t><<<grid1d(n), 256, 0, s>>>(cls, H, W, w.L, w.bits, F, (int64_t)W,
-                                                                          (uint8_t)255);
+      ccl::ccl_seed_border<SeedBorder<ClsNotAbove<T>>><<<grid1d(2 * (rows + cols)), 256, 0, s>>>(H, W, w.L, seed,
+                                                                                                  w.bits);
+      fill_out_kernel<uint8_t><<<rc(rows, cols), 256, 0, s>>>(H, W, w.L, w.bits, F, (int64_t)W, (uint8_t)255);
       return cudaGetLastError();
     });
   }
   // (d)+(e) one labelling of F serves bwlabel (relabelled) and bwareaopen (areas).
   if (e == cudaSuccess) {
     ClsValueU8 cls{F, (int64_t)W};
-    e = ccl::label(cls, H, W, label_conn, w.L, w.A, ccl::NoSeed{}, nullptr, s);
+    e = ccl::label(cls, H, W, label_conn, w.forest(true), s);
   }
   if (e == cudaSuccess) e = ccl::rank_roots(w.L, w.A, n, area_min, area_max, w.R, w.tmp, w.counts, s);
   if (e == cudaSuccess) {
-    label_out_kernel<<<grid1d(n), 256, 0, s>>>(H, W, w.L, w.R, 1, labels_out, (int64_t)W * 4, w.A, area_min, area_max,
+    label_out_kernel<<<rc(rows, cols), 256, 0, s>>>(H, W, w.L, w.R, 1, labels_out, (int64_t)W * 4, w.A, area_min, area_max,
                                                nullptr, 0, area_out, (int64_t)W);
     e = cudaGetLastError();
   }

@@ -53,6 +53,25 @@ struct alignas(16) WarpBuf {
 
 enum TileState : int { kIdle = 0, kQueued = 1, kRunning = 2, kRunningDirty = 3 };
 
+// Optional phase timers (compile with -DNSGB_RECON_PROFILE): lane 0 of every warp adds the
+// clock cycles spent per phase into 64-bit counters in the workspace header.
+#ifdef NSGB_RECON_PROFILE
+#define PROF_T0() const long long _pt0 = clock64(); long long _pt = _pt0
+#define PROF_MARK(slot)                                                        \
+  do {                                                                         \
+    const long long _now = clock64();                                          \
+    if (lane == 0) atomicAdd(a.c.prof + (slot), (unsigned long long)(_now - _pt)); \
+    _pt = _now;                                                                \
+  } while (0)
+#else
+#define PROF_T0() \
+  do {            \
+  } while (0)
+#define PROF_MARK(slot) \
+  do {                  \
+  } while (0)
+#endif
+
 struct Slot {
   int val;
   unsigned seq;
@@ -67,6 +86,7 @@ struct Ctl {
   int* status;
   int* stats;         // [0] visits, [1] sweeps, [2] re-runs
   unsigned long long* visit_count;  // budget counter
+  unsigned long long* prof;         // [8] phase cycle counters (profiling builds only)
   unsigned cap;       // ring capacity (power of two >= ntiles)
   long long max_visits;
 };
@@ -414,9 +434,11 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int l
   const int H = a.H, W = a.W;
   const bool flip = a.flip != 0, ring = a.ring != 0;
 
+  PROF_T0();
   // The caller has set the tile RUNNING; order that before reading the neighbours' pixels.
   __syncwarp();
   __threadfence();
+  PROF_MARK(1);
 
   const T* src = a.out;
   const bool coh = true;
@@ -467,6 +489,7 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int l
   }
   __syncwarp();
 
+  PROF_MARK(2);
   // Sweep to the local fixed point.
   int it = 0;
   for (;;) {
@@ -486,10 +509,12 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int l
     atomicAdd(&a.c.stats[1], it);
   }
 
+  PROF_MARK(3);
   // Write the tile back.
 #pragma unroll
   for (int i = 0; i < 32; ++i) store_word<T>(a.out, a.pitch, y0 + i, xl, H, W, O[i], fast, flip);
 
+  PROF_MARK(4);
   // Which neighbouring tiles could be raised by the new border values?
   unsigned dirs = 0;  // bit (dy+1)*3 + (dx+1)
   {
@@ -547,6 +572,7 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int l
   }
   __threadfence();
   __syncwarp();
+  PROF_MARK(5);
   if (lane == 0 && dirs) {
 #pragma unroll
     for (int d = 0; d < 9; ++d) {
@@ -557,6 +583,7 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int l
     }
   }
   __syncwarp();
+  PROF_MARK(6);
 }
 
 template <typename T, int CONN>
@@ -566,11 +593,20 @@ __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args<T> a) {
   const int lane = threadIdx.x & 31;
   for (;;) {
     int t = 0;
+#ifdef NSGB_RECON_PROFILE
+    const long long _pp = clock64();
+#endif
     if (lane == 0) t = queue_pop(a.c);
     t = __shfl_sync(NSGB_FULL, t, 0);
+#ifdef NSGB_RECON_PROFILE
+    if (lane == 0) atomicAdd(a.c.prof + 0, (unsigned long long)(clock64() - _pp));
+#endif
     if (t < 0) break;
     if (lane == 0) atomicExch(&a.c.state[t], kRunning);
     visit<T, CONN>(a, B, t, lane);
+#ifdef NSGB_RECON_PROFILE
+    const long long _pe = clock64();
+#endif
     if (lane == 0) {
       if (atomicCAS(&a.c.state[t], kRunning, kIdle) == kRunning) {
         atomicSub(a.c.pending, 1);
@@ -585,39 +621,53 @@ __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args<T> a) {
         set_status(a.c.status, kDevNotConverged);
     }
     __syncwarp();
+#ifdef NSGB_RECON_PROFILE
+    if (lane == 0) atomicAdd(a.c.prof + 7, (unsigned long long)(clock64() - _pe));
+#endif
     if (ld_relaxed(a.c.status) != 0) break;
   }
 }
 
-// Initial queue: every tile, in raster order (order 0) or as a checkerboard, even tiles first
-// (order 1), so that tiles processed at the same time are rarely neighbours.
+// Initial queue order.  order 0: raster.  order 1: checkerboard, even tiles first.  order 2:
+// four colours by (row parity, column parity) in the sequence (0,0), (1,1), (0,1), (1,0), so
+// that no two tiles of one colour touch, not even diagonally.  Tiles taken from the queue at
+// the same time are then rarely neighbours, and later colours read finished neighbours.
+__device__ __forceinline__ int initial_tile(int i, int ntiles, int tiles_x, int order) {
+  const int tiles_y = ntiles / tiles_x;
+  if (order == 1) {
+    int even = 0;
+    for (int ty = 0; ty < tiles_y; ++ty) even += (tiles_x + ((ty & 1) ? 0 : 1)) / 2;
+    int k = i, parity = 0;
+    if (k >= even) {
+      k -= even;
+      parity = 1;
+    }
+    int ty = 0;
+    for (;; ++ty) {
+      const int cnt = (tiles_x + (((ty & 1) ^ parity) ? 0 : 1)) / 2;
+      if (k < cnt) break;
+      k -= cnt;
+    }
+    const int first = ((ty & 1) ^ parity) ? 1 : 0;
+    return ty * tiles_x + first + 2 * k;
+  }
+  if (order == 2) {
+    const int seq_py[4] = {0, 1, 0, 1}, seq_px[4] = {0, 1, 1, 0};
+    int k = i;
+    for (int c = 0; c < 4; ++c) {
+      const int py = seq_py[c], px = seq_px[c];
+      const int ny = (tiles_y - py + 1) / 2, nx = (tiles_x - px + 1) / 2;
+      if (k < ny * nx) return (py + 2 * (k / nx)) * tiles_x + px + 2 * (k % nx);
+      k -= ny * nx;
+    }
+  }
+  return i;
+}
+
 __global__ void recon_init_kernel(Ctl c, int ntiles, int tiles_x, int order) {
-  const int half = (ntiles + 1) / 2;
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < c.cap; i += gridDim.x * blockDim.x) {
     if ((int)i < ntiles) {
-      int t = (int)i;
-      if (order == 1) {
-        // i-th even tile for i < #even, else the (i - #even)-th odd tile
-        const int ty_n = (ntiles + tiles_x - 1) / tiles_x;
-        int even = 0;
-        for (int ty = 0; ty < ty_n; ++ty) even += (tiles_x + ((ty & 1) ? 0 : 1)) / 2;
-        (void)half;
-        int k = (int)i, parity = 0;
-        if (k >= even) {
-          k -= even;
-          parity = 1;
-        }
-        // walk rows: row ty holds ceil/floor(tiles_x/2) tiles of this parity
-        int ty = 0;
-        for (;; ++ty) {
-          const int cnt = (tiles_x + (((ty & 1) ^ parity) ? 0 : 1)) / 2;
-          if (k < cnt) break;
-          k -= cnt;
-        }
-        const int first = ((ty & 1) ^ parity) ? 1 : 0;
-        t = ty * tiles_x + first + 2 * k;
-      }
-      c.slots[i].val = t;
+      c.slots[i].val = initial_tile((int)i, ntiles, tiles_x, order);
       c.slots[i].seq = i + 1u;
       c.state[i] = kQueued;
     } else {
@@ -633,19 +683,19 @@ __global__ void recon_init_kernel(Ctl c, int ntiles, int tiles_x, int order) {
 }
 
 // Workspace layout (ints): [0] status, [1..3] stats (visits, sweeps, re-runs), [6..7] visit
-// counter (64-bit), [8] head, [9] tail, [10] pending; from int kHdrInts: state[ntiles], then
-// the ring (2 ints per slot, cap slots).
+// counter (64-bit), [8] head, [9] tail, [10] pending, [16..31] phase timers (8 x 64-bit);
+// from int kHdrInts: state[ntiles], then the ring (2 ints per slot, cap slots).
 constexpr int kHdrInts = 64;
 
 template <typename T>
 int tiles_x_for(int64_t W) { return (int)((W + 32 * Px<T>::E - 1) / (32 * Px<T>::E)); }
 
-// Initial queue order (0 raster, 1 checkerboard); NSGB_RECON_ORDER overrides for experiments.
+// Initial queue order (see initial_tile); NSGB_RECON_ORDER overrides it for experiments.
 inline int recon_order() {
   static int order = -1;
   if (order < 0) {
     const char* e = getenv("NSGB_RECON_ORDER");
-    order = (e && *e) ? atoi(e) : 1;
+    order = (e && *e) ? atoi(e) : 2;
   }
   return order;
 }
@@ -677,6 +727,7 @@ cudaError_t launch_typed(void* out, const void* mask, int64_t H, int64_t W, int6
   a.c.status = wi + 0;
   a.c.stats = wi + 1;
   a.c.visit_count = (unsigned long long*)(wi + 6);
+  a.c.prof = (unsigned long long*)(wi + 16);
   a.c.head = (unsigned*)(wi + 8);
   a.c.tail = (unsigned*)(wi + 9);
   a.c.pending = wi + 10;
