@@ -1,0 +1,81 @@
+// Reconstruction entry point that needs no workspace from the caller.
+//
+// Some callers cannot allocate device memory at all: a plugin running inside a host framework
+// that has reserved the whole GPU for its own pool (a late cudaMalloc fails or fragments it),
+// a real-time pipeline that forbids allocation once it is running, or a foreign-language host
+// that only receives device buffers and has no allocator of its own to size a workspace with.
+// nsgb_imreconstruct_noalloc serves them: its scratch is a fixed-size array in this library's
+// own device memory, which every GPU that loads the library holds until the process exits.
+//
+// The scratch holds the reconstruction work queue (a status header, one state word per tile
+// and the tile ring), so the limit is a number of tiles: see NSGB_NOALLOC_SCRATCH_BYTES in
+// include/nsgb.h.  Every call clears what it uses before its kernel runs, but all calls share
+// the one array: calls whose work overlaps on the GPU (other streams, other host threads)
+// race on it and must be serialised by the caller.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+
+#include "../../include/nsgb.h"
+#include "common.cuh"
+#include "recon.cuh"
+
+namespace {
+
+// File-scope scratch in device memory.  Host code must never pass `g_noalloc_scratch`
+// itself to a kernel (on the host it is only a stand-in symbol); it uses the device address
+// that cudaGetSymbolAddress returns.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NSGB_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+void* g_scratch_ptr[kMaxDevices] = {nullptr};
+
+// Device address of the scratch on the current device, looked up once per device.
+cudaError_t scratch_address(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!g_scratch_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_scratch_ptr[dev] = p;
+  }
+  *out = g_scratch_ptr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" nsgb_status nsgb_imreconstruct_noalloc(int dtype, void* marker, const void* mask, int64_t rows,
+                                                  int64_t cols, int64_t pitch, int conn, int erode,
+                                                  nsgb_stream_t stream, const nsgb_opts* opts) {
+  const int esz = nsgb::elem_size(dtype);
+  if (!esz) return NSGB_ERR_UNSUPPORTED_DTYPE;
+  if (!marker || !mask || rows <= 0 || cols <= 0 || rows * cols >= (int64_t)INT32_MAX || pitch < cols * esz ||
+      pitch % esz != 0 || (conn != 4 && conn != 8))
+    return NSGB_ERR_BAD_ARG;
+  // Too large for the built-in scratch: refuse before touching the GPU.
+  if (nsgb::recon_workspace_bytes(dtype, rows, cols) > (size_t)NSGB_NOALLOC_SCRATCH_BYTES)
+    return NSGB_ERR_WORKSPACE;
+  void* ws = nullptr;
+  if (scratch_address(&ws) != cudaSuccess) return NSGB_ERR_CUDA;
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool ring = !erode && (dtype == NSGB_I32 || dtype == NSGB_F32);
+  if (opts && opts->recon_event_begin && cudaEventRecord((cudaEvent_t)opts->recon_event_begin, s) != cudaSuccess)
+    return NSGB_ERR_CUDA;
+  cudaError_t e = nsgb::recon_launch(dtype, marker, marker, mask, rows, cols, pitch, conn, erode != 0, ring, ws, s,
+                                     opts ? opts->max_visits_per_tile : 0, opts ? opts->max_visit_iters : 0);
+  if (e != cudaSuccess) return NSGB_ERR_CUDA;
+  if (opts && opts->recon_event_end && cudaEventRecord((cudaEvent_t)opts->recon_event_end, s) != cudaSuccess)
+    return NSGB_ERR_CUDA;
+  if (opts && !opts->sync) return NSGB_OK;
+  int dev_status = 0;
+  if (cudaMemcpyAsync(&dev_status, ws, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return NSGB_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return NSGB_ERR_CUDA;
+  return (nsgb_status)dev_status;
+}

@@ -13,6 +13,7 @@ LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libnsgb.so")
 U8, U16, I32, F32 = 0, 1, 2, 3
 OP_IMRECONSTRUCT, OP_IMRECONSTRUCT_BINARY, OP_FILL_HOLES, OP_HMIN = 0, 1, 2, 3
 OP_BWSELECT, OP_BWLABEL, OP_BWAREAOPEN, OP_CHAIN = 4, 5, 6, 7
+NOALLOC_SCRATCH_BYTES = 1 << 20  # NSGB_NOALLOC_SCRATCH_BYTES
 
 STATUS = {
     0: "NSGB_OK",
@@ -54,6 +55,7 @@ _SIGS = {
     "nsgb_status_string": (C.c_char_p, [_int]),
     "nsgb_device_status": (_int, [_vp, _vp]),
     "nsgb_imreconstruct": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _int, _int, _vp, _sz, _vp, _optp]),
+    "nsgb_imreconstruct_noalloc": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _int, _int, _vp, _optp]),
     "nsgb_imreconstruct_binary": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _int, _vp, _sz, _vp, _optp]),
     "nsgb_imfill_holes": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _int, _int, _vp, _sz, _vp, _optp]),
     "nsgb_imhmin": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _dbl, _int, _vp, _sz, _vp, _optp]),

@@ -172,6 +172,28 @@ nsgb_status nsgb_chain(int dtype, void* marker, const void* mask, int64_t rows, 
                        uint8_t* area_out, int32_t* n_labels, int32_t* n_kept, void* ws,
                        size_t ws_bytes, nsgb_stream_t stream, const nsgb_opts* opts);
 
+/* Size of the device scratch built into the library for nsgb_imreconstruct_noalloc: 1 MiB,
+ * enough for images of up to 65536 reconstruction tiles -- 134 Mpixel for u8/u16 (tiles of
+ * 32 x 64 pixels), 67 Mpixel for i32/f32 (32 x 32), e.g. 8192 x 16384 u8. */
+#define NSGB_NOALLOC_SCRATCH_BYTES (1u << 20)
+
+/* No counterpart in the reference: an extra entry point for callers that cannot allocate
+ * device memory (a plugin inside a framework that owns the whole GPU pool, a real-time loop
+ * that forbids allocation after start-up, a foreign-language host that only receives device
+ * buffers).  Same operation and arguments as nsgb_imreconstruct, but without a workspace: the
+ * scratch is a fixed NSGB_NOALLOC_SCRATCH_BYTES array in the library's own device memory,
+ * held by every GPU that loads the library until the process exits.
+ *   - Larger images are refused with NSGB_ERR_WORKSPACE before any GPU work.
+ *   - The first call on a device looks up the scratch's device address for that device
+ *     (cudaGetSymbolAddress, with that device current); make that first call before any
+ *     stream capture.
+ *   - It calls no cudaMalloc / cudaFree and no allocating library routine.
+ *   - All calls share the one scratch array and each call re-initialises it; calls whose work
+ *     overlaps on the GPU (other streams or host threads) race on it, so serialise them. */
+nsgb_status nsgb_imreconstruct_noalloc(int dtype, void* marker, const void* mask, int64_t rows,
+                                       int64_t cols, int64_t pitch, int conn, int erode,
+                                       nsgb_stream_t stream, const nsgb_opts* opts);
+
 #ifdef __cplusplus
 }
 #endif
