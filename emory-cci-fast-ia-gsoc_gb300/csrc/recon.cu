@@ -241,57 +241,50 @@ __device__ __forceinline__ void row_to_col(uint32_t (&O)[32], uint32_t* xp, int 
 }
 
 // Row pass on the row layout: left-to-right then right-to-left clamp propagation.
-// f_j(v) = min(max(v, o_j), m_j); for E = 2 each row is split over two lanes, whose
-// composed clamps (lo, hi) carry the left half's exit value into the right half.
+// f_j(v) = min(max(v, o_j), m_j).  For E = 2 each row is split over two lanes; the composed
+// clamps (lo, hi) of each half carry the value that enters the other half.  Both directions'
+// compositions are taken from the values before the pass, in one loop (independent chains):
+// the value flowing right-to-left out of the right half needs no left-to-right update, since a
+// value that went right and comes back left is bounded by the one that never left.
 template <typename T>
 __device__ __forceinline__ uint32_t row_pass(uint32_t (&O)[32], const uint32_t* mh, const WarpBuf& B, int lane) {
   using P = Px<T>;
   uint32_t acc = 0;
   if constexpr (P::E == 2) {
     const int q = lane & 15, half = lane >> 4;
-    // ---- left to right
-    {
-      uint32_t lo = P::LOW, hi = P::HIGH;
+    uint32_t lo = P::LOW, hi = P::HIGH, lo2 = P::LOW, hi2 = P::HIGH;
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const uint32_t m = mh[lane * 33 + j];
-        lo = P::vmin(P::vmax(lo, O[j]), m);
-        hi = P::vmin(P::vmax(hi, O[j]), m);
-      }
-      const uint32_t carry = P::pack(B.lv[2 * q + 1], B.lv[2 * q + 2]);
-      const uint32_t ex = P::vmin(P::vmax(carry, lo), hi);
-      const uint32_t from0 = __shfl_up_sync(NSGB_FULL, ex, 16);
-      uint32_t v = half ? from0 : carry;
-#pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const uint32_t m = mh[lane * 33 + j];
-        const uint32_t n = P::vmin(P::vmax(O[j], v), m);
-        acc |= n ^ O[j];
-        O[j] = n;
-        v = n;
-      }
+    for (int j = 0; j < 32; ++j) {
+      const uint32_t m = mh[lane * 33 + j];
+      lo = P::vmin(P::vmax(lo, O[j]), m);
+      hi = P::vmin(P::vmax(hi, O[j]), m);
+      const uint32_t m2 = mh[lane * 33 + 31 - j];
+      lo2 = P::vmin(P::vmax(lo2, O[31 - j]), m2);
+      hi2 = P::vmin(P::vmax(hi2, O[31 - j]), m2);
     }
-    // ---- right to left
-    {
-      uint32_t lo = P::LOW, hi = P::HIGH;
+    const uint32_t carry_l = P::pack(B.lv[2 * q + 1], B.lv[2 * q + 2]);
+    const uint32_t carry_r = P::pack(B.rv[2 * q + 1], B.rv[2 * q + 2]);
+    const uint32_t ex_l = P::vmin(P::vmax(carry_l, lo), hi);     // leaves the left half rightwards
+    const uint32_t ex_r = P::vmin(P::vmax(carry_r, lo2), hi2);   // leaves the right half leftwards
+    const uint32_t from0 = __shfl_up_sync(NSGB_FULL, ex_l, 16);
+    const uint32_t from1 = __shfl_down_sync(NSGB_FULL, ex_r, 16);
+    uint32_t v = half ? from0 : carry_l;
 #pragma unroll
-      for (int j = 31; j >= 0; --j) {
-        const uint32_t m = mh[lane * 33 + j];
-        lo = P::vmin(P::vmax(lo, O[j]), m);
-        hi = P::vmin(P::vmax(hi, O[j]), m);
-      }
-      const uint32_t carry = P::pack(B.rv[2 * q + 1], B.rv[2 * q + 2]);
-      const uint32_t ex = P::vmin(P::vmax(carry, lo), hi);
-      const uint32_t from1 = __shfl_down_sync(NSGB_FULL, ex, 16);
-      uint32_t v = half ? carry : from1;
+    for (int j = 0; j < 32; ++j) {
+      const uint32_t m = mh[lane * 33 + j];
+      const uint32_t n = P::vmin(P::vmax(O[j], v), m);
+      acc |= n ^ O[j];
+      O[j] = n;
+      v = n;
+    }
+    v = half ? carry_r : from1;
 #pragma unroll
-      for (int j = 31; j >= 0; --j) {
-        const uint32_t m = mh[lane * 33 + j];
-        const uint32_t n = P::vmin(P::vmax(O[j], v), m);
-        acc |= n ^ O[j];
-        O[j] = n;
-        v = n;
-      }
+    for (int j = 31; j >= 0; --j) {
+      const uint32_t m = mh[lane * 33 + j];
+      const uint32_t n = P::vmin(P::vmax(O[j], v), m);
+      acc |= n ^ O[j];
+      O[j] = n;
+      v = n;
     }
   } else {
     uint32_t v = B.lv[lane + 1];
@@ -446,32 +439,69 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int l
   const bool fast = interior && a.aligned;
   const int xl = x0 + E * lane;
 
-  uint32_t O[32];
+  // All loads of the tile and its halo are issued before any is used, so the visit waits for
+  // about one L2 round trip instead of a chain of them.
+  uint32_t O[32], M[32];
+  if (fast) {  // interior tile: straight-line vector loads, no per-element checks
 #pragma unroll
-  for (int i = 0; i < 32; ++i) {
-    const int y = y0 + i;
-    const uint32_t m = load_word<T>(a.mask, a.pitch, y, xl, H, W, fast, false, flip);
-    const uint32_t v = load_word<T>(src, a.pitch, y, xl, H, W, fast, coh, flip);
-    B.mv[lane * 33 + i] = m;
-    O[i] = init_word<T>(v, m, y, xl, H, W, ring);
+    for (int i = 0; i < 32; ++i) M[i] = load_word<T>(a.mask, a.pitch, y0 + i, xl, H, W, true, false, flip);
+#pragma unroll
+    for (int i = 0; i < 32; ++i) O[i] = load_word<T>(src, a.pitch, y0 + i, xl, H, W, true, true, flip);
+  } else {
+    // Edge or unaligned tile: bounds-checked loads in a rolled loop through shared memory
+    // (keeps this rarely used path out of the instruction cache's way).
+#pragma unroll 1
+    for (int i = 0; i < 32; ++i) {
+      B.xp[lane * 33 + i] = load_word<T>(a.mask, a.pitch, y0 + i, xl, H, W, false, false, flip);
+      B.mh[lane * 33 + i] = load_word<T>(src, a.pitch, y0 + i, xl, H, W, false, true, flip);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      M[i] = B.xp[lane * 33 + i];
+      O[i] = B.mh[lane * 33 + i];
+    }
+    __syncwarp();
   }
   // Halo rows (column layout words) and halo columns (single elements).
   const bool fast_top = fast && y0 > 0;
   const bool fast_bot = fast && y0 + kRows < H;
   const uint32_t topm = load_word<T>(a.mask, a.pitch, y0 - 1, xl, H, W, fast_top, false, flip);
-  const uint32_t topv = init_word<T>(load_word<T>(src, a.pitch, y0 - 1, xl, H, W, fast_top, coh, flip), topm,
-                                     y0 - 1, xl, H, W, ring);
+  const uint32_t topv_raw = load_word<T>(src, a.pitch, y0 - 1, xl, H, W, fast_top, coh, flip);
   const uint32_t botm = load_word<T>(a.mask, a.pitch, y0 + kRows, xl, H, W, fast_bot, false, flip);
-  const uint32_t botv = init_word<T>(load_word<T>(src, a.pitch, y0 + kRows, xl, H, W, fast_bot, coh, flip), botm,
-                                     y0 + kRows, xl, H, W, ring);
-  for (int k = lane; k < 34; k += 32) {
+  const uint32_t botv_raw = load_word<T>(src, a.pitch, y0 + kRows, xl, H, W, fast_bot, coh, flip);
+  uint32_t hm[4], hv[4];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const int k = lane + 32 * j;
     const int y = y0 - 1 + k;
-    const uint32_t lm = load_elem_at<T>(a.mask, a.pitch, y, x0 - 1, H, W, false, flip);
-    const uint32_t rm = load_elem_at<T>(a.mask, a.pitch, y, x0 + TW, H, W, false, flip);
-    B.lm[k] = lm;
-    B.rm[k] = rm;
-    B.lv[k] = init_elem<T>(load_elem_at<T>(src, a.pitch, y, x0 - 1, H, W, coh, flip), lm, y, x0 - 1, H, W, ring);
-    B.rv[k] = init_elem<T>(load_elem_at<T>(src, a.pitch, y, x0 + TW, H, W, coh, flip), rm, y, x0 + TW, H, W, ring);
+    const bool ok = k < 34;
+    hm[2 * j] = ok ? load_elem_at<T>(a.mask, a.pitch, y, x0 - 1, H, W, false, flip) : P::LOW;
+    hm[2 * j + 1] = ok ? load_elem_at<T>(a.mask, a.pitch, y, x0 + TW, H, W, false, flip) : P::LOW;
+    hv[2 * j] = ok ? load_elem_at<T>(src, a.pitch, y, x0 - 1, H, W, coh, flip) : P::LOW;
+    hv[2 * j + 1] = ok ? load_elem_at<T>(src, a.pitch, y, x0 + TW, H, W, coh, flip) : P::LOW;
+  }
+  // any_change: did this visit change a stored value (the clamp to the mask on load counts).
+  uint32_t any_change = 0;
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    B.mv[lane * 33 + i] = M[i];
+    const uint32_t v = init_word<T>(O[i], M[i], y0 + i, xl, H, W, ring);
+    any_change |= v ^ O[i];
+    O[i] = v;
+  }
+  const uint32_t topv = init_word<T>(topv_raw, topm, y0 - 1, xl, H, W, ring);
+  const uint32_t botv = init_word<T>(botv_raw, botm, y0 + kRows, xl, H, W, ring);
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const int k = lane + 32 * j;
+    if (k < 34) {
+      const int y = y0 - 1 + k;
+      B.lm[k] = hm[2 * j];
+      B.rm[k] = hm[2 * j + 1];
+      B.lv[k] = init_elem<T>(hv[2 * j], hm[2 * j], y, x0 - 1, H, W, ring);
+      B.rv[k] = init_elem<T>(hv[2 * j + 1], hm[2 * j + 1], y, x0 + TW, H, W, ring);
+    }
   }
   __syncwarp();
   // Mask in the row layout.
@@ -494,9 +524,10 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int l
   int it = 0;
   for (;;) {
     col_to_row<E>(O, B.xp, lane);
-    row_pass<T>(O, B.mh, B, lane);
+    any_change |= row_pass<T>(O, B.mh, B, lane);
     row_to_col<E>(O, B.xp, lane);
     const uint32_t acc = col_pass<T, CONN>(O, B, topv, botv, lane);
+    any_change |= acc;
     ++it;
     if (!__any_sync(NSGB_FULL, acc != 0)) break;
     if (it >= a.max_iters) {
@@ -510,9 +541,20 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int l
   }
 
   PROF_MARK(3);
-  // Write the tile back.
+  // Write the tile back, unless the visit changed nothing.
+  if (__any_sync(NSGB_FULL, any_change != 0)) {
+    if (fast) {
 #pragma unroll
-  for (int i = 0; i < 32; ++i) store_word<T>(a.out, a.pitch, y0 + i, xl, H, W, O[i], fast, flip);
+      for (int i = 0; i < 32; ++i) store_word<T>(a.out, a.pitch, y0 + i, xl, H, W, O[i], true, flip);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 32; ++i) B.xp[lane * 33 + i] = O[i];
+      __syncwarp();
+#pragma unroll 1
+      for (int i = 0; i < 32; ++i) store_word<T>(a.out, a.pitch, y0 + i, xl, H, W, B.xp[lane * 33 + i], false, flip);
+      __syncwarp();
+    }
+  }
 
   PROF_MARK(4);
   // Which neighbouring tiles could be raised by the new border values?
@@ -695,7 +737,7 @@ inline int recon_order() {
   static int order = -1;
   if (order < 0) {
     const char* e = getenv("NSGB_RECON_ORDER");
-    order = (e && *e) ? atoi(e) : 2;
+    order = (e && *e) ? atoi(e) : 1;
   }
   return order;
 }
