@@ -1,0 +1,67 @@
+// Image tables: every kernel works on a batch of images (a single-image call is a batch of
+// one).  Work items of all images (reconstruction tiles, labelling tiles, rank blocks, rows)
+// are numbered consecutively; each image records where its range starts, and a kernel finds
+// the image of a work item with a binary search over those starts.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nsgb {
+
+struct Img {
+  void* plane;        // reconstruction: marker in / result out; labelling: the classified image
+  const void* aux;    // reconstruction: mask; bwselect: seeds
+  int64_t pitch;      // bytes, for plane and aux
+  int H, W;
+  int aligned;        // plane / aux aligned for vector tile loads
+  int r_tiles_x, r_tiles_y, r_tile_base;  // reconstruction tiles
+  int c_tiles_x, c_tile_base;             // 32x32 labelling tiles
+  int px_base;        // first pixel in the concatenated label planes
+  int blk_base;       // first 1024-pixel rank block
+  int row_base;       // first row in the concatenated row space
+  // outputs of the chain (dense rows, may be null)
+  uint8_t* fill;
+  int32_t* labels;
+  uint8_t* area;
+};
+
+struct Imgs {
+  const Img* d;  // device table (batches), or null: a single image passed in `one`
+  int n;
+  Img one;       // the image itself when d == null (kernel parameter, no table needed)
+};
+
+__device__ __forceinline__ Img img_at(const Imgs& I, int i) { return I.d ? I.d[i] : I.one; }
+
+// Largest image index whose range start (selected by `field`) is <= key.
+template <typename F>
+__device__ __forceinline__ int img_of(const Imgs& I, int key, F field) {
+  if (!I.d) return 0;
+  int lo = 0, hi = I.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (field(I.d[mid]) <= key) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+struct RTileBase { __device__ int operator()(const Img& m) const { return m.r_tile_base; } };
+struct CTileBase { __device__ int operator()(const Img& m) const { return m.c_tile_base; } };
+struct BlkBase { __device__ int operator()(const Img& m) const { return m.blk_base; } };
+struct RowBase { __device__ int operator()(const Img& m) const { return m.row_base; } };
+
+// Totals of a batch, known on the host (grid sizes).
+struct BatchTotals {
+  int n;
+  int64_t px;      // total pixels (< 2^31)
+  int r_tiles;     // reconstruction tiles
+  int c_tiles;     // labelling tiles
+  int blocks;      // rank blocks
+  int rows;        // total rows
+  int max_w;       // widest image
+  int perimeter_max;  // largest 2*(H+W)
+};
+
+}  // namespace nsgb

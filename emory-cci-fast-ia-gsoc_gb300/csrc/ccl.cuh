@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "batch.cuh"
 #include "common.cuh"
 
 namespace nsgb {
@@ -91,11 +92,13 @@ __device__ __forceinline__ void g_union(int* L, int a, int b) {
   }
 }
 
-// Output of a labelling: L (dense H x W int32, index y*W + x; -1 = background) where every
-// foreground pixel points at its tile-local root and, after ccl_flatten_roots, every local
-// root points at the global root, so root(i) = L[L[i]] (one hop).  A (optional) holds the
-// pixel count of each local root, then of each global root.  `roots` lists the local roots
-// (global indices), `nroots` counts them.
+// Output of a labelling over a batch of images: L (int32, one dense plane per image at
+// Img::px_base, pixel index = px_base + y*W + x; -1 = background).  Every foreground pixel
+// points at its tile-local root and, after ccl_flatten_roots, every local root points at the
+// global root, so root(i) = L[L[i]] (one hop).  Indices are global (px_base included), so a
+// root is px_base + the smallest raster index of the component.  A (optional) holds the pixel
+// count of each local root, then of each global root.  `roots` lists the local roots,
+// `nroots` counts them.
 struct Forest {
   int* L;
   int* A;
@@ -108,24 +111,41 @@ __device__ __forceinline__ int root_of(const int* L, int64_t i) {
   return l < 0 ? -1 : __ldcg(L + l);
 }
 
+// Labelling tile of CTA `b`: image, tile origin.
+struct TileAt {
+  Img m;
+  int x0, y0;
+};
+__device__ __forceinline__ TileAt tile_at(const Imgs& I, int b) {
+  TileAt t;
+  t.m = img_at(I, img_of(I, b, CTileBase()));
+  const int lt = b - t.m.c_tile_base;
+  const int ty = lt / t.m.c_tiles_x;
+  t.x0 = (lt - ty * t.m.c_tiles_x) * kTile;
+  t.y0 = ty * kTile;
+  return t;
+}
+
 // Each warp owns tile rows (lane = column).  Runs of equal class along a row are found with a
 // ballot and start out joined (label = run start), so unions are only needed where runs of
 // adjacent rows touch: at a pixel that starts its run or sits under the start of a run above
 // (and, for 8-connectivity, diagonally past the two ends of the run).  That is one union per
-// touching pair of runs instead of one per pixel pair.
+// touching pair of runs instead of one per pixel pair.  One CTA per labelling tile (1-D grid
+// over the tiles of all images).
 template <class Cls, int CONN>
-__global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, int H, int W, Forest f) {
+__global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f) {
   __shared__ int s_lab[kTile * kTile];
   __shared__ int s_cnt[kTile * kTile];
   __shared__ uint8_t s_c[kTile * kTile];
-  const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile;
+  const TileAt T = tile_at(I, blockIdx.x);
+  const int x0 = T.x0, y0 = T.y0, H = T.m.H, W = T.m.W, pb = T.m.px_base;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   uint8_t c[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int ly = ty + 8 * k, i = ly * kTile + tx;
     const int gy = y0 + ly, gx = x0 + tx;
-    c[k] = (uint8_t)((gy < H && gx < W) ? cls(gy, gx) : 0u);
+    c[k] = (uint8_t)((gy < H && gx < W) ? cls(T.m, gy, gx) : 0u);
     s_c[i] = c[k];
     s_cnt[i] = 0;
   }
@@ -179,8 +199,8 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, int H, int W, For
     const int gy = y0 + ly, gx = x0 + tx;
     const bool in = gy < H && gx < W;
     const int r = root[k];
-    const int g = gy * W + gx;
-    if (in) f.L[g] = r < 0 ? -1 : (y0 + r / kTile) * W + x0 + (r % kTile);
+    const int g = pb + gy * W + gx;
+    if (in) f.L[g] = r < 0 ? -1 : pb + (y0 + r / kTile) * W + x0 + (r % kTile);
     const bool is_root = in && r == i;
     const unsigned rb = __ballot_sync(NSGB_FULL, is_root);
     if (rb) {
@@ -195,15 +215,16 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, int H, int W, For
   }
 }
 
-// Joins runs across tile edges.  Two warps per tile: warp 0 takes the bottom edge (row
-// y0+31 against row y0+32), warp 1 the right edge (column x0+31 against column x0+32, the
+// Joins runs across tile edges.  Two warps per labelling tile: warp 0 takes the bottom edge
+// (row y0+31 against row y0+32), warp 1 the right edge (column x0+31 against column x0+32, the
 // same logic transposed).  With `a` = the pixel on this side and `b` its partner across the
 // edge, runs of equal class along the edge are found with ballots, and a union is made only
 // where a run on the far side starts or where a near-side run starts under a far-side run,
 // plus the two diagonal ends of each far-side run for 8-connectivity.
 template <class Cls, int CONN>
-__global__ void __launch_bounds__(64) ccl_merge(Cls cls, int H, int W, int* __restrict__ L) {
-  const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile;
+__global__ void __launch_bounds__(64) ccl_merge(Cls cls, Imgs I, int* __restrict__ L) {
+  const TileAt T = tile_at(I, blockIdx.x);
+  const int x0 = T.x0, y0 = T.y0, H = T.m.H, W = T.m.W, pb = T.m.px_base;
   const int lane = threadIdx.x & 31;
   const bool bottom = (threadIdx.x >> 5) == 0;
   // coordinates of the near pixel (a) and the far pixel (b) for this lane
@@ -223,8 +244,8 @@ __global__ void __launch_bounds__(64) ccl_merge(Cls cls, int H, int W, int* __re
   }
   const bool in_a = ay < H && ax < W;
   const bool in_b = by < H && bx < W;
-  const uint32_t ca = in_a ? cls(ay, ax) : 0u;
-  const uint32_t cb = in_b ? cls(by, bx) : 0u;
+  const uint32_t ca = in_a ? cls(T.m, ay, ax) : 0u;
+  const uint32_t cb = in_b ? cls(T.m, by, bx) : 0u;
   // runs along the edge (lane order) on each side
   const uint32_t ca_prev = __shfl_up_sync(NSGB_FULL, ca, 1);
   const uint32_t cb_prev = __shfl_up_sync(NSGB_FULL, cb, 1);
@@ -233,17 +254,17 @@ __global__ void __launch_bounds__(64) ccl_merge(Cls cls, int H, int W, int* __re
   const bool b_start = cb != 0 && !(lane > 0 && cb_prev == cb);
   const bool b_end = cb != 0 && !(lane < 31 && cb_next == cb);
   if (cb == 0) return;
-  const int pb = by * W + bx;
-  if (ca == cb && (a_start || b_start)) g_union(L, pb, ay * W + ax);
+  const int qb = pb + by * W + bx;
+  if (ca == cb && (a_start || b_start)) g_union(L, qb, pb + ay * W + ax);
   if (CONN == 8) {
     // diagonal partners one step before the start / after the end of the far-side run
     if (b_start) {
       const int dy = bottom ? ay : ay - 1, dx = bottom ? ax - 1 : ax;
-      if (dy >= 0 && dx >= 0 && dy < H && dx < W && cls(dy, dx) == cb) g_union(L, pb, dy * W + dx);
+      if (dy >= 0 && dx >= 0 && dy < H && dx < W && cls(T.m, dy, dx) == cb) g_union(L, qb, pb + dy * W + dx);
     }
     if (b_end) {
       const int dy = bottom ? ay : ay + 1, dx = bottom ? ax + 1 : ax;
-      if (dy < H && dx < W && cls(dy, dx) == cb) g_union(L, pb, dy * W + dx);
+      if (dy < H && dx < W && cls(T.m, dy, dx) == cb) g_union(L, qb, pb + dy * W + dx);
     }
   }
 }
@@ -261,45 +282,58 @@ static __global__ void ccl_flatten_roots(Forest f, int max_roots) {
   }
 }
 
-// Seed pixels set bit root(p) in `bits`.  One thread per pixel (row / column grid).
-template <class Seed>
-__global__ void ccl_seed_pixels(int H, int W, const int* __restrict__ L, Seed seed, unsigned* __restrict__ bits) {
+__device__ __forceinline__ void set_root_bit(unsigned* bits, int r) {
+  const unsigned bit = 1u << (r & 31);
+  if (!(__ldcg(&bits[r >> 5]) & bit)) atomicOr(&bits[r >> 5], bit);
+}
+
+// Row grid over the rows of all images: x = column (blockIdx.x * blockDim.x + threadIdx.x),
+// blockIdx.y strides the concatenated rows; f(image, y, x) runs for every pixel.
+template <class F>
+__device__ __forceinline__ void for_batch_pixels(const Imgs& I, int total_rows, F&& f) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= W) return;
-  for (int y = blockIdx.y; y < H; y += gridDim.y) {
-    if (!seed(y, x)) continue;
-    const int r = root_of(L, (int64_t)y * W + x);
-    if (r < 0) continue;
-    const unsigned bit = 1u << (r & 31);
-    if (!(__ldcg(&bits[r >> 5]) & bit)) atomicOr(&bits[r >> 5], bit);
+  for (int gr = blockIdx.y; gr < total_rows; gr += gridDim.y) {
+    const Img m = img_at(I, img_of(I, gr, RowBase()));
+    if (x < m.W) f(m, gr - m.row_base, x);
   }
 }
 
-// Seed pixels on the image border only: thread k walks the border (top row, bottom row, left
-// column, right column).
+// Seed pixels set bit root(p) in `bits`.
 template <class Seed>
-__global__ void ccl_seed_border(int H, int W, const int* __restrict__ L, Seed seed, unsigned* __restrict__ bits) {
-  const int64_t per = 2 * (int64_t)W + 2 * (int64_t)H;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < per; k += (int64_t)gridDim.x * blockDim.x) {
+__global__ void ccl_seed_pixels(Imgs I, int total_rows, const int* __restrict__ L, Seed seed,
+                                unsigned* __restrict__ bits) {
+  for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
+    if (!seed(m, y, x)) return;
+    const int r = root_of(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
+    if (r >= 0) set_root_bit(bits, r);
+  });
+}
+
+// Seed pixels on each image's border only: blockIdx.y = image, x walks its border (top row,
+// bottom row, left column, right column).
+template <class Seed>
+__global__ void ccl_seed_border(Imgs I, const int* __restrict__ L, Seed seed, unsigned* __restrict__ bits) {
+  const Img m = img_at(I, blockIdx.y);
+  const int H = m.H, W = m.W;
+  const int per = 2 * W + 2 * H;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < per; k += gridDim.x * blockDim.x) {
     int y, x;
     if (k < W) {
       y = 0;
-      x = (int)k;
-    } else if (k < 2 * (int64_t)W) {
+      x = k;
+    } else if (k < 2 * W) {
       y = H - 1;
-      x = (int)(k - W);
-    } else if (k < 2 * (int64_t)W + H) {
-      y = (int)(k - 2 * (int64_t)W);
+      x = k - W;
+    } else if (k < 2 * W + H) {
+      y = k - 2 * W;
       x = 0;
     } else {
-      y = (int)(k - 2 * (int64_t)W - H);
+      y = k - 2 * W - H;
       x = W - 1;
     }
-    if (!seed(y, x)) continue;
-    const int r = root_of(L, (int64_t)y * W + x);
-    if (r < 0) continue;
-    const unsigned bit = 1u << (r & 31);
-    if (!(__ldcg(&bits[r >> 5]) & bit)) atomicOr(&bits[r >> 5], bit);
+    if (!seed(m, y, x)) continue;
+    const int r = root_of(L, (int64_t)m.px_base + (int64_t)y * W + x);
+    if (r >= 0) set_root_bit(bits, r);
   }
 }
 
@@ -310,35 +344,35 @@ __device__ __forceinline__ bool test_bit(const unsigned* bits, int r) {
 }
 
 // Host helpers (ccl.cu).
-inline dim3 tile_grid(int H, int W) { return dim3((W + kTile - 1) / kTile, (H + kTile - 1) / kTile); }
 int flat_grid(int64_t n);
-// Grid for the row / column kernels: x covers the columns (256 per block), y strides rows.
-inline dim3 rowcol_grid(int H, int W) {
-  return dim3((W + 255) / 256, (unsigned)(H < 65535 ? H : 65535));
+// Row grids: x covers the widest image (256 columns per block), y strides the rows.
+inline dim3 rowcol_grid(int total_rows, int max_w) {
+  return dim3((max_w + 255) / 256, (unsigned)(total_rows < 65535 ? total_rows : 65535));
 }
 
-// Labels the image: local pass, edge merge, root flattening.  Afterwards root(i) = L[L[i]].
+// Labels every image of the batch: local pass, edge merge, root flattening.  Afterwards
+// root(i) = L[L[i]].
 template <class Cls>
-cudaError_t label(const Cls& cls, int H, int W, int conn, const Forest& f, cudaStream_t s) {
-  const dim3 g = tile_grid(H, W);
+cudaError_t label(const Cls& cls, const Imgs& I, const BatchTotals& t, int conn, const Forest& f, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(f.nroots, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
   if (conn == 8) {
-    ccl_local<Cls, 8><<<g, kThreads, 0, s>>>(cls, H, W, f);
-    ccl_merge<Cls, 8><<<g, 64, 0, s>>>(cls, H, W, f.L);
+    ccl_local<Cls, 8><<<t.c_tiles, kThreads, 0, s>>>(cls, I, f);
+    ccl_merge<Cls, 8><<<t.c_tiles, 64, 0, s>>>(cls, I, f.L);
   } else {
-    ccl_local<Cls, 4><<<g, kThreads, 0, s>>>(cls, H, W, f);
-    ccl_merge<Cls, 4><<<g, 64, 0, s>>>(cls, H, W, f.L);
+    ccl_local<Cls, 4><<<t.c_tiles, kThreads, 0, s>>>(cls, I, f);
+    ccl_merge<Cls, 4><<<t.c_tiles, 64, 0, s>>>(cls, I, f.L);
   }
-  ccl_flatten_roots<<<flat_grid((int64_t)H * W / 4 + 1), 256, 0, s>>>(f, H * W);
+  ccl_flatten_roots<<<flat_grid(t.px / 4 + 1), 256, 0, s>>>(f, (int)t.px);
   return cudaGetLastError();
 }
 
 // Raster-order ranks of the roots: rank[r] = number of roots before r (only written at roots),
 // total roots and (if A) the number of roots whose area lies in [lo, hi) go to counts[0..1].
-cudaError_t rank_roots(const int* L, const int* A, int64_t n, int lo, int hi, int* rank, int* block_tmp,
-                       int* counts, cudaStream_t s);
-size_t rank_tmp_ints(int64_t n);
+// counts[2*i] / counts[2*i+1] for image i.  block_tmp: 2 ints per rank block.
+cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const int* L, const int* A, int lo, int hi, int* rank,
+                       int* block_tmp, int* counts, cudaStream_t s);
+constexpr int kBlockPx = 1024;
 
 }  // namespace ccl
 }  // namespace nsgb

@@ -1,14 +1,18 @@
 // The operations of the reconstruction / labelling path and their C ABI (include/nsgb.h).
 // Each operation is a short sequence of kernels on the caller's stream, using only the
-// caller's workspace.  Reference functions are cited at each entry point.
+// caller's workspace.  All kernels take an image table (batch.cuh); a single-image call is a
+// batch of one whose image is passed by value.  Reference functions are cited at each entry
+// point.
 #include <cuda_runtime.h>
 #include <limits.h>
 #include <stdint.h>
 #include <string.h>
 
 #include <limits>
+#include <vector>
 
 #include "../../include/nsgb.h"
+#include "batch.cuh"
 #include "ccl.cuh"
 #include "common.cuh"
 #include "recon.cuh"
@@ -19,157 +23,163 @@ namespace {
 // ------------------------------------------------------------------------------------------
 // Pixel access helpers.
 template <typename T>
-__device__ __forceinline__ T px(const T* base, int64_t pitch, int y, int x) {
+__device__ __forceinline__ T px(const void* base, int64_t pitch, int y, int x) {
   return __ldg((const T*)((const char*)base + (int64_t)y * pitch) + x);
 }
 template <typename T>
-__device__ __forceinline__ T pxcg(const T* base, int64_t pitch, int y, int x) {
+__device__ __forceinline__ T pxcg(const void* base, int64_t pitch, int y, int x) {
   return __ldcg((const T*)((const char*)base + (int64_t)y * pitch) + x);
 }
 template <typename T>
-__device__ __forceinline__ T* pxp(T* base, int64_t pitch, int y, int x) {
+__device__ __forceinline__ T* pxp(void* base, int64_t pitch, int y, int x) {
   return (T*)((char*)base + (int64_t)y * pitch) + x;
 }
 
 // ------------------------------------------------------------------------------------------
-// Classifiers (class 0 = background; equal non-zero classes are joined).
+// Classifiers (class 0 = background; equal non-zero classes are joined).  They read the
+// image's plane (Img::plane) or aux plane.
 struct ClsValueU8 {  // bwlabel: the pixel value
-  const uint8_t* img;
-  int64_t pitch;
-  __device__ uint32_t operator()(int y, int x) const { return px(img, pitch, y, x); }
+  __device__ uint32_t operator()(const Img& m, int y, int x) const { return px<uint8_t>(m.plane, m.pitch, y, x); }
 };
-template <typename T>
-struct ClsNonZero {  // binary reconstruction, bwselect: mask != 0
-  const T* img;
-  int64_t pitch;
-  __device__ uint32_t operator()(int y, int x) const { return px(img, pitch, y, x) != (T)0 ? 1u : 0u; }
-};
-template <typename T>
-struct ClsNotMax {  // binary hole filling: pixels that are not foreground (max<T>)
-  const T* img;
-  int64_t pitch;
-  __device__ uint32_t operator()(int y, int x) const {
-    return px(img, pitch, y, x) != std::numeric_limits<T>::max() ? 1u : 0u;
+struct ClsDenseU8 {  // the chain's filled image F in the workspace (dense, at px_base)
+  const uint8_t* F;
+  __device__ uint32_t operator()(const Img& m, int y, int x) const {
+    return __ldg(F + m.px_base + (int64_t)y * m.W + x);
   }
 };
 template <typename T>
-struct ClsNotAbove {  // hole filling of (R > thr): the complement class !(R > thr)
-  const T* img;
-  int64_t pitch;
+struct ClsNonZero {  // binary reconstruction (mask = aux), bwselect (image = plane)
+  bool use_aux;
+  __device__ uint32_t operator()(const Img& m, int y, int x) const {
+    return px<T>(use_aux ? m.aux : m.plane, m.pitch, y, x) != (T)0 ? 1u : 0u;
+  }
+};
+template <typename T>
+struct ClsNotMax {  // binary hole filling: pixels that are not foreground (max<T>)
+  __device__ uint32_t operator()(const Img& m, int y, int x) const {
+    return px<T>(m.plane, m.pitch, y, x) != std::numeric_limits<T>::max() ? 1u : 0u;
+  }
+};
+template <typename T>
+struct ClsNotAbove {  // hole filling of (R > thr): the complement class !(R > thr); R = plane
   double thr;
-  __device__ uint32_t operator()(int y, int x) const { return !((double)pxcg(img, pitch, y, x) > thr) ? 1u : 0u; }
+  __device__ uint32_t operator()(const Img& m, int y, int x) const {
+    return !((double)pxcg<T>(m.plane, m.pitch, y, x) > thr) ? 1u : 0u;
+  }
 };
 
 // Seeds (pixels that flag their component's root).
 template <class Cls>
 struct SeedBorder {
   Cls cls;
-  int H, W;
-  __device__ bool operator()(int y, int x) const {
-    return (y == 0 || y == H - 1 || x == 0 || x == W - 1) && cls(y, x) != 0u;
-  }
+  __device__ bool operator()(const Img& m, int y, int x) const { return cls(m, y, x) != 0u; }
 };
 template <typename T>
-struct SeedBoth {  // marker != 0 and mask != 0
-  const T* a;
-  const T* b;
-  int64_t pitch;
-  __device__ bool operator()(int y, int x) const {
-    return pxcg(a, pitch, y, x) != (T)0 && px(b, pitch, y, x) != (T)0;
+struct SeedBoth {  // a != 0 and b != 0, with a = plane or aux as selected
+  bool a_is_plane;
+  __device__ bool operator()(const Img& m, int y, int x) const {
+    const void* a = a_is_plane ? m.plane : m.aux;
+    const void* b = a_is_plane ? m.aux : m.plane;
+    return pxcg<T>(a, m.pitch, y, x) != (T)0 && px<T>(b, m.pitch, y, x) != (T)0;
   }
 };
 
 // ------------------------------------------------------------------------------------------
-// Output kernels.  Row / column grids (x = column, y strides rows); a pixel's root is
-// L[L[i]] after the labelling (ccl::root_of).
+// Output kernels (row grids over all images; a pixel's root is L[L[i]]).
 
 // Binary hole filling: 0 where the non-foreground pixel's component touches the border.
+// Writes the workspace plane F (dense, if given) and the caller's output (single image:
+// `out` / `pitch_out`; batch: Img::fill, dense).
 template <typename TO>
-__global__ void fill_out_kernel(int H, int W, const int* __restrict__ L, const unsigned* __restrict__ bits, TO* out,
-                                int64_t pitch_out, TO fg) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= W) return;
-  for (int y = blockIdx.y; y < H; y += gridDim.y) {
-    const int r = ccl::root_of(L, (int64_t)y * W + x);
-    *pxp(out, pitch_out, y, x) = (r >= 0 && ccl::test_bit(bits, r)) ? (TO)0 : fg;
-  }
+__global__ void fill_out_kernel(Imgs I, int total_rows, const int* __restrict__ L, const unsigned* __restrict__ bits,
+                                uint8_t* F, TO* out, int64_t pitch_out, TO fg) {
+  ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
+    const int64_t gi = (int64_t)m.px_base + (int64_t)y * m.W + x;
+    const int r = ccl::root_of(L, gi);
+    const bool hole_free = r >= 0 && ccl::test_bit(bits, r);
+    const TO v = hole_free ? (TO)0 : fg;
+    if (F) F[gi] = (uint8_t)v;
+    if (!I.d) {
+      if (out) *pxp<TO>(out, pitch_out, y, x) = v;
+    } else if (m.fill) {
+      ((TO*)m.fill)[(int64_t)y * m.W + x] = v;
+    }
+  });
 }
 
-// Binary reconstruction output, in place on the marker.
+// Binary reconstruction output, in place on the marker (= plane).
 template <typename T>
-__global__ void binrecon_out_kernel(T* marker, int64_t pitch, int H, int W, const int* __restrict__ L,
+__global__ void binrecon_out_kernel(Imgs I, int total_rows, const int* __restrict__ L,
                                     const unsigned* __restrict__ bits) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= W) return;
-  for (int y = blockIdx.y; y < H; y += gridDim.y) {
-    T* p = pxp(marker, pitch, y, x);
-    if (*p != (T)0) continue;
-    const int r = ccl::root_of(L, (int64_t)y * W + x);
+  ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
+    T* p = pxp<T>(m.plane, m.pitch, y, x);
+    if (*p != (T)0) return;
+    const int r = ccl::root_of(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
     if (r >= 0 && ccl::test_bit(bits, r)) *p = std::numeric_limits<T>::max();
-  }
+  });
 }
 
 template <typename T>
-__global__ void bwselect_out_kernel(const T* image, T* out, int64_t pitch, int H, int W, const int* __restrict__ L,
+__global__ void bwselect_out_kernel(Imgs I, int total_rows, void* out, const int* __restrict__ L,
                                     const unsigned* __restrict__ bits) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= W) return;
-  for (int y = blockIdx.y; y < H; y += gridDim.y) {
-    const T v = px(image, pitch, y, x);
-    const int r = ccl::root_of(L, (int64_t)y * W + x);
-    *pxp(out, pitch, y, x) = (v != (T)0 && r >= 0 && ccl::test_bit(bits, r)) ? v : (T)0;
-  }
+  ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
+    const T v = px<T>(m.plane, m.pitch, y, x);
+    const int r = ccl::root_of(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
+    *pxp<T>(out, m.pitch, y, x) = (v != (T)0 && r >= 0 && ccl::test_bit(bits, r)) ? v : (T)0;
+  });
 }
 
-// Labels out: relabel ? (bg 0, root's rank + 1) : root index / -1.  Optional area-filter
-// outputs from the same pass.  rank / A are read-only here: L1-cached loads, because a giant
-// component's root is read by every one of its pixels.
-__global__ void label_out_kernel(int H, int W, const int* __restrict__ L, const int* __restrict__ rank, int relabel,
-                                 int32_t* labels, int64_t pitch_labels, const int* __restrict__ A, int lo, int hi,
-                                 int32_t* kept_labels, int64_t pitch_kept, uint8_t* flat, int64_t pitch_flat) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= W) return;
-  for (int y = blockIdx.y; y < H; y += gridDim.y) {
-    const int r = ccl::root_of(L, (int64_t)y * W + x);
-    if (labels) *pxp(labels, pitch_labels, y, x) = relabel ? (r < 0 ? 0 : __ldg(&rank[r]) + 1) : r;
+// Labels out: relabel ? (bg 0, root's rank + 1) : the root's raster index in its image / -1.
+// Optional area-filter outputs from the same pass.  rank / A are read-only here: L1-cached
+// loads, because a giant component's root is read by every one of its pixels.  Single image:
+// explicit output pointers / pitches; batch: Img::labels / Img::area (dense).
+__global__ void label_out_kernel(Imgs I, int total_rows, const int* __restrict__ L, const int* __restrict__ rank,
+                                 int relabel, int32_t* labels, int64_t pitch_labels, const int* __restrict__ A, int lo,
+                                 int hi, int32_t* kept_labels, int64_t pitch_kept, uint8_t* flat, int64_t pitch_flat) {
+  ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
+    const int r = ccl::root_of(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
+    const int lab = relabel ? (r < 0 ? 0 : __ldg(&rank[r]) + 1) : (r < 0 ? -1 : r - m.px_base);
+    bool keep = false;
     if (A) {
       const int a = r >= 0 ? __ldg(&A[r]) : 0;
-      const bool keep = r >= 0 && a >= lo && a < hi;
-      if (kept_labels) *pxp(kept_labels, pitch_kept, y, x) = keep ? r : -1;
-      if (flat) *pxp(flat, pitch_flat, y, x) = keep ? 255 : 0;
+      keep = r >= 0 && a >= lo && a < hi;
     }
-  }
+    if (!I.d) {
+      if (labels) *pxp<int32_t>(labels, pitch_labels, y, x) = lab;
+      if (A && kept_labels) *pxp<int32_t>(kept_labels, pitch_kept, y, x) = keep ? r - m.px_base : -1;
+      if (A && flat) *pxp<uint8_t>(flat, pitch_flat, y, x) = keep ? 255 : 0;
+    } else {
+      const int64_t li = (int64_t)y * m.W + x;
+      if (m.labels) m.labels[li] = lab;
+      if (A && m.area) m.area[li] = keep ? 255 : 0;
+    }
+  });
 }
 
 // Area of arbitrary int32 labels in [-1, n): dense histogram (background -1 skipped).
-__global__ void label_hist_kernel(const int32_t* lab, int64_t pitch, int H, int W, int* __restrict__ A, int* status) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= W) return;
-  const int64_t n = (int64_t)H * W;
-  for (int y = blockIdx.y; y < H; y += gridDim.y) {
-    const int l = px(lab, pitch, y, x);
-    if (l == -1) continue;
+__global__ void label_hist_kernel(Imgs I, int total_rows, int* __restrict__ A, int* status) {
+  ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
+    const int64_t n = (int64_t)m.H * m.W;
+    const int l = px<int32_t>(m.plane, m.pitch, y, x);
+    if (l == -1) return;
     if (l < -1 || (int64_t)l >= n) {
       set_status(status, NSGB_ERR_BAD_ARG);
-      continue;
+      return;
     }
     atomicAdd(&A[l], 1);
-  }
+  });
 }
 
-__global__ void labeled_area_out_kernel(const int32_t* lab, int64_t pitch, int H, int W, const int* __restrict__ A,
-                                        int lo, int hi, int32_t* kept_labels, int64_t pitch_kept, uint8_t* flat,
-                                        int64_t pitch_flat) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= W) return;
-  const int64_t n = (int64_t)H * W;
-  for (int y = blockIdx.y; y < H; y += gridDim.y) {
-    const int l = px(lab, pitch, y, x);
+__global__ void labeled_area_out_kernel(Imgs I, int total_rows, const int* __restrict__ A, int lo, int hi,
+                                        int32_t* kept_labels, int64_t pitch_kept, uint8_t* flat, int64_t pitch_flat) {
+  ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
+    const int64_t n = (int64_t)m.H * m.W;
+    const int l = px<int32_t>(m.plane, m.pitch, y, x);
     const int a = (l >= 0 && (int64_t)l < n) ? __ldg(&A[l]) : 0;
     const bool keep = l >= 0 && (int64_t)l < n && a >= lo && a < hi;
-    if (kept_labels) *pxp(kept_labels, pitch_kept, y, x) = keep ? l : -1;
-    if (flat) *pxp(flat, pitch_flat, y, x) = keep ? 255 : 0;
-  }
+    if (kept_labels) *pxp<int32_t>(kept_labels, pitch_kept, y, x) = keep ? l : -1;
+    if (flat) *pxp<uint8_t>(flat, pitch_flat, y, x) = keep ? 255 : 0;
+  });
 }
 
 __global__ void count_labels_in_range_kernel(const int* __restrict__ A, int64_t n, int lo, int hi, int* out) {
@@ -183,7 +193,7 @@ __global__ void count_labels_in_range_kernel(const int* __restrict__ A, int64_t 
 }
 
 // ------------------------------------------------------------------------------------------
-// Elementwise kernels (row / column grids).
+// Elementwise kernels on one image (row / column grids).
 #define NSGB_FOR_PIXELS                                   \
   const int x = blockIdx.x * blockDim.x + threadIdx.x;    \
   if (x >= W) return;                                     \
@@ -192,7 +202,7 @@ __global__ void count_labels_in_range_kernel(const int* __restrict__ A, int64_t 
 template <typename T>
 __global__ void threshold_kernel(const T* in, int64_t pitch_in, uint8_t* out, int64_t pitch_out, int H, int W,
                                  double thr) {
-  NSGB_FOR_PIXELS { *pxp(out, pitch_out, y, x) = (double)px(in, pitch_in, y, x) > thr ? 255 : 0; }
+  NSGB_FOR_PIXELS { *pxp<uint8_t>(out, pitch_out, y, x) = (double)px<T>(in, pitch_in, y, x) > thr ? 255 : 0; }
 }
 
 template <typename T>
@@ -210,7 +220,7 @@ __device__ __forceinline__ T invert_value(T v) {
 
 template <typename T>
 __global__ void invert_kernel(const T* in, T* out, int64_t pitch, int H, int W) {
-  NSGB_FOR_PIXELS { *pxp(out, pitch, y, x) = invert_value(px(in, pitch, y, x)); }
+  NSGB_FOR_PIXELS { *pxp<T>(out, pitch, y, x) = invert_value(px<T>(in, pitch, y, x)); }
 }
 
 // Hole-filling marker: the image on the border, max<T> inside.
@@ -218,7 +228,7 @@ template <typename T>
 __global__ void fill_marker_kernel(const T* image, T* out, int64_t pitch, int H, int W) {
   NSGB_FOR_PIXELS {
     const bool border = y == 0 || y == H - 1 || x == 0 || x == W - 1;
-    *pxp(out, pitch, y, x) = border ? px(image, pitch, y, x) : std::numeric_limits<T>::max();
+    *pxp<T>(out, pitch, y, x) = border ? px<T>(image, pitch, y, x) : std::numeric_limits<T>::max();
   }
 }
 
@@ -226,7 +236,7 @@ __global__ void fill_marker_kernel(const T* image, T* out, int64_t pitch, int H,
 template <typename T>
 __global__ void hmin_marker_kernel(const T* image, T* out, int64_t pitch, int H, int W, double h) {
   NSGB_FOR_PIXELS {
-    const T v = px(image, pitch, y, x);
+    const T v = px<T>(image, pitch, y, x);
     T r;
     if constexpr (std::numeric_limits<T>::is_integer) {
       const int64_t s = (int64_t)v + (int64_t)h;
@@ -234,17 +244,72 @@ __global__ void hmin_marker_kernel(const T* image, T* out, int64_t pitch, int H,
     } else {
       r = v + (T)h;
     }
-    *pxp(out, pitch, y, x) = r;
+    *pxp<T>(out, pitch, y, x) = r;
   }
 }
 
 template <typename T>
 __global__ void fill_const_kernel(T* out, int64_t pitch, int H, int W, T v) {
-  NSGB_FOR_PIXELS { *pxp(out, pitch, y, x) = v; }
+  NSGB_FOR_PIXELS { *pxp<T>(out, pitch, y, x) = v; }
 }
 
 // ------------------------------------------------------------------------------------------
-// Workspace layout.  [recon region][L: N ints][A: N ints][R: N ints][bits][rank tmp][F: N bytes]
+// Plans and workspace.
+
+struct Plan {
+  Imgs I;
+  BatchTotals t;
+};
+
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// Fills the labelling / rank / row fields of `m` and advances the running totals.
+void add_image(Img& m, BatchTotals& t) {
+  m.c_tiles_x = (m.W + ccl::kTile - 1) / ccl::kTile;
+  const int c_tiles_y = (m.H + ccl::kTile - 1) / ccl::kTile;
+  m.r_tile_base = t.r_tiles;
+  m.c_tile_base = t.c_tiles;
+  m.px_base = (int)t.px;
+  m.blk_base = t.blocks;
+  m.row_base = t.rows;
+  const int64_t npx = (int64_t)m.H * m.W;
+  t.r_tiles += m.r_tiles_x * m.r_tiles_y;
+  t.c_tiles += m.c_tiles_x * c_tiles_y;
+  t.px += npx;
+  t.blocks += (int)((npx + ccl::kBlockPx - 1) / ccl::kBlockPx);
+  t.rows += m.H;
+  if (m.W > t.max_w) t.max_w = m.W;
+  if (2 * (m.H + m.W) > t.perimeter_max) t.perimeter_max = 2 * (m.H + m.W);
+  t.n += 1;
+}
+
+Plan single_plan(int dtype, void* plane, const void* aux, int64_t H, int64_t W, int64_t pitch) {
+  Plan P = {};
+  P.I.n = 1;
+  P.I.d = nullptr;
+  P.I.one = recon_image(dtype, plane, aux, H, W, pitch);
+  add_image(P.I.one, P.t);
+  return P;
+}
+
+struct WsSizes {
+  size_t recon, L, A, R, bits, tmp, F, table, total;
+};
+
+WsSizes ws_sizes(const BatchTotals& t) {
+  WsSizes z;
+  z.recon = align256(recon_workspace_bytes_tiles(t.r_tiles > 0 ? t.r_tiles : 1));
+  z.L = align256(sizeof(int) * (size_t)t.px);
+  z.A = z.L;
+  z.R = z.L;
+  z.bits = align256(sizeof(unsigned) * (size_t)(t.px / 32 + 1));
+  z.tmp = align256(sizeof(int) * (size_t)(2 * (int64_t)t.blocks + 2 * (int64_t)t.n + 8));
+  z.F = align256((size_t)t.px);
+  z.table = t.n > 1 ? align256(sizeof(Img) * (size_t)t.n) : 0;
+  z.total = z.recon + z.L + z.A + z.R + z.bits + z.tmp + z.F + z.table;
+  return z;
+}
+
 struct Ws {
   int* status;  // == start of the recon region
   void* recon;
@@ -252,36 +317,17 @@ struct Ws {
   int* A;
   int* R;        // root ranks; before ranking, the list of local roots
   unsigned* bits;
-  int* tmp;
-  int* counts;   // [2]
+  int* tmp;      // 2 ints per rank block
+  int* counts;   // 2 per image
   int* nroots;   // [1]
   uint8_t* F;
+  Img* table;
+  size_t bits_bytes;
   ccl::Forest forest(bool areas) const { return ccl::Forest{L, areas ? A : nullptr, R, nroots}; }
 };
 
-size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
-
-struct WsSizes {
-  size_t recon, L, A, R, bits, tmp, F, total;
-};
-
-WsSizes ws_sizes(int dtype, int64_t H, int64_t W) {
-  WsSizes z;
-  const int64_t n = H * W;
-  const int rd = dtype >= 0 && dtype <= 3 ? dtype : 0;
-  z.recon = align256(recon_workspace_bytes(rd, H, W));
-  z.L = align256(sizeof(int) * (size_t)n);
-  z.A = z.L;
-  z.R = z.L;
-  z.bits = align256(sizeof(unsigned) * (size_t)((n + 31) / 32 + 1));
-  z.tmp = align256(sizeof(int) * (ccl::rank_tmp_ints(n) + 4));
-  z.F = align256((size_t)n);
-  z.total = z.recon + z.L + z.A + z.R + z.bits + z.tmp + z.F;
-  return z;
-}
-
-Ws carve(void* ws, int dtype, int64_t H, int64_t W) {
-  const WsSizes z = ws_sizes(dtype, H, W);
+Ws carve(void* ws, const BatchTotals& t) {
+  const WsSizes z = ws_sizes(t);
   char* p = (char*)ws;
   Ws w;
   w.status = (int*)p;
@@ -294,17 +340,83 @@ Ws carve(void* ws, int dtype, int64_t H, int64_t W) {
   w.R = (int*)p;
   p += z.R;
   w.bits = (unsigned*)p;
+  w.bits_bytes = sizeof(unsigned) * (size_t)(t.px / 32 + 1);
   p += z.bits;
   w.tmp = (int*)p;
-  w.counts = w.tmp + (ccl::rank_tmp_ints(H * W));
-  w.nroots = w.counts + 2;
+  w.counts = w.tmp + 2 * (int64_t)t.blocks;
+  w.nroots = w.counts + 2 * (int64_t)t.n;
   p += z.tmp;
   w.F = (uint8_t*)p;
+  p += z.F;
+  w.table = t.n > 1 ? (Img*)p : nullptr;
   return w;
 }
 
 inline int grid1d(int64_t n) { return ccl::flat_grid(n); }
 inline dim3 rc(int64_t rows, int64_t cols) { return ccl::rowcol_grid((int)rows, (int)cols); }
+inline dim3 rcb(const BatchTotals& t) { return ccl::rowcol_grid(t.rows, t.max_w); }
+
+// Records the caller's optional timing event around the reconstruction kernel.
+cudaError_t record(const nsgb_opts* o, bool begin, cudaStream_t s) {
+  if (!o) return cudaSuccess;
+  void* ev = begin ? o->recon_event_begin : o->recon_event_end;
+  return ev ? cudaEventRecord((cudaEvent_t)ev, s) : cudaSuccess;
+}
+
+// Reconstruction of the whole plan bracketed by the optional timing events.
+cudaError_t recon_timed(const nsgb_opts* o, int dtype, const Plan& P, int conn, bool erode, bool ring, void* ws,
+                        cudaStream_t s) {
+  cudaError_t e = record(o, true, s);
+  if (e != cudaSuccess) return e;
+  e = recon_launch_batch(dtype, P.I, P.t.r_tiles, conn, erode, ring, ws, s, o ? o->max_visits_per_tile : 0,
+                         o ? o->max_visit_iters : 0);
+  if (e != cudaSuccess) return e;
+  return record(o, false, s);
+}
+
+template <typename F>
+cudaError_t dispatch_int(int dtype, F&& f) {
+  switch (dtype) {
+    case NSGB_U8: return f((uint8_t*)nullptr);
+    case NSGB_U16: return f((uint16_t*)nullptr);
+    case NSGB_I32: return f((int32_t*)nullptr);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// The single-tile / batched chain on a prepared plan: (a) reconstruction in place,
+// (b)+(c) threshold fused into the binary hole fill, (d)+(e) one labelling of the filled image
+// for both the raster relabel and the areas.  Counts land in w.counts (2 per image).
+cudaError_t chain_impl(int dtype, const Plan& P, const Ws& w, int recon_conn, double thr, int fill_conn,
+                       int label_conn, int area_min, int area_max, uint8_t* fill_out, int32_t* labels_out,
+                       uint8_t* area_out, const nsgb_opts* opts, cudaStream_t s) {
+  const BatchTotals& t = P.t;
+  cudaError_t e = recon_timed(opts, dtype, P, recon_conn, false, dtype == NSGB_I32, w.recon, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.bits, 0, w.bits_bytes, s);
+  if (e == cudaSuccess) {
+    e = dispatch_int(dtype, [&](auto* tag) -> cudaError_t {
+      using T = std::remove_pointer_t<decltype(tag)>;
+      ClsNotAbove<T> cls{thr};
+      cudaError_t r = ccl::label(cls, P.I, t, fill_conn, w.forest(false), s);
+      if (r != cudaSuccess) return r;
+      const int gx = grid1d(t.perimeter_max) > 64 ? 64 : grid1d(t.perimeter_max);
+      ccl::ccl_seed_border<SeedBorder<ClsNotAbove<T>>><<<dim3(gx, t.n), 256, 0, s>>>(
+          P.I, w.L, SeedBorder<ClsNotAbove<T>>{cls}, w.bits);
+      fill_out_kernel<uint8_t><<<rcb(t), 256, 0, s>>>(P.I, t.rows, w.L, w.bits, w.F, fill_out,
+                                                      P.I.d ? 0 : (int64_t)P.I.one.W, (uint8_t)255);
+      return cudaGetLastError();
+    });
+  }
+  if (e == cudaSuccess) e = ccl::label(ClsDenseU8{w.F}, P.I, t, label_conn, w.forest(true), s);
+  if (e == cudaSuccess) e = ccl::rank_roots(P.I, t, w.L, w.A, area_min, area_max, w.R, w.tmp, w.counts, s);
+  if (e == cudaSuccess) {
+    const int64_t W1 = P.I.d ? 0 : P.I.one.W;
+    label_out_kernel<<<rcb(t), 256, 0, s>>>(P.I, t.rows, w.L, w.R, 1, labels_out, W1 * 4, w.A, area_min, area_max,
+                                            nullptr, 0, area_out, W1);
+    e = cudaGetLastError();
+  }
+  return e;
+}
 
 }  // namespace
 }  // namespace nsgb
@@ -324,24 +436,6 @@ bool want_sync(const nsgb_opts* o) { return o == nullptr || o->sync != 0; }
 
 nsgb_status cuda_status(cudaError_t e) { return e == cudaSuccess ? NSGB_OK : NSGB_ERR_CUDA; }
 
-// Records the caller's optional timing event around the reconstruction kernel.
-cudaError_t record(const nsgb_opts* o, bool begin, cudaStream_t s) {
-  if (!o) return cudaSuccess;
-  void* ev = begin ? o->recon_event_begin : o->recon_event_end;
-  return ev ? cudaEventRecord((cudaEvent_t)ev, s) : cudaSuccess;
-}
-
-// Reconstruction launch bracketed by the optional timing events.
-cudaError_t recon_timed(const nsgb_opts* o, int dtype, void* out, const void* marker, const void* mask, int64_t H,
-                        int64_t W, int64_t pitch, int conn, bool erode, bool ring, void* ws, cudaStream_t s) {
-  cudaError_t e = record(o, true, s);
-  if (e != cudaSuccess) return e;
-  e = recon_launch(dtype, out, marker, mask, H, W, pitch, conn, erode, ring, ws, s, o ? o->max_visits_per_tile : 0,
-                   o ? o->max_visit_iters : 0);
-  if (e != cudaSuccess) return e;
-  return record(o, false, s);
-}
-
 // Finishes a call: reports launch errors; with sync, waits and reports the device status.
 nsgb_status finish(cudaError_t e, const void* ws, cudaStream_t s, const nsgb_opts* o) {
   if (e != cudaSuccess) return NSGB_ERR_CUDA;
@@ -356,21 +450,15 @@ nsgb_status finish(cudaError_t e, const void* ws, cudaStream_t s, const nsgb_opt
   return (nsgb_status)dev_status;
 }
 
-nsgb_status check_ws(void* ws, size_t ws_bytes, int op, int dtype, int64_t rows, int64_t cols) {
+nsgb_status check_ws_bytes(void* ws, size_t ws_bytes, size_t need) {
   if (!ws) return NSGB_ERR_WORKSPACE;
-  if (ws_bytes < nsgb_workspace_size(op, dtype, rows, cols)) return NSGB_ERR_WORKSPACE;
+  if (ws_bytes < need) return NSGB_ERR_WORKSPACE;
   if ((uintptr_t)ws % 256 != 0) return NSGB_ERR_WORKSPACE;
   return NSGB_OK;
 }
 
-template <typename F>
-cudaError_t dispatch_int(int dtype, F&& f) {
-  switch (dtype) {
-    case NSGB_U8: return f((uint8_t*)nullptr);
-    case NSGB_U16: return f((uint16_t*)nullptr);
-    case NSGB_I32: return f((int32_t*)nullptr);
-    default: return cudaErrorInvalidValue;
-  }
+nsgb_status check_ws(void* ws, size_t ws_bytes, int op, int dtype, int64_t rows, int64_t cols) {
+  return check_ws_bytes(ws, ws_bytes, nsgb_workspace_size(op, dtype, rows, cols));
 }
 
 }  // namespace
@@ -380,12 +468,10 @@ extern "C" {
 size_t nsgb_workspace_size(int op, int dtype, int64_t rows, int64_t cols) {
   if (rows <= 0 || cols <= 0) return 0;
   if (op == NSGB_OP_BWLABEL || op == NSGB_OP_BWAREAOPEN) dtype = NSGB_U8;
+  if (dtype < 0 || dtype > 3) return 0;
   if (op == NSGB_OP_IMRECONSTRUCT || op == NSGB_OP_HMIN) return align256(recon_workspace_bytes(dtype, rows, cols));
-  if (op == NSGB_OP_FILL_HOLES) {
-    const WsSizes z = ws_sizes(dtype, rows, cols);
-    return z.total;
-  }
-  return ws_sizes(dtype, rows, cols).total;
+  const Plan P = single_plan(dtype, nullptr, nullptr, rows, cols, cols * elem_size(dtype));
+  return ws_sizes(P.t).total;
 }
 
 const char* nsgb_status_string(int status) {
@@ -422,7 +508,8 @@ nsgb_status nsgb_imreconstruct(int dtype, void* marker, const void* mask, int64_
   if (st != NSGB_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
   const bool ring = !erode && (dtype == NSGB_I32 || dtype == NSGB_F32);
-  cudaError_t e = recon_timed(opts, dtype, marker, marker, mask, rows, cols, pitch, conn, erode != 0, ring, ws, s);
+  const Plan P = single_plan(dtype, marker, mask, rows, cols, pitch);
+  cudaError_t e = recon_timed(opts, dtype, P, conn, erode != 0, ring, ws, s);
   return finish(e, ws, s, opts);
 }
 
@@ -437,19 +524,18 @@ nsgb_status nsgb_imreconstruct_binary(int dtype, void* marker, const void* mask,
   nsgb_status st = check_ws(ws, ws_bytes, NSGB_OP_IMRECONSTRUCT_BINARY, dtype, rows, cols);
   if (st != NSGB_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  const int H = (int)rows, W = (int)cols;
-  Ws w = carve(ws, dtype, rows, cols);
+  const Plan P = single_plan(dtype, marker, mask, rows, cols, pitch);
+  Ws w = carve(ws, P.t);
   cudaError_t e = cudaMemsetAsync(w.status, 0, sizeof(int), s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.bits, 0, sizeof(unsigned) * (size_t)((rows * cols + 31) / 32 + 1), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.bits, 0, w.bits_bytes, s);
   if (e == cudaSuccess) {
     e = dispatch_int(dtype, [&](auto* tag) -> cudaError_t {
       using T = std::remove_pointer_t<decltype(tag)>;
-      ClsNonZero<T> cls{(const T*)mask, pitch};
-      SeedBoth<T> seed{(const T*)marker, (const T*)mask, pitch};
-      cudaError_t r = ccl::label(cls, H, W, conn, w.forest(false), s);
+      ClsNonZero<T> cls{true};
+      cudaError_t r = ccl::label(cls, P.I, P.t, conn, w.forest(false), s);
       if (r != cudaSuccess) return r;
-      ccl::ccl_seed_pixels<SeedBoth<T>><<<rc(rows, cols), 256, 0, s>>>(H, W, w.L, seed, w.bits);
-      binrecon_out_kernel<T><<<rc(rows, cols), 256, 0, s>>>((T*)marker, pitch, H, W, w.L, w.bits);
+      ccl::ccl_seed_pixels<SeedBoth<T>><<<rc(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, SeedBoth<T>{true}, w.bits);
+      binrecon_out_kernel<T><<<rc(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.bits);
       return cudaGetLastError();
     });
   }
@@ -468,7 +554,8 @@ nsgb_status nsgb_imfill_holes(int dtype, const void* image, void* out, int64_t r
   if (st != NSGB_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
   const int H = (int)rows, W = (int)cols;
-  Ws w = carve(ws, dtype, rows, cols);
+  const Plan P = single_plan(dtype, (void*)image, nullptr, rows, cols, pitch);
+  Ws w = carve(ws, P.t);
   cudaError_t e = cudaMemsetAsync(w.status, 0, sizeof(int), s);
   if (e != cudaSuccess) return NSGB_ERR_CUDA;
   if (binary) {
@@ -478,17 +565,16 @@ nsgb_status nsgb_imfill_holes(int dtype, const void* image, void* out, int64_t r
       fill_const_kernel<int32_t><<<rc(rows, cols), 256, 0, s>>>((int32_t*)out, pitch, H, W, INT_MAX);
       return finish(cudaGetLastError(), ws, s, opts);
     }
-    e = cudaMemsetAsync(w.bits, 0, sizeof(unsigned) * (size_t)((rows * cols + 31) / 32 + 1), s);
+    e = cudaMemsetAsync(w.bits, 0, w.bits_bytes, s);
     if (e == cudaSuccess) {
       e = dispatch_int(dtype, [&](auto* tag) -> cudaError_t {
         using T = std::remove_pointer_t<decltype(tag)>;
-        ClsNotMax<T> cls{(const T*)image, pitch};
-        SeedBorder<ClsNotMax<T>> seed{cls, H, W};
-        cudaError_t r = ccl::label(cls, H, W, conn, w.forest(false), s);
+        ClsNotMax<T> cls;
+        cudaError_t r = ccl::label(cls, P.I, P.t, conn, w.forest(false), s);
         if (r != cudaSuccess) return r;
-        ccl::ccl_seed_border<SeedBorder<ClsNotMax<T>>><<<grid1d(2 * (rows + cols)), 256, 0, s>>>(H, W, w.L, seed,
-                                                                                                w.bits);
-        fill_out_kernel<T><<<rc(rows, cols), 256, 0, s>>>(H, W, w.L, w.bits, (T*)out, pitch,
+        ccl::ccl_seed_border<SeedBorder<ClsNotMax<T>>><<<dim3(grid1d(2 * (rows + cols)), 1), 256, 0, s>>>(
+            P.I, w.L, SeedBorder<ClsNotMax<T>>{cls}, w.bits);
+        fill_out_kernel<T><<<rc(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.bits, nullptr, (T*)out, pitch,
                                                           std::numeric_limits<T>::max());
         return cudaGetLastError();
       });
@@ -503,8 +589,8 @@ nsgb_status nsgb_imfill_holes(int dtype, const void* image, void* out, int64_t r
     case NSGB_I32: fill_marker_kernel<int32_t><<<rc(rows, cols), 256, 0, s>>>((const int32_t*)image, (int32_t*)out, pitch, H, W); break;
     case NSGB_F32: fill_marker_kernel<float><<<rc(rows, cols), 256, 0, s>>>((const float*)image, (float*)out, pitch, H, W); break;
   }
-  e = recon_launch(dtype, out, out, image, rows, cols, pitch, conn, true, false, ws, s, opts ? opts->max_visits_per_tile : 0,
-                   opts ? opts->max_visit_iters : 0);
+  const Plan R = single_plan(dtype, out, image, rows, cols, pitch);
+  e = recon_timed(opts, dtype, R, conn, true, false, ws, s);
   return finish(e, ws, s, opts);
 }
 
@@ -526,8 +612,8 @@ nsgb_status nsgb_imhmin(int dtype, const void* image, void* out, int64_t rows, i
   }
   // invert(recon(invert(I) - h, invert(I))): the order-reversed reconstruction with the
   // reference's 0-valued padding ring taken in the inverted domain.
-  cudaError_t e = recon_launch(dtype, out, out, image, rows, cols, pitch, conn, true, true, ws, s,
-                               opts ? opts->max_visits_per_tile : 0, opts ? opts->max_visit_iters : 0);
+  const Plan P = single_plan(dtype, out, image, rows, cols, pitch);
+  cudaError_t e = recon_timed(opts, dtype, P, conn, true, true, ws, s);
   return finish(e, ws, s, opts);
 }
 
@@ -541,19 +627,20 @@ nsgb_status nsgb_bwselect(int dtype, const void* image, const void* seeds, void*
   nsgb_status st = check_ws(ws, ws_bytes, NSGB_OP_BWSELECT, dtype, rows, cols);
   if (st != NSGB_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  const int H = (int)rows, W = (int)cols;
-  Ws w = carve(ws, dtype, rows, cols);
+  const Plan P = single_plan(dtype, (void*)image, seeds, rows, cols, pitch);
+  Ws w = carve(ws, P.t);
   cudaError_t e = cudaMemsetAsync(w.status, 0, sizeof(int), s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.bits, 0, sizeof(unsigned) * (size_t)((rows * cols + 31) / 32 + 1), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.bits, 0, w.bits_bytes, s);
   if (e == cudaSuccess) {
     e = dispatch_int(dtype, [&](auto* tag) -> cudaError_t {
       using T = std::remove_pointer_t<decltype(tag)>;
-      ClsNonZero<T> cls{(const T*)image, pitch};
-      SeedBoth<T> seed{(const T*)seeds, (const T*)image, pitch};
-      cudaError_t r = ccl::label(cls, H, W, conn, w.forest(false), s);
+      ClsNonZero<T> cls{false};
+      cudaError_t r = ccl::label(cls, P.I, P.t, conn, w.forest(false), s);
       if (r != cudaSuccess) return r;
-      ccl::ccl_seed_pixels<SeedBoth<T>><<<rc(rows, cols), 256, 0, s>>>(H, W, w.L, seed, w.bits);
-      bwselect_out_kernel<T><<<rc(rows, cols), 256, 0, s>>>((const T*)image, (T*)out, pitch, H, W, w.L, w.bits);
+      // seeds (aux) != 0 and image (plane) != 0
+      ccl::ccl_seed_pixels<SeedBoth<T>><<<rc(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, SeedBoth<T>{false},
+                                                                        w.bits);
+      bwselect_out_kernel<T><<<rc(rows, cols), 256, 0, s>>>(P.I, P.t.rows, out, w.L, w.bits);
       return cudaGetLastError();
     });
   }
@@ -569,17 +656,15 @@ nsgb_status nsgb_bwlabel(const uint8_t* bin, int32_t* labels, int64_t rows, int6
   nsgb_status st = check_ws(ws, ws_bytes, NSGB_OP_BWLABEL, NSGB_U8, rows, cols);
   if (st != NSGB_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  const int H = (int)rows, W = (int)cols;
-  const int64_t n = rows * cols;
-  Ws w = carve(ws, NSGB_U8, rows, cols);
+  const Plan P = single_plan(NSGB_U8, (void*)bin, nullptr, rows, cols, pitch_in);
+  Ws w = carve(ws, P.t);
   cudaError_t e = cudaMemsetAsync(w.status, 0, sizeof(int), s);
   if (e != cudaSuccess) return NSGB_ERR_CUDA;
-  ClsValueU8 cls{bin, pitch_in};
-  e = ccl::label(cls, H, W, conn, w.forest(false), s);
-  if (e == cudaSuccess) e = ccl::rank_roots(w.L, nullptr, n, 0, 0, w.R, w.tmp, w.counts, s);
+  e = ccl::label(ClsValueU8{}, P.I, P.t, conn, w.forest(false), s);
+  if (e == cudaSuccess) e = ccl::rank_roots(P.I, P.t, w.L, nullptr, 0, 0, w.R, w.tmp, w.counts, s);
   if (e == cudaSuccess) {
-    label_out_kernel<<<rc(rows, cols), 256, 0, s>>>(H, W, w.L, w.R, relabel, labels, pitch_labels, nullptr, 0, 0, nullptr,
-                                               0, nullptr, 0);
+    label_out_kernel<<<rc(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.R, relabel, labels, pitch_labels, nullptr,
+                                                     0, 0, nullptr, 0, nullptr, 0);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess && count) {
@@ -600,18 +685,17 @@ nsgb_status nsgb_bwareaopen(const void* in, int labeled, int32_t* labels_out, ui
   nsgb_status st = check_ws(ws, ws_bytes, NSGB_OP_BWAREAOPEN, NSGB_U8, rows, cols);
   if (st != NSGB_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  const int H = (int)rows, W = (int)cols;
   const int64_t n = rows * cols;
-  Ws w = carve(ws, NSGB_U8, rows, cols);
+  const Plan P = single_plan(NSGB_U8, (void*)in, nullptr, rows, cols, pitch_in);
+  Ws w = carve(ws, P.t);
   cudaError_t e = cudaMemsetAsync(w.status, 0, sizeof(int), s);
   if (e != cudaSuccess) return NSGB_ERR_CUDA;
   if (!labeled) {
-    ClsValueU8 cls{(const uint8_t*)in, pitch_in};
-    e = ccl::label(cls, H, W, conn, w.forest(true), s);
-    if (e == cudaSuccess) e = ccl::rank_roots(w.L, w.A, n, min_size, max_size, w.R, w.tmp, w.counts, s);
+    e = ccl::label(ClsValueU8{}, P.I, P.t, conn, w.forest(true), s);
+    if (e == cudaSuccess) e = ccl::rank_roots(P.I, P.t, w.L, w.A, min_size, max_size, w.R, w.tmp, w.counts, s);
     if (e == cudaSuccess) {
-      label_out_kernel<<<rc(rows, cols), 256, 0, s>>>(H, W, w.L, w.R, 0, nullptr, 0, w.A, min_size, max_size, labels_out,
-                                                 pitch_labels, flat_out, pitch_flat);
+      label_out_kernel<<<rc(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.R, 0, nullptr, 0, w.A, min_size, max_size,
+                                                       labels_out, pitch_labels, flat_out, pitch_flat);
       e = cudaGetLastError();
     }
     if (e == cudaSuccess && count) {
@@ -623,10 +707,10 @@ nsgb_status nsgb_bwareaopen(const void* in, int labeled, int32_t* labels_out, ui
   e = cudaMemsetAsync(w.A, 0, sizeof(int) * (size_t)n, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(w.counts, 0, 2 * sizeof(int), s);
   if (e == cudaSuccess) {
-    label_hist_kernel<<<rc(rows, cols), 256, 0, s>>>((const int32_t*)in, pitch_in, H, W, w.A, w.status);
+    label_hist_kernel<<<rc(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.A, w.status);
     count_labels_in_range_kernel<<<grid1d(n), 256, 0, s>>>(w.A, n, min_size, max_size, w.counts + 1);
-    labeled_area_out_kernel<<<rc(rows, cols), 256, 0, s>>>((const int32_t*)in, pitch_in, H, W, w.A, min_size, max_size,
-                                                      labels_out, pitch_labels, flat_out, pitch_flat);
+    labeled_area_out_kernel<<<rc(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.A, min_size, max_size, labels_out,
+                                                            pitch_labels, flat_out, pitch_flat);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess && count) {
@@ -681,41 +765,10 @@ nsgb_status nsgb_chain(int dtype, void* marker, const void* mask, int64_t rows, 
   nsgb_status st = check_ws(ws, ws_bytes, NSGB_OP_CHAIN, dtype, rows, cols);
   if (st != NSGB_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  const int H = (int)rows, W = (int)cols;
-  const int64_t n = rows * cols;
-  Ws w = carve(ws, dtype, rows, cols);
-  uint8_t* F = fill_out ? fill_out : w.F;
-  // (a) reconstruction by dilation, in place on the marker.
-  cudaError_t e = recon_timed(opts, dtype, marker, marker, mask, rows, cols, pitch, recon_conn, false,
-                              dtype == NSGB_I32, ws, s);
-  // (b)+(c) threshold fused into the binary hole fill: label the R <= thr class, flag the
-  // components that touch the border, F = 0 there and 255 elsewhere.
-  if (e == cudaSuccess)
-    e = cudaMemsetAsync(w.bits, 0, sizeof(unsigned) * (size_t)((n + 31) / 32 + 1), s);
-  if (e == cudaSuccess) {
-    e = dispatch_int(dtype, [&](auto* tag) -> cudaError_t {
-      using T = std::remove_pointer_t<decltype(tag)>;
-      ClsNotAbove<T> cls{(const T*)marker, pitch, thr};
-      SeedBorder<ClsNotAbove<T>> seed{cls, H, W};
-      cudaError_t r = ccl::label(cls, H, W, fill_conn, w.forest(false), s);
-      if (r != cudaSuccess) return r;
-      ccl::ccl_seed_border<SeedBorder<ClsNotAbove<T>>><<<grid1d(2 * (rows + cols)), 256, 0, s>>>(H, W, w.L, seed,
-                                                                                                  w.bits);
-      fill_out_kernel<uint8_t><<<rc(rows, cols), 256, 0, s>>>(H, W, w.L, w.bits, F, (int64_t)W, (uint8_t)255);
-      return cudaGetLastError();
-    });
-  }
-  // (d)+(e) one labelling of F serves bwlabel (relabelled) and bwareaopen (areas).
-  if (e == cudaSuccess) {
-    ClsValueU8 cls{F, (int64_t)W};
-    e = ccl::label(cls, H, W, label_conn, w.forest(true), s);
-  }
-  if (e == cudaSuccess) e = ccl::rank_roots(w.L, w.A, n, area_min, area_max, w.R, w.tmp, w.counts, s);
-  if (e == cudaSuccess) {
-    label_out_kernel<<<rc(rows, cols), 256, 0, s>>>(H, W, w.L, w.R, 1, labels_out, (int64_t)W * 4, w.A, area_min, area_max,
-                                               nullptr, 0, area_out, (int64_t)W);
-    e = cudaGetLastError();
-  }
+  const Plan P = single_plan(dtype, marker, mask, rows, cols, pitch);
+  Ws w = carve(ws, P.t);
+  cudaError_t e = chain_impl(dtype, P, w, recon_conn, thr, fill_conn, label_conn, area_min, area_max, fill_out,
+                             labels_out, area_out, opts, s);
   if (e == cudaSuccess && (n_labels || n_kept)) {
     int32_t c[2] = {0, 0};
     e = cudaMemcpyAsync(c, w.counts, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
@@ -724,6 +777,137 @@ nsgb_status nsgb_chain(int dtype, void* marker, const void* mask, int64_t rows, 
     if (n_kept) *n_kept = c[1];
   }
   return finish(e, ws, s, opts);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Batches.  nsgb_batch_prepare writes the image table into the workspace once and fills the
+// caller's nsgb_batch (host copy of the totals); nsgb_chain_batch / nsgb_imreconstruct_batch
+// then only enqueue kernels and memsets (plus small count reads when asked for).
+
+namespace {
+
+bool batch_totals(int dtype, const nsgb_tile* tiles, int n, std::vector<Img>* imgs, BatchTotals* t) {
+  *t = BatchTotals{};
+  if (imgs) imgs->clear();
+  const int esz = elem_size(dtype);
+  if (!esz || !tiles || n <= 0) return false;
+  for (int i = 0; i < n; ++i) {
+    const nsgb_tile& tl = tiles[i];
+    if (!tl.marker || !tl.mask || !valid_dims(tl.rows, tl.cols) || !valid_pitch(tl.pitch, tl.cols, esz))
+      return false;
+    Img m = recon_image(dtype, tl.marker, tl.mask, tl.rows, tl.cols, tl.pitch);
+    add_image(m, *t);
+    m.fill = tl.fill_out;
+    m.labels = tl.labels_out;
+    m.area = tl.area_out;
+    if (t->px >= (int64_t)INT_MAX) return false;
+    if (imgs) imgs->push_back(m);
+  }
+  return true;
+}
+
+// Batch workspaces always carry the device table, even for one image.
+BatchTotals table_totals(BatchTotals t) {
+  if (t.n == 1) t.n = 2;
+  return t;
+}
+
+nsgb_status batch_plan(const nsgb_batch* b, Plan* P, Ws* w) {
+  if (!b || !b->ws) return NSGB_ERR_BAD_ARG;
+  BatchTotals t;
+  t.n = b->n;
+  t.px = b->total_px;
+  t.r_tiles = b->recon_tiles;
+  t.c_tiles = b->label_tiles;
+  t.blocks = b->rank_blocks;
+  t.rows = b->total_rows;
+  t.max_w = b->max_cols;
+  t.perimeter_max = b->max_perimeter;
+  if (t.n <= 0) return NSGB_ERR_BAD_ARG;
+  if (b->ws_bytes < ws_sizes(table_totals(t)).total) return NSGB_ERR_WORKSPACE;
+  *w = carve(b->ws, table_totals(t));
+  P->t = t;
+  P->I = Imgs{};
+  P->I.n = t.n;
+  P->I.d = w->table;
+  return NSGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t nsgb_batch_workspace_size(int dtype, const nsgb_tile* tiles, int n_tiles) {
+  BatchTotals t;
+  if (!batch_totals(dtype, tiles, n_tiles, nullptr, &t)) return 0;
+  return ws_sizes(table_totals(t)).total;
+}
+
+nsgb_status nsgb_batch_prepare(int dtype, const nsgb_tile* tiles, int n_tiles, void* ws, size_t ws_bytes,
+                               nsgb_batch* batch) {
+  if (!batch) return NSGB_ERR_BAD_ARG;
+  std::vector<Img> imgs;
+  BatchTotals t;
+  if (!batch_totals(dtype, tiles, n_tiles, &imgs, &t)) return NSGB_ERR_BAD_ARG;
+  nsgb_status st = check_ws_bytes(ws, ws_bytes, nsgb_batch_workspace_size(dtype, tiles, n_tiles));
+  if (st != NSGB_OK) return st;
+  Ws w = carve(ws, table_totals(t));
+  // Synchronous copy: the host array goes away when this returns.
+  if (cudaMemcpy(w.table, imgs.data(), sizeof(Img) * imgs.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return NSGB_ERR_CUDA;
+  memset(batch, 0, sizeof(*batch));
+  batch->dtype = dtype;
+  batch->n = t.n;
+  batch->total_px = t.px;
+  batch->recon_tiles = t.r_tiles;
+  batch->label_tiles = t.c_tiles;
+  batch->rank_blocks = t.blocks;
+  batch->total_rows = t.rows;
+  batch->max_cols = t.max_w;
+  batch->max_perimeter = t.perimeter_max;
+  batch->ws = ws;
+  batch->ws_bytes = ws_bytes;
+  return NSGB_OK;
+}
+
+nsgb_status nsgb_chain_batch(const nsgb_batch* batch, int recon_conn, double thr, int fill_conn, int label_conn,
+                             int32_t area_min, int32_t area_max, int32_t* n_labels, int32_t* n_kept,
+                             nsgb_stream_t stream, const nsgb_opts* opts) {
+  if (!valid_conn(recon_conn) || !valid_conn(fill_conn) || !valid_conn(label_conn)) return NSGB_ERR_BAD_ARG;
+  Plan P;
+  Ws w;
+  nsgb_status st = batch_plan(batch, &P, &w);
+  if (st != NSGB_OK) return st;
+  if (batch->dtype == NSGB_F32 || !elem_size(batch->dtype)) return NSGB_ERR_UNSUPPORTED_DTYPE;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = chain_impl(batch->dtype, P, w, recon_conn, thr, fill_conn, label_conn, area_min, area_max,
+                             nullptr, nullptr, nullptr, opts, s);
+  if (e == cudaSuccess && (n_labels || n_kept)) {
+    std::vector<int32_t> c(2 * (size_t)P.t.n);
+    e = cudaMemcpyAsync(c.data(), w.counts, c.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    for (int i = 0; i < P.t.n && e == cudaSuccess; ++i) {
+      if (n_labels) n_labels[i] = c[2 * i];
+      if (n_kept) n_kept[i] = c[2 * i + 1];
+    }
+  }
+  return finish(e, w.status, s, opts);
+}
+
+nsgb_status nsgb_imreconstruct_batch(const nsgb_batch* batch, int conn, int erode, nsgb_stream_t stream,
+                                     const nsgb_opts* opts) {
+  if (!valid_conn(conn)) return NSGB_ERR_BAD_ARG;
+  Plan P;
+  Ws w;
+  nsgb_status st = batch_plan(batch, &P, &w);
+  if (st != NSGB_OK) return st;
+  if (!elem_size(batch->dtype)) return NSGB_ERR_UNSUPPORTED_DTYPE;
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool ring = !erode && (batch->dtype == NSGB_I32 || batch->dtype == NSGB_F32);
+  cudaError_t e = recon_timed(opts, batch->dtype, P, conn, erode != 0, ring, w.recon, s);
+  return finish(e, w.status, s, opts);
 }
 
 }  // extern "C"

@@ -32,6 +32,7 @@
 #include <stdint.h>
 #include <stdlib.h>
 
+#include "batch.cuh"
 #include "common.cuh"
 #include "recon.cuh"
 
@@ -91,14 +92,12 @@ struct Ctl {
   long long max_visits;
 };
 
-template <typename T>
+// Images of the batch: Img::plane is reconstructed in place (it holds the marker on entry),
+// Img::aux is the mask.  Tiles of all images are numbered consecutively.
 struct Args {
-  T* out;          // reconstructed in place (holds the marker on entry)
-  const T* mask;
-  int64_t pitch;   // bytes, shared by both planes
-  int H, W;
-  int tiles_x, tiles_y, ntiles;
-  int flip, ring, aligned;
+  Imgs I;
+  int ntiles;
+  int flip, ring;
   int max_iters;
   Ctl c;
 };
@@ -417,15 +416,24 @@ __device__ __forceinline__ void mark_tile(const Ctl& c, int nt) {
   set_status(c.status, kDevTimeout);
 }
 
-template <typename T, int CONN>
-__device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int lane) {
+// Image fields: from the kernel parameters for a single image (constant bank, nothing pinned
+// in registers), from the device table for a batch.
+#define IMF(field) (BATCH ? a.I.d[ii].field : a.I.one.field)
+
+template <typename T, int CONN, bool BATCH>
+__device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane) {
   using P = Px<T>;
   constexpr int E = P::E;
   constexpr int TW = 32 * E;
-  const int ty = t / a.tiles_x, tx = t - ty * a.tiles_x;
+  const int ii = BATCH ? img_of(a.I, t, RTileBase()) : 0;
+  const int lt = t - IMF(r_tile_base);
+  const int ty = lt / IMF(r_tiles_x), tx = lt - ty * IMF(r_tiles_x);
   const int y0 = ty * kRows, x0 = tx * TW;
-  const int H = a.H, W = a.W;
+  const int H = IMF(H), W = IMF(W);
   const bool flip = a.flip != 0, ring = a.ring != 0;
+  T* const out = (T*)IMF(plane);
+  const T* const mask = (const T*)IMF(aux);
+  const int64_t pitch = IMF(pitch);
 
   PROF_T0();
   // The caller has set the tile RUNNING; order that before reading the neighbours' pixels.
@@ -433,10 +441,10 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int l
   __threadfence();
   PROF_MARK(1);
 
-  const T* src = a.out;
+  const T* src = out;
   const bool coh = true;
   const bool interior = (y0 + kRows <= H) && (x0 + TW <= W);
-  const bool fast = interior && a.aligned;
+  const bool fast = interior && IMF(aligned);
   const int xl = x0 + E * lane;
 
   // All loads of the tile and its halo are issued before any is used, so the visit waits for
@@ -444,16 +452,16 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int l
   uint32_t O[32], M[32];
   if (fast) {  // interior tile: straight-line vector loads, no per-element checks
 #pragma unroll
-    for (int i = 0; i < 32; ++i) M[i] = load_word<T>(a.mask, a.pitch, y0 + i, xl, H, W, true, false, flip);
+    for (int i = 0; i < 32; ++i) M[i] = load_word<T>(mask, pitch, y0 + i, xl, H, W, true, false, flip);
 #pragma unroll
-    for (int i = 0; i < 32; ++i) O[i] = load_word<T>(src, a.pitch, y0 + i, xl, H, W, true, true, flip);
+    for (int i = 0; i < 32; ++i) O[i] = load_word<T>(src, pitch, y0 + i, xl, H, W, true, true, flip);
   } else {
     // Edge or unaligned tile: bounds-checked loads in a rolled loop through shared memory
     // (keeps this rarely used path out of the instruction cache's way).
 #pragma unroll 1
     for (int i = 0; i < 32; ++i) {
-      B.xp[lane * 33 + i] = load_word<T>(a.mask, a.pitch, y0 + i, xl, H, W, false, false, flip);
-      B.mh[lane * 33 + i] = load_word<T>(src, a.pitch, y0 + i, xl, H, W, false, true, flip);
+      B.xp[lane * 33 + i] = load_word<T>(mask, pitch, y0 + i, xl, H, W, false, false, flip);
+      B.mh[lane * 33 + i] = load_word<T>(src, pitch, y0 + i, xl, H, W, false, true, flip);
     }
     __syncwarp();
 #pragma unroll
@@ -466,20 +474,20 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int l
   // Halo rows (column layout words) and halo columns (single elements).
   const bool fast_top = fast && y0 > 0;
   const bool fast_bot = fast && y0 + kRows < H;
-  const uint32_t topm = load_word<T>(a.mask, a.pitch, y0 - 1, xl, H, W, fast_top, false, flip);
-  const uint32_t topv_raw = load_word<T>(src, a.pitch, y0 - 1, xl, H, W, fast_top, coh, flip);
-  const uint32_t botm = load_word<T>(a.mask, a.pitch, y0 + kRows, xl, H, W, fast_bot, false, flip);
-  const uint32_t botv_raw = load_word<T>(src, a.pitch, y0 + kRows, xl, H, W, fast_bot, coh, flip);
+  const uint32_t topm = load_word<T>(mask, pitch, y0 - 1, xl, H, W, fast_top, false, flip);
+  const uint32_t topv_raw = load_word<T>(src, pitch, y0 - 1, xl, H, W, fast_top, coh, flip);
+  const uint32_t botm = load_word<T>(mask, pitch, y0 + kRows, xl, H, W, fast_bot, false, flip);
+  const uint32_t botv_raw = load_word<T>(src, pitch, y0 + kRows, xl, H, W, fast_bot, coh, flip);
   uint32_t hm[4], hv[4];
 #pragma unroll
   for (int j = 0; j < 2; ++j) {
     const int k = lane + 32 * j;
     const int y = y0 - 1 + k;
     const bool ok = k < 34;
-    hm[2 * j] = ok ? load_elem_at<T>(a.mask, a.pitch, y, x0 - 1, H, W, false, flip) : P::LOW;
-    hm[2 * j + 1] = ok ? load_elem_at<T>(a.mask, a.pitch, y, x0 + TW, H, W, false, flip) : P::LOW;
-    hv[2 * j] = ok ? load_elem_at<T>(src, a.pitch, y, x0 - 1, H, W, coh, flip) : P::LOW;
-    hv[2 * j + 1] = ok ? load_elem_at<T>(src, a.pitch, y, x0 + TW, H, W, coh, flip) : P::LOW;
+    hm[2 * j] = ok ? load_elem_at<T>(mask, pitch, y, x0 - 1, H, W, false, flip) : P::LOW;
+    hm[2 * j + 1] = ok ? load_elem_at<T>(mask, pitch, y, x0 + TW, H, W, false, flip) : P::LOW;
+    hv[2 * j] = ok ? load_elem_at<T>(src, pitch, y, x0 - 1, H, W, coh, flip) : P::LOW;
+    hv[2 * j + 1] = ok ? load_elem_at<T>(src, pitch, y, x0 + TW, H, W, coh, flip) : P::LOW;
   }
   // any_change: did this visit change a stored value (the clamp to the mask on load counts).
   uint32_t any_change = 0;
@@ -545,13 +553,13 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int l
   if (__any_sync(NSGB_FULL, any_change != 0)) {
     if (fast) {
 #pragma unroll
-      for (int i = 0; i < 32; ++i) store_word<T>(a.out, a.pitch, y0 + i, xl, H, W, O[i], true, flip);
+      for (int i = 0; i < 32; ++i) store_word<T>(out, pitch, y0 + i, xl, H, W, O[i], true, flip);
     } else {
 #pragma unroll
       for (int i = 0; i < 32; ++i) B.xp[lane * 33 + i] = O[i];
       __syncwarp();
 #pragma unroll 1
-      for (int i = 0; i < 32; ++i) store_word<T>(a.out, a.pitch, y0 + i, xl, H, W, B.xp[lane * 33 + i], false, flip);
+      for (int i = 0; i < 32; ++i) store_word<T>(out, pitch, y0 + i, xl, H, W, B.xp[lane * 33 + i], false, flip);
       __syncwarp();
     }
   }
@@ -620,16 +628,16 @@ __device__ __forceinline__ void visit(const Args<T>& a, WarpBuf& B, int t, int l
     for (int d = 0; d < 9; ++d) {
       if (!((dirs >> d) & 1u)) continue;
       const int ny = ty + d / 3 - 1, nx = tx + d % 3 - 1;
-      if (ny < 0 || ny >= a.tiles_y || nx < 0 || nx >= a.tiles_x) continue;
-      mark_tile(a.c, ny * a.tiles_x + nx);
+      if (ny < 0 || ny >= IMF(r_tiles_y) || nx < 0 || nx >= IMF(r_tiles_x)) continue;
+      mark_tile(a.c, IMF(r_tile_base) + ny * IMF(r_tiles_x) + nx);
     }
   }
   __syncwarp();
   PROF_MARK(6);
 }
 
-template <typename T, int CONN>
-__global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args<T> a) {
+template <typename T, int CONN, bool BATCH>
+__global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   WarpBuf& B = reinterpret_cast<WarpBuf*>(smem_raw)[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
@@ -645,7 +653,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args<T> a) {
 #endif
     if (t < 0) break;
     if (lane == 0) atomicExch(&a.c.state[t], kRunning);
-    visit<T, CONN>(a, B, t, lane);
+    visit<T, CONN, BATCH>(a, B, t, lane);
 #ifdef NSGB_RECON_PROFILE
     const long long _pe = clock64();
 #endif
@@ -706,10 +714,12 @@ __device__ __forceinline__ int initial_tile(int i, int ntiles, int tiles_x, int 
   return i;
 }
 
-__global__ void recon_init_kernel(Ctl c, int ntiles, int tiles_x, int order) {
+__global__ void recon_init_kernel(Ctl c, Imgs I, int ntiles, int order) {
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < c.cap; i += gridDim.x * blockDim.x) {
     if ((int)i < ntiles) {
-      c.slots[i].val = initial_tile((int)i, ntiles, tiles_x, order);
+      const Img im = img_at(I, img_of(I, (int)i, RTileBase()));
+      const int local = (int)i - im.r_tile_base;
+      c.slots[i].val = im.r_tile_base + initial_tile(local, im.r_tiles_x * im.r_tiles_y, im.r_tiles_x, order);
       c.slots[i].seq = i + 1u;
       c.state[i] = kQueued;
     } else {
@@ -748,22 +758,14 @@ inline unsigned ring_cap(int64_t ntiles) {
   return c;
 }
 
-template <typename T, int CONN>
-cudaError_t launch_typed(void* out, const void* mask, int64_t H, int64_t W, int64_t pitch, bool erode, bool ring,
-                         void* ws, cudaStream_t s, int max_visits_per_tile, int max_iters) {
-  Args<T> a;
-  a.out = (T*)out;
-  a.mask = (const T*)mask;
-  a.pitch = pitch;
-  a.H = (int)H;
-  a.W = (int)W;
-  a.tiles_x = tiles_x_for<T>(W);
-  a.tiles_y = (int)((H + kRows - 1) / kRows);
-  a.ntiles = a.tiles_x * a.tiles_y;
+template <typename T, int CONN, bool BATCH>
+cudaError_t launch_typed(const Imgs& I, int ntiles, bool erode, bool ring, void* ws, cudaStream_t s,
+                         int max_visits_per_tile, int max_iters) {
+  Args a;
+  a.I = I;
+  a.ntiles = ntiles;
   a.flip = erode ? 1 : 0;
   a.ring = ring ? 1 : 0;
-  const int vec = Px<T>::E == 2 ? 2 * (int)sizeof(T) : (int)sizeof(T);
-  a.aligned = (((uintptr_t)out % vec) == 0 && ((uintptr_t)mask % vec) == 0 && (pitch % vec) == 0) ? 1 : 0;
   a.max_iters = max_iters > 0 ? max_iters : 4096;
   int* wi = (int*)ws;
   a.c.status = wi + 0;
@@ -774,13 +776,13 @@ cudaError_t launch_typed(void* out, const void* mask, int64_t H, int64_t W, int6
   a.c.tail = (unsigned*)(wi + 9);
   a.c.pending = wi + 10;
   a.c.state = wi + kHdrInts;
-  a.c.cap = ring_cap(a.ntiles);
-  a.c.slots = (Slot*)(a.c.state + ((a.ntiles + 1) & ~1));
-  a.c.max_visits = (long long)(max_visits_per_tile > 0 ? max_visits_per_tile : 1 << 20) * a.ntiles;
+  a.c.cap = ring_cap(ntiles);
+  a.c.slots = (Slot*)(a.c.state + ((ntiles + 1) & ~1));
+  a.c.max_visits = (long long)(max_visits_per_tile > 0 ? max_visits_per_tile : 1 << 20) * ntiles;
 
   cudaError_t e = cudaMemsetAsync(wi, 0, sizeof(int) * kHdrInts, s);
   if (e != cudaSuccess) return e;
-  recon_init_kernel<<<(a.c.cap + 255) / 256, 256, 0, s>>>(a.c, a.ntiles, a.tiles_x, recon_order());
+  recon_init_kernel<<<(a.c.cap + 255) / 256, 256, 0, s>>>(a.c, I, ntiles, recon_order());
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
 
@@ -790,40 +792,83 @@ cudaError_t launch_typed(void* out, const void* mask, int64_t H, int64_t W, int6
   cudaGetDevice(&dev);
   int& occ = occ_cache[dev & 7];
   if (occ == 0) {
-    e = cudaFuncSetAttribute(recon_kernel<T, CONN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(recon_kernel<T, CONN, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int bps = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, recon_kernel<T, CONN>, kWarps * 32, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, recon_kernel<T, CONN, BATCH>, kWarps * 32, smem);
     if (e != cudaSuccess) return e;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     occ = bps * sms;
     if (occ <= 0) return cudaErrorLaunchOutOfResources;
   }
-  int grid = (a.ntiles + kWarps - 1) / kWarps;
+  int grid = (ntiles + kWarps - 1) / kWarps;
   if (grid > occ) grid = occ;
   if (grid < 1) grid = 1;
   void* args[] = {&a};
   // Cooperative launch: all CTAs are co-resident, so warps waiting on the queue never block
   // warps that still have to be scheduled.
-  return cudaLaunchCooperativeKernel((const void*)recon_kernel<T, CONN>, dim3(grid), dim3(kWarps * 32), args, smem,
+  return cudaLaunchCooperativeKernel((const void*)recon_kernel<T, CONN, BATCH>, dim3(grid), dim3(kWarps * 32), args, smem,
                                      s);
 }
 
 }  // namespace
 
-size_t recon_workspace_bytes(int dtype, int64_t H, int64_t W) {
-  int64_t tx = 0;
+int recon_tiles_x(int dtype, int64_t W) {
   switch (dtype) {
-    case NSGB_U8: tx = tiles_x_for<uint8_t>(W); break;
-    case NSGB_U16: tx = tiles_x_for<uint16_t>(W); break;
-    case NSGB_I32: tx = tiles_x_for<int32_t>(W); break;
-    case NSGB_F32: tx = tiles_x_for<float>(W); break;
+    case NSGB_U8: return tiles_x_for<uint8_t>(W);
+    case NSGB_U16: return tiles_x_for<uint16_t>(W);
+    case NSGB_I32: return tiles_x_for<int32_t>(W);
+    case NSGB_F32: return tiles_x_for<float>(W);
     default: return 0;
   }
-  const int64_t ty = (H + kRows - 1) / kRows;
-  const int64_t nt = tx * ty;
+}
+
+int recon_tiles_y(int64_t H) { return (int)((H + kRows - 1) / kRows); }
+
+size_t recon_workspace_bytes_tiles(int64_t nt) {
   return sizeof(int) * (size_t)(kHdrInts + ((nt + 1) & ~1) + 2 * (int64_t)ring_cap(nt));
+}
+
+size_t recon_workspace_bytes(int dtype, int64_t H, int64_t W) {
+  const int tx = recon_tiles_x(dtype, W);
+  if (tx <= 0) return 0;
+  return recon_workspace_bytes_tiles((int64_t)tx * recon_tiles_y(H));
+}
+
+cudaError_t recon_launch_batch(int dtype, const Imgs& I, int ntiles, int conn, bool erode, bool ring, void* ws,
+                               cudaStream_t s, int max_visits, int max_iters) {
+  switch (dtype) {
+#define NSGB_RECON_CASE(CODE, TYPE)                                                                       \
+  case CODE:                                                                                               \
+    if (I.d)                                                                                               \
+      return conn == 8 ? launch_typed<TYPE, 8, true>(I, ntiles, erode, ring, ws, s, max_visits, max_iters) \
+                       : launch_typed<TYPE, 4, true>(I, ntiles, erode, ring, ws, s, max_visits, max_iters);\
+    return conn == 8 ? launch_typed<TYPE, 8, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters)  \
+                     : launch_typed<TYPE, 4, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters);
+    NSGB_RECON_CASE(NSGB_U8, uint8_t)
+    NSGB_RECON_CASE(NSGB_U16, uint16_t)
+    NSGB_RECON_CASE(NSGB_I32, int32_t)
+    NSGB_RECON_CASE(NSGB_F32, float)
+#undef NSGB_RECON_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+Img recon_image(int dtype, void* plane, const void* mask, int64_t H, int64_t W, int64_t pitch) {
+  Img m = {};
+  m.plane = plane;
+  m.aux = mask;
+  m.pitch = pitch;
+  m.H = (int)H;
+  m.W = (int)W;
+  const int esz = elem_size(dtype);
+  const int vec = (dtype == NSGB_U8 || dtype == NSGB_U16) ? 2 * esz : esz;
+  m.aligned = (((uintptr_t)plane % vec) == 0 && ((uintptr_t)mask % vec) == 0 && (pitch % vec) == 0) ? 1 : 0;
+  m.r_tiles_x = recon_tiles_x(dtype, W);
+  m.r_tiles_y = recon_tiles_y(H);
+  m.r_tile_base = 0;
+  return m;
 }
 
 cudaError_t recon_launch(int dtype, void* out, const void* marker, const void* mask, int64_t H, int64_t W,
@@ -835,18 +880,11 @@ cudaError_t recon_launch(int dtype, void* out, const void* marker, const void* m
     cudaError_t e = cudaMemcpy2DAsync(out, pitch, marker, pitch, (size_t)W * esz, (size_t)H, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return e;
   }
-  switch (dtype) {
-#define NSGB_RECON_CASE(CODE, TYPE)                                                                           \
-  case CODE:                                                                                                   \
-    return conn == 8 ? launch_typed<TYPE, 8>(out, mask, H, W, pitch, erode, ring, ws, s, max_visits, max_iters) \
-                     : launch_typed<TYPE, 4>(out, mask, H, W, pitch, erode, ring, ws, s, max_visits, max_iters);
-    NSGB_RECON_CASE(NSGB_U8, uint8_t)
-    NSGB_RECON_CASE(NSGB_U16, uint16_t)
-    NSGB_RECON_CASE(NSGB_I32, int32_t)
-    NSGB_RECON_CASE(NSGB_F32, float)
-#undef NSGB_RECON_CASE
-    default: return cudaErrorInvalidValue;
-  }
+  Imgs I = {};
+  I.n = 1;
+  I.one = recon_image(dtype, out, mask, H, W, pitch);
+  return recon_launch_batch(dtype, I, I.one.r_tiles_x * I.one.r_tiles_y, conn, erode, ring, ws, s, max_visits,
+                            max_iters);
 }
 
 }  // namespace nsgb

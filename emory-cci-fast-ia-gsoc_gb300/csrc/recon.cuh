@@ -5,7 +5,20 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include "batch.cuh"
+
 namespace nsgb {
+
+// Reconstruction tile grid of an image (tiles are 32 rows x 32 packed words).
+int recon_tiles_x(int dtype, int64_t W);
+int recon_tiles_y(int64_t H);
+size_t recon_workspace_bytes_tiles(int64_t ntiles);
+// An image descriptor for reconstruction (tile bases left at 0).
+Img recon_image(int dtype, void* plane, const void* mask, int64_t H, int64_t W, int64_t pitch);
+// Reconstructs every image of the batch in place (Img::plane holds the marker, Img::aux the
+// mask) in one persistent launch over all their tiles.
+cudaError_t recon_launch_batch(int dtype, const Imgs& I, int ntiles, int conn, bool erode, bool ring, void* ws,
+                               cudaStream_t s, int max_visits, int max_iters);
 
 // Workspace bytes for a reconstruction of an H x W image of `dtype`.
 size_t recon_workspace_bytes(int dtype, int64_t H, int64_t W);

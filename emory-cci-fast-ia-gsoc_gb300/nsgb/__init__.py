@@ -23,7 +23,8 @@ from ._ffi import NsgbError, lib
 
 __all__ = [
     "imreconstruct", "imreconstructBinary", "imfillHoles", "imhmin", "bwselect", "bwlabel", "bwlabel2",
-    "bwareaopen2", "threshold", "invert", "chain", "NsgbError", "workspace",
+    "bwareaopen2", "threshold", "invert", "chain", "imreconstructQueueThroughput", "chain_batch", "BatchPlan",
+    "NsgbError", "workspace",
 ]
 
 _DT = {torch.uint8: _ffi.U8, torch.int32: _ffi.I32, torch.float32: _ffi.F32}
@@ -283,3 +284,78 @@ def chain(marker: torch.Tensor, mask: torch.Tensor, recon_conn: int = 8, thr: fl
     _ffi.check(st, "chain")
     return {"recon": rec, "fill": fill, "labels": labels, "area": area, "n_labels": int(nl.value),
             "n_kept": int(nk.value)}
+
+
+class BatchPlan:
+    """A prepared batch of tiles (nsgb_batch_prepare): the image table lives in a workspace
+    owned by this object; `chain()` / `reconstruct()` then launch kernels only."""
+
+    def __init__(self, markers, masks, with_outputs: bool = True) -> None:
+        if len(markers) != len(masks) or not markers:
+            raise NsgbError(1, "batch: markers and masks must be non-empty lists of equal length")
+        dt = _dtype_code(masks[0])
+        self.markers = [_contig(m) for m in markers]
+        self.masks = [_contig(m) for m in masks]
+        self.fill, self.labels, self.area = [], [], []
+        tiles = (_ffi.Tile * len(markers))()
+        for i, (mk, ms) in enumerate(zip(self.markers, self.masks)):
+            _check_image(mk, "marker")
+            _check_image(ms, "mask")
+            _same_shape(mk, ms, "batch")
+            if _dtype_code(ms) != dt:
+                raise NsgbError(1, "batch: all tiles must share one dtype")
+            rows, cols = ms.shape
+            if with_outputs:
+                self.fill.append(torch.empty((rows, cols), dtype=torch.uint8, device=ms.device))
+                self.labels.append(torch.empty((rows, cols), dtype=torch.int32, device=ms.device))
+                self.area.append(torch.empty((rows, cols), dtype=torch.uint8, device=ms.device))
+            tiles[i] = _ffi.Tile(mk.data_ptr(), ms.data_ptr(), rows, cols, _pitch(ms),
+                                 self.fill[i].data_ptr() if with_outputs else None,
+                                 self.labels[i].data_ptr() if with_outputs else None,
+                                 self.area[i].data_ptr() if with_outputs else None)
+        need = lib.nsgb_batch_workspace_size(dt, tiles, len(markers))
+        if need == 0:
+            raise NsgbError(1, "batch: bad tiles (or more than 2^31 pixels in total)")
+        self._ws = torch.empty(need + 256, dtype=torch.uint8, device=self.masks[0].device)
+        ptr = (self._ws.data_ptr() + 255) & ~255
+        self.batch = _ffi.Batch()
+        _ffi.check(lib.nsgb_batch_prepare(dt, tiles, len(markers), ptr, need, C.byref(self.batch)), "batch_prepare")
+        self.n = len(markers)
+
+    def chain(self, recon_conn=8, thr=128.0, fill_conn=4, label_conn=8, area_min=11, area_max=1000,
+              counts: bool = True, sync: bool = True):
+        nl = (C.c_int32 * self.n)() if counts else None
+        nk = (C.c_int32 * self.n)() if counts else None
+        opts = _ffi.Opts(1 if sync else 0, 0, 0)
+        st = lib.nsgb_chain_batch(C.byref(self.batch), recon_conn, float(thr), fill_conn, label_conn, int(area_min),
+                                  int(area_max), nl, nk, _stream(), C.byref(opts))
+        _ffi.check(st, "chain_batch")
+        if counts:
+            return list(nl), list(nk)
+        return None
+
+    def reconstruct(self, connectivity: int, erode: bool = False, sync: bool = True) -> None:
+        opts = _ffi.Opts(1 if sync else 0, 0, 0)
+        st = lib.nsgb_imreconstruct_batch(C.byref(self.batch), connectivity, 1 if erode else 0, _stream(),
+                                          C.byref(opts))
+        _ffi.check(st, "imreconstruct_batch")
+
+
+def imreconstructQueueThroughput(seeds, images, connectivity: int, nItFirstPass: int = 0):
+    """nscale::gpu::imreconstructQueueThroughput<T> (MorphologicOperationsGPU.cpp:447-545):
+    reconstruct a list of tiles in one batched launch.  Returns new tensors (nItFirstPass is
+    accepted for compatibility and has no meaning here)."""
+    outs = [_contig(s).clone() for s in seeds]
+    plan = BatchPlan(outs, list(images), with_outputs=False)
+    plan.reconstruct(connectivity)
+    return outs
+
+
+def chain_batch(markers, masks, recon_conn=8, thr=128.0, fill_conn=4, label_conn=8, area_min=11, area_max=1000):
+    """The segmentation chain on a batch of tiles (one launch per stage for all of them).
+    Returns a list of dicts like `chain`."""
+    recon = [_contig(m).clone() for m in markers]
+    plan = BatchPlan(recon, list(masks))
+    nl, nk = plan.chain(recon_conn, thr, fill_conn, label_conn, area_min, area_max)
+    return [{"recon": recon[i], "fill": plan.fill[i], "labels": plan.labels[i], "area": plan.area[i],
+             "n_labels": nl[i], "n_kept": nk[i]} for i in range(plan.n)]

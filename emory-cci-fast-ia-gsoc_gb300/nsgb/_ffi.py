@@ -38,6 +38,17 @@ class Opts(C.Structure):
                 ("reserved", C.c_int * 5), ("recon_event_begin", C.c_void_p), ("recon_event_end", C.c_void_p)]
 
 
+class Tile(C.Structure):
+    _fields_ = [("marker", C.c_void_p), ("mask", C.c_void_p), ("rows", C.c_int64), ("cols", C.c_int64),
+                ("pitch", C.c_int64), ("fill_out", C.c_void_p), ("labels_out", C.c_void_p), ("area_out", C.c_void_p)]
+
+
+class Batch(C.Structure):
+    _fields_ = [("dtype", C.c_int), ("n", C.c_int), ("total_px", C.c_int64), ("recon_tiles", C.c_int),
+                ("label_tiles", C.c_int), ("rank_blocks", C.c_int), ("total_rows", C.c_int), ("max_cols", C.c_int),
+                ("max_perimeter", C.c_int), ("ws", C.c_void_p), ("ws_bytes", C.c_size_t), ("reserved", C.c_int * 8)]
+
+
 def _load() -> C.CDLL:
     if not os.path.exists(LIB_PATH):
         raise ImportError(f"libnsgb.so is not built ({LIB_PATH}); run __graft_entry__.build()")
@@ -67,6 +78,11 @@ _SIGS = {
     "nsgb_invert": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _vp]),
     "nsgb_chain": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _int, _dbl, _int, _int, C.c_int32, C.c_int32,
                           _vp, _vp, _vp, _i32p, _i32p, _vp, _sz, _vp, _optp]),
+    "nsgb_batch_workspace_size": (_sz, [_int, C.POINTER(Tile), _int]),
+    "nsgb_batch_prepare": (_int, [_int, C.POINTER(Tile), _int, _vp, _sz, C.POINTER(Batch)]),
+    "nsgb_chain_batch": (_int, [C.POINTER(Batch), _int, _dbl, _int, _int, C.c_int32, C.c_int32, _i32p, _i32p, _vp,
+                                _optp]),
+    "nsgb_imreconstruct_batch": (_int, [C.POINTER(Batch), _int, _int, _vp, _optp]),
     "nsgb_synth_tile_u8": (_int, [_vp, _vp, _i64, _i64, _i64, _i64, C.c_uint64]),
     "nsgb_synth_scale_u16": (_int, [_vp, _vp, _vp, _i64]),
     "nsgb_synth_scale_i32": (_int, [_vp, _vp, _vp, _i64]),

@@ -172,6 +172,46 @@ nsgb_status nsgb_chain(int dtype, void* marker, const void* mask, int64_t rows, 
                        uint8_t* area_out, int32_t* n_labels, int32_t* n_kept, void* ws,
                        size_t ws_bytes, nsgb_stream_t stream, const nsgb_opts* opts);
 
+/* ---- Batches: many images of uneven sizes in one persistent reconstruction launch and one
+ * launch per labelling stage (the reference's imreconstructQueueThroughput<T>,
+ * MorphologicOperationsGPU.cpp:447-545 -> morphReconVector, cuda/global_queue.cu:903-968,
+ * batched up to 70 images with one CTA each; here any number, the work of all images shared
+ * by the whole GPU). */
+typedef struct {
+  void* marker;        /* in: marker; out: reconstruction (in place) */
+  const void* mask;
+  int64_t rows, cols, pitch; /* pitch in bytes, shared by marker and mask */
+  uint8_t* fill_out;   /* chain outputs, dense rows x cols (each optional) */
+  int32_t* labels_out;
+  uint8_t* area_out;
+} nsgb_tile;
+
+/* Host copy of a prepared batch (filled by nsgb_batch_prepare; treat as opaque). */
+typedef struct {
+  int dtype, n;
+  int64_t total_px;
+  int recon_tiles, label_tiles, rank_blocks, total_rows, max_cols, max_perimeter;
+  void* ws;
+  size_t ws_bytes;
+  int reserved[8];
+} nsgb_batch;
+
+/* Workspace bytes for a batch (total pixels must stay below 2^31). */
+size_t nsgb_batch_workspace_size(int dtype, const nsgb_tile* tiles, int n_tiles);
+/* Writes the batch's image table into `ws` (synchronous) and fills `batch`.  Afterwards the
+ * batch calls below enqueue kernels only, so they can be replayed many times (and recorded
+ * once) with the same tiles. */
+nsgb_status nsgb_batch_prepare(int dtype, const nsgb_tile* tiles, int n_tiles, void* ws, size_t ws_bytes,
+                               nsgb_batch* batch);
+/* nsgb_chain on every tile of the batch; n_labels / n_kept: optional host arrays of n_tiles
+ * (forcing a synchronization). */
+nsgb_status nsgb_chain_batch(const nsgb_batch* batch, int recon_conn, double thr, int fill_conn,
+                             int label_conn, int32_t area_min, int32_t area_max, int32_t* n_labels,
+                             int32_t* n_kept, nsgb_stream_t stream, const nsgb_opts* opts);
+/* nsgb_imreconstruct on every tile of the batch, in place on each marker. */
+nsgb_status nsgb_imreconstruct_batch(const nsgb_batch* batch, int conn, int erode, nsgb_stream_t stream,
+                                     const nsgb_opts* opts);
+
 /* Size of the device scratch built into the library for nsgb_imreconstruct_noalloc: 1 MiB,
  * enough for images of up to 65536 reconstruction tiles -- 134 Mpixel for u8/u16 (tiles of
  * 32 x 64 pixels), 67 Mpixel for i32/f32 (32 x 32), e.g. 8192 x 16384 u8. */
