@@ -34,7 +34,9 @@ PKG = os.path.join(ROOT, "emory-cci-fast-ia-gsoc_gb300")
 sys.path.insert(0, PKG)
 
 METRIC = "imreconstruct+bwlabel MPix/s, uint8 4096², plain vs batched GPU; % of HBM peak"
-KERNELS_PER_CHAIN = 12  # recon 1 + fill 4 + label 3 + rank 3 + output 1 (see csrc/ops.cu nsgb_chain)
+# recon init + recon, fill (local, merge, flatten, border seeds, output), label (local, merge,
+# flatten), rank (count, scan, assign), label/area output: see csrc/ops.cu chain_impl
+KERNELS_PER_CHAIN = 14
 RECON_BYTES_PER_PX = 3  # marker read + mask read + result write (u8)
 CHAIN_BYTES_PER_PX = 17  # recon 3 + threshold 2 + fill 2 + bwlabel 5 + bwareaopen 5
 
@@ -49,6 +51,10 @@ def parse_args():
     p.add_argument("--ellipses", type=int, default=6000)
     p.add_argument("--e2e-steps", type=int, default=50)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--batch-tiles", type=int, default=256)
+    p.add_argument("--batch-steps", type=int, default=5)
+    p.add_argument("--batch-dtypes", default="u8,u16,i32")
+    p.add_argument("--no-batch", action="store_true")
     return p.parse_args()
 
 
@@ -377,11 +383,208 @@ def run_nsgb(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_port(marker_h, mask_h)
+    if not args.no_batch:
+        line["batched"] = batched_section(args, dev)
     if rank == 0:
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+# -- batched form ---------------------------------------------------------------------------
+BATCH_SCALE = {"u8": 1, "u16": 257, "i32": 1000}
+
+
+def batch_tiles_host(n, seed_sizes=0xC2):
+    """n synthetic u8 tiles (mask, marker); H and W i.i.d. uniform in [256, 4096], one ellipse
+    per 2800 px^2, tile i generated with seed i.  Generated on all host threads."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from nsgb import synth
+
+    h, w = synth.tile_sizes(n, 256, 4096, seed_sizes)
+    with ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+        return list(ex.map(lambda i: synth.tile_u8(int(h[i]), int(w[i]), synth.ellipses_for(int(h[i]), int(w[i])), i),
+                           range(n)))
+
+
+class FlatTiles:
+    """Tiles of one dtype packed into one device buffer (each tile starts 256-byte aligned), so
+    that all markers are restored with one copy."""
+
+    def __init__(self, shapes, torch_dtype, dev):
+        import torch
+        # zero-filled so that the padding between tiles compares equal across buffers
+
+        esz = torch.empty((), dtype=torch_dtype).element_size()
+        self.offsets, off = [], 0
+        for hh, ww in shapes:
+            self.offsets.append(off)
+            off += (hh * ww * esz + 255) // 256 * 256
+        self.buf = torch.zeros(off // esz, dtype=torch_dtype, device=dev)
+        self.esz = esz
+        self.views = [self.buf[o // esz:o // esz + hh * ww].view(hh, ww) for o, (hh, ww) in zip(self.offsets, shapes)]
+
+
+def run_batched(args, dev, tiles_u8, dtype):
+    """Plain per-tile loop (nsgb_chain per tile on one stream) against the batched chain
+    (nsgb_chain_batch recorded once in a CUDA graph and replayed) on the same tiles."""
+    import torch
+
+    from nsgb import _ffi, synth
+
+    lib = _ffi.lib
+    tdt = {"u8": torch.uint8, "u16": torch.int16, "i32": torch.int32}[dtype]
+    code = {"u8": _ffi.U8, "u16": _ffi.U16, "i32": _ffi.I32}[dtype]
+    thr = 128.0 * BATCH_SCALE[dtype]
+    shapes = [m.shape for m, _ in tiles_u8]
+    n = len(shapes)
+    total_px = sum(hh * ww for hh, ww in shapes)
+    mask, marker, work = (FlatTiles(shapes, tdt, dev) for _ in range(3))
+    for i, (m8, k8) in enumerate(tiles_u8):
+        if dtype == "u8":
+            m, k = m8, k8
+        else:
+            m, k = synth.scale(m8, dtype)
+            if dtype == "u16":
+                m, k = m.view("int16"), k.view("int16")
+        mask.views[i].copy_(torch.from_numpy(m))
+        marker.views[i].copy_(torch.from_numpy(k))
+    outs = {}
+    for arm in ("plain", "batch"):
+        outs[arm] = (FlatTiles(shapes, torch.uint8, dev), FlatTiles(shapes, torch.int32, dev),
+                     FlatTiles(shapes, torch.uint8, dev))
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+
+    # plain loop: one workspace sized for the largest tile
+    mh, mw = max(s[0] for s in shapes), max(s[1] for s in shapes)
+    ws_bytes = lib.nsgb_workspace_size(_ffi.OP_CHAIN, code, mh, mw)
+    ws_t = torch.empty(ws_bytes + 256, dtype=torch.uint8, device=dev)
+    ws = (ws_t.data_ptr() + 255) & ~255
+    plain_counts = [(C.c_int32(0), C.c_int32(0)) for _ in range(n)]
+    sync_opts, async_opts = _ffi.Opts(1, 0, 0), _ffi.Opts(0, 0, 0)
+    fo, lo, ao = outs["plain"]
+
+    def plain(with_counts):
+        for i, (hh, ww) in enumerate(shapes):
+            nl, nk = plain_counts[i]
+            st = lib.nsgb_chain(code, work.views[i].data_ptr(), mask.views[i].data_ptr(), hh, ww, ww * work.esz, 8,
+                                thr, 4, 8, 11, 1000, fo.views[i].data_ptr(), lo.views[i].data_ptr(),
+                                ao.views[i].data_ptr(), C.byref(nl) if with_counts else None,
+                                C.byref(nk) if with_counts else None, ws, ws_bytes, sp,
+                                C.byref(sync_opts if with_counts else async_opts))
+            if st != 0:
+                raise RuntimeError(f"nsgb_chain tile {i}: {_ffi.STATUS.get(st, st)}")
+
+    # batch: prepare once, record the chain and the count copy in a CUDA graph
+    bf, bl, ba = outs["batch"]
+    tarr = (_ffi.Tile * n)()
+    for i, (hh, ww) in enumerate(shapes):
+        tarr[i] = _ffi.Tile(work.views[i].data_ptr(), mask.views[i].data_ptr(), hh, ww, ww * work.esz,
+                            bf.views[i].data_ptr(), bl.views[i].data_ptr(), ba.views[i].data_ptr())
+    bws_bytes = lib.nsgb_batch_workspace_size(code, tarr, n)
+    if bws_bytes == 0:
+        raise RuntimeError("batch too large for one workspace")
+    bws_t = torch.empty(bws_bytes + 256, dtype=torch.uint8, device=dev)
+    bws = (bws_t.data_ptr() + 255) & ~255
+    batch = _ffi.Batch()
+    _ffi.check(lib.nsgb_batch_prepare(code, tarr, n, bws, bws_bytes, C.byref(batch)), "batch_prepare")
+    counts = torch.zeros(2 * n, dtype=torch.int32).pin_memory()
+
+    def batch_call():
+        _ffi.check(lib.nsgb_chain_batch(C.byref(batch), 8, thr, 4, 8, 11, 1000, None, None,
+                                        C.c_void_p(torch.cuda.current_stream().cuda_stream), C.byref(async_opts)),
+                   "chain_batch")
+        _ffi.check(lib.nsgb_batch_counts_async(C.byref(batch), counts.data_ptr(),
+                                               C.c_void_p(torch.cuda.current_stream().cuda_stream)),
+                   "batch_counts_async")
+
+    work.buf.copy_(marker.buf)
+    batch_call()  # warm the launch path outside the capture
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    cs = torch.cuda.Stream()
+    cs.wait_stream(stream)
+    with torch.cuda.stream(cs):
+        graph.capture_begin()
+        batch_call()
+        graph.capture_end()
+    stream.wait_stream(cs)
+    torch.cuda.synchronize()
+
+    def timed(fn, steps, warmup):
+        res = []
+        for k in range(warmup + steps):
+            work.buf.copy_(marker.buf)  # marker restore, outside the events
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            if k >= warmup:
+                res.append(a.elapsed_time(b))
+        return statistics.mean(res)
+
+    steps, warm = args.batch_steps, 3
+    t_plain = timed(lambda: plain(True), steps, warm)
+    t_plain_async = timed(lambda: plain(False), steps, warm)
+    plain(True)  # leave the plain outputs of an exact run (work restored by the last timed step)
+    torch.cuda.synchronize()
+    pc = [(a.value, b.value) for a, b in plain_counts]
+    work.buf.copy_(marker.buf)
+    t_batch = timed(graph.replay, steps, warm)
+    torch.cuda.synchronize()
+    st = lib.nsgb_device_status(C.c_void_p(bws), sp)
+    if st != 0:
+        raise RuntimeError(f"batch device status: {_ffi.STATUS.get(st, st)}")
+    bc = counts.view(n, 2).tolist()
+    same = (all(tuple(x) == y for x, y in zip(bc, pc)) and torch.equal(bf.buf, fo.buf) and torch.equal(bl.buf, lo.buf)
+            and torch.equal(ba.buf, ao.buf))
+    mp = total_px / 1e6
+    return {
+        "plain_mpix_s": mp / (t_plain / 1e3), "plain_ms": t_plain,
+        "plain_async_mpix_s": mp / (t_plain_async / 1e3), "plain_async_ms": t_plain_async,
+        "batched_graph_mpix_s": mp / (t_batch / 1e3), "batched_ms": t_batch,
+        "speedup_vs_plain": t_plain / t_batch, "speedup_vs_plain_async": t_plain_async / t_batch,
+        "batch_equals_single_tile": bool(same),
+        "gpu_launches_per_batch": KERNELS_PER_CHAIN,
+    }
+
+
+def cpu_tile_parallel(tiles_u8, budget_tiles):
+    """The oracle chain, one tile per host thread, on the first `budget_tiles` tiles."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    sample = tiles_u8[:budget_tiles]
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        list(ex.map(lambda mk: oracle.chain(mk[1], mk[0]), sample))
+    dt = time.perf_counter() - t0
+    px = sum(m.size for m, _ in sample)
+    return {"value": px / 1e6 / dt, "unit": "MPix/s", "cores": threads, "kind": "port",
+            "sample": f"first {len(sample)} of the u8 tiles, one tile per thread, {dt:.1f} s"}
+
+
+def batched_section(args, dev):
+    tiles = batch_tiles_host(args.batch_tiles)
+    res = {"workload": f"{args.batch_tiles} tiles, H and W i.i.d. uniform in [256,4096], 1 ellipse per 2800 px^2, "
+                       "chain (a)-(e) per tile; u16 = u8 x 257, i32 = u8 x 1000 (threshold scaled the same way)",
+           "total_px": int(sum(m.size for m, _ in tiles)),
+           "plain": "nsgb_chain per tile on one stream, counts read per tile (the reference API returns them)",
+           "plain_async": "nsgb_chain per tile on one stream, no count reads",
+           "batched": "nsgb_chain_batch + nsgb_batch_counts_async recorded once in a CUDA graph, replayed",
+           "l2": "inputs larger than L2; marker restore outside the timed events"}
+    for d in [x for x in args.batch_dtypes.split(",") if x]:
+        res[d] = run_batched(args, dev, tiles, d)
+    if not args.no_cpu_baseline:
+        res["cpu_tile_parallel"] = cpu_tile_parallel(tiles, 2 * (os.cpu_count() or 1))
+    return res
 
 
 def main():

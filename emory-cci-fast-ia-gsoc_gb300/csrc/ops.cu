@@ -896,6 +896,16 @@ nsgb_status nsgb_chain_batch(const nsgb_batch* batch, int recon_conn, double thr
   return finish(e, w.status, s, opts);
 }
 
+nsgb_status nsgb_batch_counts_async(const nsgb_batch* batch, int32_t* counts, nsgb_stream_t stream) {
+  Plan P;
+  Ws w;
+  if (!counts) return NSGB_ERR_BAD_ARG;
+  nsgb_status st = batch_plan(batch, &P, &w);
+  if (st != NSGB_OK) return st;
+  return cuda_status(cudaMemcpyAsync(counts, w.counts, 2 * sizeof(int32_t) * (size_t)P.t.n, cudaMemcpyDefault,
+                                     (cudaStream_t)stream));
+}
+
 nsgb_status nsgb_imreconstruct_batch(const nsgb_batch* batch, int conn, int erode, nsgb_stream_t stream,
                                      const nsgb_opts* opts) {
   if (!valid_conn(conn)) return NSGB_ERR_BAD_ARG;

@@ -334,6 +334,13 @@ class BatchPlan:
             return list(nl), list(nk)
         return None
 
+    def counts_async(self, out: torch.Tensor) -> None:
+        """Enqueue the per-tile (n_labels, n_kept) of the last chain into `out` (int32, 2*n,
+        device or pinned host) without synchronising."""
+        if out.dtype != torch.int32 or out.numel() < 2 * self.n or not out.is_contiguous():
+            raise NsgbError(1, "counts_async: need a contiguous int32 tensor of 2*n elements")
+        _ffi.check(lib.nsgb_batch_counts_async(C.byref(self.batch), out.data_ptr(), _stream()), "batch_counts_async")
+
     def reconstruct(self, connectivity: int, erode: bool = False, sync: bool = True) -> None:
         opts = _ffi.Opts(1 if sync else 0, 0, 0)
         st = lib.nsgb_imreconstruct_batch(C.byref(self.batch), connectivity, 1 if erode else 0, _stream(),

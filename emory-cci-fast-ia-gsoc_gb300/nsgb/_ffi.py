@@ -82,6 +82,7 @@ _SIGS = {
     "nsgb_batch_prepare": (_int, [_int, C.POINTER(Tile), _int, _vp, _sz, C.POINTER(Batch)]),
     "nsgb_chain_batch": (_int, [C.POINTER(Batch), _int, _dbl, _int, _int, C.c_int32, C.c_int32, _i32p, _i32p, _vp,
                                 _optp]),
+    "nsgb_batch_counts_async": (_int, [C.POINTER(Batch), _vp, _vp]),
     "nsgb_imreconstruct_batch": (_int, [C.POINTER(Batch), _int, _int, _vp, _optp]),
     "nsgb_synth_tile_u8": (_int, [_vp, _vp, _i64, _i64, _i64, _i64, C.c_uint64]),
     "nsgb_synth_scale_u16": (_int, [_vp, _vp, _vp, _i64]),

@@ -208,6 +208,11 @@ nsgb_status nsgb_batch_prepare(int dtype, const nsgb_tile* tiles, int n_tiles, v
 nsgb_status nsgb_chain_batch(const nsgb_batch* batch, int recon_conn, double thr, int fill_conn,
                              int label_conn, int32_t area_min, int32_t area_max, int32_t* n_labels,
                              int32_t* n_kept, nsgb_stream_t stream, const nsgb_opts* opts);
+/* Enqueues a copy of the per-tile counts of the last nsgb_chain_batch on this batch into
+ * `counts` (device or page-locked host memory, 2 * n_tiles int32: n_labels of tile i at
+ * [2i], n_kept at [2i+1]).  No synchronization, so it can be recorded in a CUDA graph after
+ * nsgb_chain_batch called with n_labels = n_kept = NULL. */
+nsgb_status nsgb_batch_counts_async(const nsgb_batch* batch, int32_t* counts, nsgb_stream_t stream);
 /* nsgb_imreconstruct on every tile of the batch, in place on each marker. */
 nsgb_status nsgb_imreconstruct_batch(const nsgb_batch* batch, int conn, int erode, nsgb_stream_t stream,
                                      const nsgb_opts* opts);

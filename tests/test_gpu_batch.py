@@ -63,3 +63,40 @@ def test_batch_of_one_and_replay(nsgb, oracle):
         assert nl[0] == exp["n_labels"] and nk[0] == exp["n_kept"]
         assert np.array_equal(plan.labels[0].cpu().numpy(), exp["labels"])
         assert np.array_equal(recon.cpu().numpy(), exp["recon"])
+
+
+@pytest.mark.parametrize("dtype", ["u8", "u16", "i32"])
+def test_chain_batch_full_workload(nsgb, oracle, dtype):
+    """The full batched workload: 256 tiles with H, W i.i.d. uniform in [256, 4096] (tile i
+    from seed i, one ellipse per 2800 px^2), every tile checked against the oracle."""
+    import torch
+    from concurrent.futures import ThreadPoolExecutor
+
+    from nsgb import synth
+
+    h, w = synth.tile_sizes(256, 256, 4096, 0xC2)
+    scale = {"u8": 1, "u16": 257, "i32": 1000}[dtype]
+
+    def make(i):
+        m, k = synth.tile_u8(int(h[i]), int(w[i]), synth.ellipses_for(int(h[i]), int(w[i])), i)
+        return (m, k) if dtype == "u8" else synth.scale(m, dtype)
+
+    with ThreadPoolExecutor() as ex:
+        tiles = list(ex.map(make, range(256)))
+    res = nsgb.chain_batch([torch.from_numpy(k).cuda() for _, k in tiles],
+                           [torch.from_numpy(m).cuda() for m, _ in tiles], thr=128 * scale)
+
+    def check(i):
+        m, k = tiles[i]
+        exp = oracle.chain(k, m, thr=128 * scale)
+        got = res[i]
+        return (np.array_equal(got["recon"].cpu().numpy(), exp["recon"])
+                and np.array_equal(got["fill"].cpu().numpy(), exp["fill"])
+                and np.array_equal(got["labels"].cpu().numpy(), exp["labels"])
+                and np.array_equal(got["area"].cpu().numpy(), exp["area"])
+                and got["n_labels"] == exp["n_labels"] and got["n_kept"] == exp["n_kept"])
+
+    torch.cuda.synchronize()
+    with ThreadPoolExecutor() as ex:
+        ok = list(ex.map(check, range(256)))
+    assert all(ok), [i for i, v in enumerate(ok) if not v][:10]
