@@ -23,6 +23,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "batch.cuh"
 #include "common.cuh"
 
@@ -126,6 +128,17 @@ __device__ __forceinline__ TileAt tile_at(const Imgs& I, int b) {
   return t;
 }
 
+// Width of the class values a classifier produces: 8 bits unless it declares `class_t`
+// (the float plateau classifier needs all 32 bits of a value).
+template <class Cls, class = void>
+struct class_type {
+  using type = uint8_t;
+};
+template <class Cls>
+struct class_type<Cls, std::void_t<typename Cls::class_t>> {
+  using type = typename Cls::class_t;
+};
+
 // Each warp owns tile rows (lane = column).  Runs of equal class along a row are found with a
 // ballot and start out joined (label = run start), so unions are only needed where runs of
 // adjacent rows touch: at a pixel that starts its run or sits under the start of a run above
@@ -134,18 +147,19 @@ __device__ __forceinline__ TileAt tile_at(const Imgs& I, int b) {
 // over the tiles of all images).
 template <class Cls, int CONN>
 __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f) {
+  using CT = typename class_type<Cls>::type;
   __shared__ int s_lab[kTile * kTile];
   __shared__ int s_cnt[kTile * kTile];
-  __shared__ uint8_t s_c[kTile * kTile];
+  __shared__ CT s_c[kTile * kTile];
   const TileAt T = tile_at(I, blockIdx.x);
   const int x0 = T.x0, y0 = T.y0, H = T.m.H, W = T.m.W, pb = T.m.px_base;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  uint8_t c[4];
+  CT c[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int ly = ty + 8 * k, i = ly * kTile + tx;
     const int gy = y0 + ly, gx = x0 + tx;
-    c[k] = (uint8_t)((gy < H && gx < W) ? cls(T.m, gy, gx) : 0u);
+    c[k] = (CT)((gy < H && gx < W) ? cls(T.m, gy, gx) : 0u);
     s_c[i] = c[k];
     s_cnt[i] = 0;
   }
@@ -153,7 +167,7 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int ly = ty + 8 * k, i = ly * kTile + tx;
-    const uint8_t left = __shfl_up_sync(NSGB_FULL, c[k], 1);
+    const CT left = (CT)__shfl_up_sync(NSGB_FULL, (uint32_t)c[k], 1);
     same_left[k] = __ballot_sync(NSGB_FULL, tx > 0 && c[k] != 0 && left == c[k]);
     // run start: highest lane <= tx whose pixel does not continue a run from the left
     const unsigned starts = ~same_left[k] & (0xFFFFFFFFu >> (31 - tx));
@@ -164,11 +178,11 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int ly = ty + 8 * k, i = ly * kTile + tx;
-    const uint8_t v = c[k];
+    const CT v = c[k];
     if (!v || ly == 0) continue;
     const bool run_start = !((same_left[k] >> tx) & 1u);
     const int u = i - kTile;
-    const uint8_t up = s_c[u];
+    const CT up = s_c[u];
     const bool up_start = up != 0 && !(tx > 0 && s_c[u - 1] == up);
     if (up == v && (run_start || up_start)) s_union(s_lab, i, u);
     if (CONN == 8) {

@@ -921,3 +921,260 @@ nsgb_status nsgb_imreconstruct_batch(const nsgb_batch* batch, int conn, int erod
 }
 
 }  // extern "C"
+
+// ============================================================================================
+// Differentiable float32 reconstruction by dilation (an extension: the reference has no
+// gradient).  The result only ever copies input values, so each R(p) has one source pixel:
+// mask(q) (clamped at q), marker(q), or the zero ring the reference pads around the image
+// (MorphologicOperations.cpp:671-674, which can only win on a border pixel, as 0).  A source
+// and the pixels that took its value form a plateau (connected, equal R), so the forward
+// labels the plateaus of R with the union-find labeller and gives each the best source it
+// contains (mask before marker before ring, then the smallest raster index):
+//   prov = ~q (mask q), q (marker q), INT32_MIN (ring); q = y * cols + x within the image.
+// The adjoint scatters the upstream gradient along prov with exact 32.32 fixed-point sums.
+namespace nsgb {
+namespace {
+
+constexpr int kKeyNone = 0x7F7F7F7F;  // memset byte 0x7F: no source seen yet
+
+// Plateau class: all 32 bits of R (+0 and -0 merged), plus one so that no value is background.
+struct ClsPlateau {
+  using class_t = uint32_t;
+  __device__ uint32_t operator()(const Img& m, int y, int x) const {
+    uint32_t v = __float_as_uint(pxcg<float>(m.plane, m.pitch, y, x));
+    if ((v << 1) == 0u) v = 0u;
+    return v + 1u;
+  }
+};
+
+__device__ __forceinline__ const void* shifted(const void* p, int64_t off) {
+  return (const void*)((uintptr_t)p + (uintptr_t)off);
+}
+
+// Source key of pixel (y, x): mask q < marker n + q < ring 2n; kKeyNone if p is no source.
+// plane = R, aux = mask, the marker sits `marker_off` bytes from R in every image.
+__device__ __forceinline__ int source_key(const Img& m, int64_t marker_off, int y, int x) {
+  const float r = pxcg<float>(m.plane, m.pitch, y, x);
+  const int n = m.H * m.W, q = y * m.W + x;
+  if (r == px<float>(m.aux, m.pitch, y, x)) return q;
+  if (r == px<float>(shifted(m.plane, marker_off), m.pitch, y, x)) return n + q;
+  if (r == 0.0f && (y == 0 || y == m.H - 1 || x == 0 || x == m.W - 1)) return 2 * n;
+  return kKeyNone;
+}
+
+__global__ void source_best_kernel(Imgs I, int total_rows, int64_t marker_off, const int* __restrict__ L,
+                                   int* __restrict__ best) {
+  ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
+    const int key = source_key(m, marker_off, y, x);
+    if (key == kKeyNone) return;
+    const int r = ccl::root_of(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
+    if (key < __ldcg(&best[r])) atomicMin(&best[r], key);
+  });
+}
+
+__global__ void prov_out_kernel(Imgs I, int total_rows, const int* __restrict__ L, const int* __restrict__ best,
+                                int64_t prov_off, int* status) {
+  ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
+    const int r = ccl::root_of(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
+    const int key = __ldg(&best[r]);
+    const int n = m.H * m.W;
+    int32_t p;
+    if (key < n) p = ~key;
+    else if (key < 2 * n) p = key - n;
+    else {
+      p = INT_MIN;
+      if (key != 2 * n) set_status(status, NSGB_ERR_BAD_ARG);  // a plateau without a source: NaN input
+    }
+    *pxp<int32_t>((void*)shifted(m.plane, prov_off), m.pitch, y, x) = p;
+  });
+}
+
+// Adjoint, pass 1: every pixel adds its gradient (rounded to a multiple of 2^-32) to the
+// accumulator of its source.  Lanes of a warp hold consecutive pixels of one row, which
+// mostly share a source: a segmented warp scan sums runs of equal targets first, so only the
+// last lane of each run issues an atomic.  plane = g, aux = prov.
+__global__ void grad_scatter_kernel(Imgs I, int total_rows, unsigned long long* __restrict__ acc_marker,
+                                    unsigned long long* __restrict__ acc_mask, int* status) {
+  const int lane = threadIdx.x & 31;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int gr = blockIdx.y; gr < total_rows; gr += gridDim.y) {  // uniform per block
+    const Img m = img_at(I, img_of(I, gr, RowBase()));
+    const int y = gr - m.row_base;
+    long long key = -1, v = 0;
+    if (x < m.W) {
+      const int32_t p = px<int32_t>(m.aux, m.pitch, y, x);
+      if (p != INT_MIN) {
+        const int64_t q = p >= 0 ? (int64_t)p : ~(int64_t)p;
+        if (q < (int64_t)m.H * m.W) {
+          v = __double2ll_rn((double)px<float>(m.plane, m.pitch, y, x) * 4294967296.0);
+          key = ((int64_t)m.px_base + q) | (p < 0 ? (1ll << 40) : 0ll);
+        } else {
+          set_status(status, NSGB_ERR_BAD_ARG);
+        }
+      }
+    }
+    const long long kprev = __shfl_up_sync(NSGB_FULL, key, 1);
+    const long long knext = __shfl_down_sync(NSGB_FULL, key, 1);
+    bool head = lane == 0 || kprev != key;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long v2 = __shfl_up_sync(NSGB_FULL, v, o);
+      const bool h2 = __shfl_up_sync(NSGB_FULL, head, o);
+      if (lane >= o && !head) {
+        v += v2;
+        head = h2;
+      }
+    }
+    const bool tail = lane == 31 || knext != key;
+    if (tail && key >= 0) {
+      unsigned long long* a = (key >> 40) ? acc_mask : acc_marker;
+      atomicAdd(a + (key & ((1ll << 40) - 1)), (unsigned long long)v);
+    }
+  }
+}
+
+// Adjoint, pass 2: accumulators to float.  plane = g; dmarker / dmask at byte offsets.
+__global__ void grad_out_kernel(Imgs I, int total_rows, const long long* __restrict__ acc_marker,
+                                const long long* __restrict__ acc_mask, int64_t dmarker_off, int64_t dmask_off) {
+  ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
+    const int64_t gi = (int64_t)m.px_base + (int64_t)y * m.W + x;
+    const double s = 2.3283064365386962890625e-10;  // 2^-32
+    *pxp<float>((void*)shifted(m.plane, dmarker_off), m.pitch, y, x) =
+        __double2float_rn(__ll2double_rn(__ldcs(acc_marker + gi)) * s);
+    *pxp<float>((void*)shifted(m.plane, dmask_off), m.pitch, y, x) =
+        __double2float_rn(__ll2double_rn(__ldcs(acc_mask + gi)) * s);
+  });
+}
+
+// Image table of `n` equally sized images `stride` bytes apart (image 0 = proto).
+__global__ void stack_table_kernel(Img proto, int n, int64_t stride, BatchTotals one, Img* table) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Img m = proto;
+  m.plane = (void*)((uintptr_t)proto.plane + (uintptr_t)(i * stride));
+  m.aux = (const void*)((uintptr_t)proto.aux + (uintptr_t)(i * stride));
+  m.r_tile_base = i * one.r_tiles;
+  m.c_tile_base = i * one.c_tiles;
+  m.px_base = (int)(i * one.px);
+  m.blk_base = i * one.blocks;
+  m.row_base = i * one.rows;
+  table[i] = m;
+}
+
+// Totals of `n` stacked copies of one image's plan.
+BatchTotals stacked_totals(const BatchTotals& one, int64_t n) {
+  BatchTotals t = one;
+  t.n = (int)n;
+  t.px = one.px * n;
+  t.r_tiles = (int)(one.r_tiles * n);
+  t.c_tiles = (int)(one.c_tiles * n);
+  t.blocks = (int)(one.blocks * n);
+  t.rows = (int)(one.rows * n);
+  return t;
+}
+
+bool f32_dims_ok(int64_t batch, int64_t rows, int64_t cols, int64_t pitch, int64_t stride) {
+  if (batch <= 0 || rows <= 0 || cols <= 0 || rows >= INT_MAX || cols >= INT_MAX) return false;
+  if (pitch < cols * 4 || pitch % 4) return false;
+  const int64_t n = rows * cols;
+  if (2 * n >= kKeyNone || n * batch >= (int64_t)INT_MAX || rows * batch >= (int64_t)INT_MAX) return false;
+  if (batch > 1 && (stride < rows * pitch || stride % 4)) return false;
+  return true;
+}
+
+size_t f32_fwd_bytes(int64_t batch, int64_t rows, int64_t cols) {
+  const Plan P1 = single_plan(NSGB_F32, nullptr, nullptr, rows, cols, cols * 4);
+  return ws_sizes(stacked_totals(P1.t, batch)).total;
+}
+
+size_t f32_bwd_bytes(int64_t batch, int64_t rows, int64_t cols) {
+  const size_t px = (size_t)(batch * rows * cols);
+  return 256 + 2 * align256(8 * px) + (batch > 1 ? align256(sizeof(Img) * (size_t)batch) : 0);
+}
+
+// Plan over the stacked images; with more than one image the table is built on the device.
+cudaError_t stacked_plan(void* plane, const void* aux, int64_t batch, int64_t rows, int64_t cols, int64_t pitch,
+                         int64_t stride, Img* table, Plan* P, cudaStream_t s) {
+  const Plan P1 = single_plan(NSGB_F32, plane, aux, rows, cols, pitch);
+  P->t = stacked_totals(P1.t, batch);
+  P->I = P1.I;
+  P->I.n = (int)batch;
+  if (batch == 1) return cudaSuccess;
+  Img proto = P1.I.one;
+  proto.aligned = proto.aligned && (stride % 4 == 0);
+  P->I.one = proto;
+  P->I.d = table;
+  stack_table_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, s>>>(proto, (int)batch, stride, P1.t, table);
+  return cudaGetLastError();
+}
+
+}  // namespace
+}  // namespace nsgb
+
+extern "C" {
+
+size_t nsgb_recon_f32_workspace_size(int64_t batch, int64_t rows, int64_t cols, int backward) {
+  if (!f32_dims_ok(batch, rows, cols, cols * 4, rows * cols * 4)) return 0;
+  return backward ? f32_bwd_bytes(batch, rows, cols) : f32_fwd_bytes(batch, rows, cols);
+}
+
+nsgb_status nsgb_recon_f32_fwd(const float* marker, const float* mask, float* out, int32_t* prov, int64_t batch,
+                               int64_t rows, int64_t cols, int64_t pitch, int64_t image_stride, int conn, void* ws,
+                               size_t ws_bytes, nsgb_stream_t stream, const nsgb_opts* opts) {
+  if (!marker || !mask || !out || !prov || (const void*)out == (const void*)marker || !valid_conn(conn) ||
+      !f32_dims_ok(batch, rows, cols, pitch, image_stride))
+    return NSGB_ERR_BAD_ARG;
+  nsgb_status st = check_ws_bytes(ws, ws_bytes, f32_fwd_bytes(batch, rows, cols));
+  if (st != NSGB_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const Plan P1 = single_plan(NSGB_F32, out, mask, rows, cols, pitch);
+  const Ws w = carve(ws, stacked_totals(P1.t, batch));
+  Plan P;
+  cudaError_t e = stacked_plan(out, mask, batch, rows, cols, pitch, image_stride, w.table, &P, s);
+  // out = marker, image by image (one 2-D copy when the stack is contiguous)
+  const bool dense = batch == 1 || image_stride == rows * pitch;
+  for (int64_t b = 0; e == cudaSuccess && b < (dense ? 1 : batch); ++b)
+    e = cudaMemcpy2DAsync((char*)out + b * image_stride, pitch, (const char*)marker + b * image_stride, pitch,
+                          (size_t)cols * 4, (size_t)(dense ? rows * batch : rows), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = recon_timed(opts, NSGB_F32, P, conn, false, true, w.recon, s);
+  if (e == cudaSuccess) e = ccl::label(ClsPlateau{}, P.I, P.t, conn, w.forest(false), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.A, 0x7F, sizeof(int) * (size_t)P.t.px, s);
+  if (e == cudaSuccess) {
+    const int64_t moff = (int64_t)((uintptr_t)marker - (uintptr_t)out);
+    const int64_t poff = (int64_t)((uintptr_t)prov - (uintptr_t)out);
+    source_best_kernel<<<rcb(P.t), 256, 0, s>>>(P.I, P.t.rows, moff, w.L, w.A);
+    prov_out_kernel<<<rcb(P.t), 256, 0, s>>>(P.I, P.t.rows, w.L, w.A, poff, w.status);
+    e = cudaGetLastError();
+  }
+  return finish(e, ws, s, opts);
+}
+
+nsgb_status nsgb_recon_f32_bwd(const float* grad_out, const int32_t* prov, float* grad_marker, float* grad_mask,
+                               int64_t batch, int64_t rows, int64_t cols, int64_t pitch, int64_t image_stride,
+                               void* ws, size_t ws_bytes, nsgb_stream_t stream, const nsgb_opts* opts) {
+  if (!grad_out || !prov || !grad_marker || !grad_mask || !f32_dims_ok(batch, rows, cols, pitch, image_stride))
+    return NSGB_ERR_BAD_ARG;
+  nsgb_status st = check_ws_bytes(ws, ws_bytes, f32_bwd_bytes(batch, rows, cols));
+  if (st != NSGB_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t px = (size_t)(batch * rows * cols);
+  char* p = (char*)ws;
+  int* status = (int*)p;
+  auto* am = (unsigned long long*)(p + 256);
+  auto* ak = (unsigned long long*)(p + 256 + align256(8 * px));
+  Img* table = batch > 1 ? (Img*)(p + 256 + 2 * align256(8 * px)) : nullptr;
+  Plan P;
+  cudaError_t e = cudaMemsetAsync(status, 0, sizeof(int), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(am, 0, 2 * align256(8 * px), s);
+  if (e == cudaSuccess) e = stacked_plan((void*)grad_out, prov, batch, rows, cols, pitch, image_stride, table, &P, s);
+  if (e == cudaSuccess) {
+    grad_scatter_kernel<<<rcb(P.t), 256, 0, s>>>(P.I, P.t.rows, am, ak, status);
+    const int64_t dmo = (int64_t)((uintptr_t)grad_marker - (uintptr_t)grad_out);
+    const int64_t dko = (int64_t)((uintptr_t)grad_mask - (uintptr_t)grad_out);
+    grad_out_kernel<<<rcb(P.t), 256, 0, s>>>(P.I, P.t.rows, (const long long*)am, (const long long*)ak, dmo, dko);
+    e = cudaGetLastError();
+  }
+  return finish(e, ws, s, opts);
+}
+
+}  // extern "C"

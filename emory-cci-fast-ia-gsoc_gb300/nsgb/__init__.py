@@ -24,7 +24,7 @@ from ._ffi import NsgbError, lib
 __all__ = [
     "imreconstruct", "imreconstructBinary", "imfillHoles", "imhmin", "bwselect", "bwlabel", "bwlabel2",
     "bwareaopen2", "threshold", "invert", "chain", "imreconstructQueueThroughput", "chain_batch", "BatchPlan",
-    "NsgbError", "workspace",
+    "recon_f32", "recon_f32_backward", "NsgbError", "workspace",
 ]
 
 _DT = {torch.uint8: _ffi.U8, torch.int32: _ffi.I32, torch.float32: _ffi.F32}
@@ -366,3 +366,60 @@ def chain_batch(markers, masks, recon_conn=8, thr=128.0, fill_conn=4, label_conn
     nl, nk = plan.chain(recon_conn, thr, fill_conn, label_conn, area_min, area_max)
     return [{"recon": recon[i], "fill": plan.fill[i], "labels": plan.labels[i], "area": plan.area[i],
              "n_labels": nl[i], "n_kept": nk[i]} for i in range(plan.n)]
+
+
+def _stack3(t: torch.Tensor, name: str) -> torch.Tensor:
+    if t.dtype != torch.float32 or not t.is_cuda or t.dim() not in (2, 3):
+        raise NsgbError(1, f"{name}: need a float32 CUDA tensor [H, W] or [B, H, W]")
+    t = _contig(t)
+    return t if t.dim() == 3 else t.unsqueeze(0)
+
+
+_f32_ws = {}
+
+
+def _f32_workspace(B, H, W, backward, dev):
+    need = lib.nsgb_recon_f32_workspace_size(B, H, W, 1 if backward else 0)
+    if need == 0:
+        raise NsgbError(1, "recon_f32: image stack too large")
+    key = (dev.index, bool(backward))
+    buf = _f32_ws.get(key)
+    if buf is None or buf.numel() < need + 256:
+        buf = torch.empty(need + 256, dtype=torch.uint8, device=dev)
+        _f32_ws[key] = buf
+    return (buf.data_ptr() + 255) & ~255, need
+
+
+def recon_f32(marker: torch.Tensor, mask: torch.Tensor, connectivity: int = 8):
+    """Float32 reconstruction by dilation with its provenance map (no counterpart in the
+    reference).  Returns (out, prov) shaped like the inputs; prov = q (marker q), ~q (mask q)
+    or INT32_MIN (the zero ring), q = y * W + x."""
+    squeeze = marker.dim() == 2
+    mk, ms = _stack3(marker, "marker"), _stack3(mask, "mask")
+    _same_shape(mk, ms, "recon_f32")
+    B, H, W = ms.shape
+    out = torch.empty_like(ms)
+    prov = torch.empty(ms.shape, dtype=torch.int32, device=ms.device)
+    ws, nb = _f32_workspace(B, H, W, False, ms.device)
+    st = lib.nsgb_recon_f32_fwd(mk.data_ptr(), ms.data_ptr(), out.data_ptr(), prov.data_ptr(), B, H, W, W * 4,
+                                H * W * 4, connectivity, ws, nb, _stream(), None)
+    _ffi.check(st, "recon_f32_fwd")
+    return (out[0], prov[0]) if squeeze else (out, prov)
+
+
+def recon_f32_backward(grad: torch.Tensor, prov: torch.Tensor):
+    """Adjoint of recon_f32: (d/dmarker, d/dmask) of sum(grad * out), with exact 32.32
+    fixed-point sums."""
+    squeeze = grad.dim() == 2
+    g = _stack3(grad, "grad")
+    p = _contig(prov).view(g.shape)
+    if p.dtype != torch.int32:
+        raise NsgbError(1, "recon_f32_backward: prov must be int32")
+    B, H, W = g.shape
+    dm = torch.empty_like(g)
+    dk = torch.empty_like(g)
+    ws, nb = _f32_workspace(B, H, W, True, g.device)
+    st = lib.nsgb_recon_f32_bwd(g.data_ptr(), p.data_ptr(), dm.data_ptr(), dk.data_ptr(), B, H, W, W * 4,
+                                H * W * 4, ws, nb, _stream(), None)
+    _ffi.check(st, "recon_f32_bwd")
+    return (dm[0], dk[0]) if squeeze else (dm, dk)

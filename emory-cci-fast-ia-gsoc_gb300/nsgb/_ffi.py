@@ -84,6 +84,11 @@ _SIGS = {
                                 _optp]),
     "nsgb_batch_counts_async": (_int, [C.POINTER(Batch), _vp, _vp]),
     "nsgb_imreconstruct_batch": (_int, [C.POINTER(Batch), _int, _int, _vp, _optp]),
+    "nsgb_recon_f32_workspace_size": (_sz, [C.c_int64, C.c_int64, C.c_int64, _int]),
+    "nsgb_recon_f32_fwd": (_int, [_vp, _vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int64, _int,
+                                  _vp, _sz, _vp, _optp]),
+    "nsgb_recon_f32_bwd": (_int, [_vp, _vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                  _vp, _sz, _vp, _optp]),
     "nsgb_synth_tile_u8": (_int, [_vp, _vp, _i64, _i64, _i64, _i64, C.c_uint64]),
     "nsgb_synth_scale_u16": (_int, [_vp, _vp, _vp, _i64]),
     "nsgb_synth_scale_i32": (_int, [_vp, _vp, _vp, _i64]),

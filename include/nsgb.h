@@ -239,6 +239,33 @@ nsgb_status nsgb_imreconstruct_noalloc(int dtype, void* marker, const void* mask
                                        int64_t cols, int64_t pitch, int conn, int erode,
                                        nsgb_stream_t stream, const nsgb_opts* opts);
 
+/* ---------------------------------------------------------------------------------------
+ * Differentiable float32 reconstruction by dilation.  No counterpart in the reference (its
+ * imreconstruct<float>, MorphologicOperations.cpp:665-838 / imreconstructFloatCaller, has no
+ * gradient).  Works on `batch` equally sized images stacked `image_stride` bytes apart; all
+ * planes (marker, mask, out, prov, gradients) share rows, cols, pitch and image_stride.
+ *
+ * Forward: out = imreconstruct(marker, mask, conn) (the reference's float semantics,
+ * including its zero ring) and prov = the source of each output value:
+ *   prov = q       out(p) is marker(q),    q = y * cols + x within the same image
+ *   prov = ~q      out(p) is mask(q)
+ *   prov = INT32_MIN   out(p) is the constant 0 of the zero ring (border pixels only)
+ * Ties (several sources with the value of one connected plateau of equal output) go to a mask
+ * source first, then a marker source, then the ring, and the smallest q among those.
+ * out must not alias marker.  NaN inputs give NSGB_ERR_BAD_ARG.
+ *
+ * Backward: grad_marker(q) = sum of grad_out(p) over prov(p) = q, grad_mask(q) = sum over
+ * prov(p) = ~q.  Each grad_out(p) is rounded to a multiple of 2^-32 and the sums are exact
+ * 64-bit integer sums (independent of order, so bit-reproducible); |grad_out| < 2^31.
+ * Out-of-range prov entries are skipped and reported as NSGB_ERR_BAD_ARG. */
+size_t nsgb_recon_f32_workspace_size(int64_t batch, int64_t rows, int64_t cols, int backward);
+nsgb_status nsgb_recon_f32_fwd(const float* marker, const float* mask, float* out, int32_t* prov, int64_t batch,
+                               int64_t rows, int64_t cols, int64_t pitch, int64_t image_stride, int conn, void* ws,
+                               size_t ws_bytes, nsgb_stream_t stream, const nsgb_opts* opts);
+nsgb_status nsgb_recon_f32_bwd(const float* grad_out, const int32_t* prov, float* grad_marker, float* grad_mask,
+                               int64_t batch, int64_t rows, int64_t cols, int64_t pitch, int64_t image_stride,
+                               void* ws, size_t ws_bytes, nsgb_stream_t stream, const nsgb_opts* opts);
+
 #ifdef __cplusplus
 }
 #endif

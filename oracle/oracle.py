@@ -45,6 +45,10 @@ def _load() -> C.CDLL:
     lib.orc_chain.restype = i32
     lib.orc_chain_replicas_seconds.argtypes = [vp, vp, i64, i64, C.c_int, C.c_int]
     lib.orc_chain_replicas_seconds.restype = C.c_double
+    lib.orc_recon_f32_prov.argtypes = [vp, vp, i64, i64, i64, C.c_int, vp, vp, C.c_int]
+    lib.orc_recon_f32_prov.restype = C.c_int
+    lib.orc_recon_f32_grad.argtypes = [vp, vp, i64, i64, i64, vp, vp, C.c_int]
+    lib.orc_recon_fd.argtypes = [vp, vp, vp, i64, i64, C.c_int, vp, i64, C.c_double, vp, vp, C.c_int]
     return lib
 
 
@@ -174,3 +178,50 @@ def ref_area_threshold_labeled(labels: np.ndarray, lo: int, hi: int):
     out = np.empty((H, W), np.int32)
     n = r.ref_cc_area_threshold_labeled(_p(labels), W, H, _p(out), -1, lo, hi)
     return out, int(n)
+
+
+# -- differentiable float32 reconstruction ------------------------------------------------
+def _stack(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a if a.ndim == 3 else a[None]
+
+
+def recon_f32_prov(marker: np.ndarray, mask: np.ndarray, conn: int, threads: int = 0):
+    """(R, prov) for one image or a stack [B, H, W] (prov: ~q mask source, q marker source,
+    INT32_MIN the zero ring)."""
+    squeeze = np.ndim(mask) == 2
+    mk, ms = _stack(marker), _stack(mask)
+    B, H, W = ms.shape
+    R = np.empty_like(ms)
+    prov = np.empty(ms.shape, np.int32)
+    rc = lib.orc_recon_f32_prov(_p(mk), _p(ms), B, H, W, conn, _p(R), _p(prov), threads or (os.cpu_count() or 1))
+    if rc != 0:
+        raise ValueError("a plateau without a source (NaN input?)")
+    return (R[0], prov[0]) if squeeze else (R, prov)
+
+
+def recon_f32_grad(g: np.ndarray, prov: np.ndarray, threads: int = 0):
+    """CPU reference gradient (dmarker, dmask): exact fixed-point (2^-32) sums."""
+    squeeze = np.ndim(g) == 2
+    gg = _stack(g)
+    pp = np.ascontiguousarray(prov, dtype=np.int32).reshape(gg.shape)
+    B, H, W = gg.shape
+    dm = np.empty_like(gg)
+    dk = np.empty_like(gg)
+    lib.orc_recon_f32_grad(_p(gg), _p(pp), B, H, W, _p(dm), _p(dk), threads or (os.cpu_count() or 1))
+    return (dm[0], dk[0]) if squeeze else (dm, dk)
+
+
+def recon_fd(marker, mask, g, conn, idx, h=1e-4, threads: int = 0):
+    """Central differences in float64 at the listed flat pixel indices.  Returns
+    (fd_marker, fd_mask, valid_marker, valid_mask)."""
+    mk = np.ascontiguousarray(marker, dtype=np.float32)
+    ms = np.ascontiguousarray(mask, dtype=np.float32)
+    gg = np.ascontiguousarray(g, dtype=np.float32)
+    ix = np.ascontiguousarray(idx, dtype=np.int64)
+    H, W = ms.shape
+    fd = np.empty(2 * len(ix), np.float64)
+    ok = np.empty(2 * len(ix), np.int32)
+    lib.orc_recon_fd(_p(mk), _p(ms), _p(gg), H, W, conn, _p(ix), len(ix), h, _p(fd), _p(ok),
+                     threads or (os.cpu_count() or 1))
+    return fd[0::2], fd[1::2], ok[0::2].astype(bool), ok[1::2].astype(bool)

@@ -3,6 +3,7 @@
 //
 // All images are dense row-major (pitch == width).  dtype codes: 0 = u8, 1 = u16,
 // 2 = i32, 3 = f32 (the same codes as the product's C ABI).
+#include <atomic>
 #include <chrono>
 #include <cstdint>
 #include <thread>
@@ -21,6 +22,19 @@ int dispatch(int dtype, F&& f) {
     case 3: f((float*)nullptr); return 0;
     default: return -1;
   }
+}
+
+// Runs f(0..n-1) on up to `threads` host threads.
+template <typename F>
+void parallel_for(int64_t n, int threads, F&& f) {
+  if (threads < 1) threads = 1;
+  std::atomic<int64_t> next{0};
+  std::vector<std::thread> pool;
+  for (int t = 0; t < threads && t < n; ++t)
+    pool.emplace_back([&] {
+      for (int64_t i = next++; i < n; i = next++) f(i);
+    });
+  for (auto& th : pool) th.join();
 }
 
 }  // namespace
@@ -142,6 +156,66 @@ double orc_chain_replicas_seconds(const uint8_t* marker, const uint8_t* mask, in
   for (auto& th : pool) th.join();
   auto t1 = std::chrono::steady_clock::now();
   return std::chrono::duration<double>(t1 - t0).count();
+}
+
+// Float32 reconstruction by dilation with provenance over a stack of `B` dense H x W images,
+// one host thread per image.  Returns 0, or -1 if a plateau had no source.
+int orc_recon_f32_prov(const float* marker, const float* mask, int64_t B, int64_t H, int64_t W, int conn,
+                       float* R, int32_t* prov, int threads) {
+  const int64_t n = H * W;
+  std::vector<int> bad((size_t)B, 0);
+  parallel_for(B, threads, [&](int64_t b) {
+    orc::imreconstruct<float>(marker + b * n, mask + b * n, H, W, conn, R + b * n);
+    bad[b] = !orc::recon_provenance<float>(marker + b * n, mask + b * n, R + b * n, H, W, conn, prov + b * n);
+  });
+  for (int v : bad)
+    if (v) return -1;
+  return 0;
+}
+
+// The CPU reference gradient (fixed-point sums, see recon_grad_fixed) over B stacked images.
+void orc_recon_f32_grad(const float* g, const int32_t* prov, int64_t B, int64_t H, int64_t W, float* dmarker,
+                        float* dmask, int threads) {
+  const int64_t n = H * W;
+  parallel_for(B, threads, [&](int64_t b) {
+    orc::recon_grad_fixed(g + b * n, prov + b * n, n, dmarker + b * n, dmask + b * n);
+  });
+}
+
+// Central finite differences of L = sum_p g(p) R(p) for one H x W float image, evaluated in
+// float64: for each listed pixel, marker (kind 0) and mask (kind 1) are moved by +-h and the
+// reconstruction recomputed in double.  fd = sum_p g(p) (R+(p) - R-(p)) / 2h.  valid = the
+// provenance map at x+h and at x-h equals the one at x (otherwise the function is not
+// locally linear there and the pixel is rejected).
+void orc_recon_fd(const float* marker, const float* mask, const float* g, int64_t H, int64_t W, int conn,
+                  const int64_t* idx, int64_t n_idx, double h, double* fd, int32_t* valid, int threads) {
+  const int64_t n = H * W;
+  std::vector<double> mk(marker, marker + n), ms(mask, mask + n), R0((size_t)n);
+  std::vector<int32_t> p0((size_t)n);
+  orc::imreconstruct<double>(mk.data(), ms.data(), H, W, conn, R0.data());
+  orc::recon_provenance<double>(mk.data(), ms.data(), R0.data(), H, W, conn, p0.data());
+  parallel_for(2 * n_idx, threads, [&](int64_t t) {
+    const int64_t i = idx[t / 2];
+    const int kind = (int)(t % 2);
+    std::vector<double> a = kind == 0 ? mk : ms;
+    const std::vector<double>& other = kind == 0 ? ms : mk;
+    std::vector<double> Rp((size_t)n), Rm((size_t)n);
+    std::vector<int32_t> pp((size_t)n), pm((size_t)n);
+    const double x0 = a[i];
+    a[i] = x0 + h;
+    const double* mkp = kind == 0 ? a.data() : other.data();
+    const double* msp = kind == 0 ? other.data() : a.data();
+    orc::imreconstruct<double>(mkp, msp, H, W, conn, Rp.data());
+    bool ok = orc::recon_provenance<double>(mkp, msp, Rp.data(), H, W, conn, pp.data());
+    a[i] = x0 - h;
+    orc::imreconstruct<double>(mkp, msp, H, W, conn, Rm.data());
+    ok = ok && orc::recon_provenance<double>(mkp, msp, Rm.data(), H, W, conn, pm.data());
+    double s = 0.0;
+    for (int64_t p = 0; p < n; ++p)
+      if (Rp[p] != Rm[p]) s += (double)g[p] * (Rp[p] - Rm[p]);
+    fd[t] = s / (2.0 * h);
+    valid[t] = ok && pp == p0 && pm == p0;
+  });
 }
 
 }  // extern "C"

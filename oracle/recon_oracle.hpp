@@ -19,6 +19,8 @@
 #pragma once
 
 #include <algorithm>
+#include <cmath>
+#include <climits>
 #include <cstdint>
 #include <cstring>
 #include <deque>
@@ -421,6 +423,88 @@ inline int32_t bwareaopen2(const void* image, bool labeled, bool flatten, int32_
 template <typename T>
 inline void threshold_gt(const T* in, int64_t n, double k, uint8_t* out) {
   for (int64_t i = 0; i < n; ++i) out[i] = (double)in[i] > k ? 255 : 0;
+}
+
+// ---------------------------------------------------------------------------------------
+// Differentiable float reconstruction (an extension: the reference has no gradient).
+//
+// The reconstruction R only ever copies input values, so every R(p) is the value of one
+// source: mask(q) (the mask clamped at q), marker(q) (q's marker survived), or the constant 0
+// of the zero ring that the reference pads around the image (MorphologicOperations.cpp:
+// 671-674; it can only win on a border pixel, as 0).  A source and every pixel that took its
+// value form one plateau: a connected set (same connectivity) of equal R.  The provenance of
+// p names the source of p's plateau, preferring a mask source, then a marker source, then the
+// ring, and the smallest raster index among equals:
+//   prov = ~q (mask source q), q (marker source q), INT32_MIN (ring).
+// Found here by a breadth-first flood of each plateau (the GPU uses union-find).  Returns
+// false if some plateau has no source (only possible with NaN inputs).
+template <typename T>
+bool recon_provenance(const T* marker, const T* mask, const T* R, int64_t H, int64_t W, int conn,
+                      int32_t* prov) {
+  const int64_t n = H * W;
+  std::vector<uint8_t> seen((size_t)n, 0);
+  std::vector<int64_t> comp;
+  std::vector<int64_t> stack;
+  for (int64_t s = 0; s < n; ++s) {
+    if (seen[s]) continue;
+    comp.clear();
+    stack.assign(1, s);
+    seen[s] = 1;
+    const T v = R[s];
+    int64_t best = INT64_MAX;
+    while (!stack.empty()) {
+      const int64_t i = stack.back();
+      stack.pop_back();
+      comp.push_back(i);
+      const int64_t y = i / W, x = i % W;
+      int64_t key = INT64_MAX;
+      if (R[i] == mask[i]) key = i;
+      else if (R[i] == marker[i]) key = n + i;
+      else if (R[i] == (T)0 && (y == 0 || y == H - 1 || x == 0 || x == W - 1)) key = 2 * n;
+      best = std::min(best, key);
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          if (!dy && !dx) continue;
+          if (conn == 4 && dy && dx) continue;
+          const int64_t yy = y + dy, xx = x + dx;
+          if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
+          const int64_t j = yy * W + xx;
+          if (!seen[j] && R[j] == v) {
+            seen[j] = 1;
+            stack.push_back(j);
+          }
+        }
+    }
+    int32_t pv;
+    if (best < n) pv = (int32_t)~best;
+    else if (best < 2 * n) pv = (int32_t)(best - n);
+    else if (best == 2 * n) pv = INT32_MIN;
+    else return false;
+    for (int64_t i : comp) prov[i] = pv;
+  }
+  return true;
+}
+
+// Adjoint of R with respect to marker and mask for an upstream gradient g:
+//   dmarker(q) = sum of g(p) over p with prov(p) = q,  dmask(q) = sum over prov(p) = ~q.
+// Each g(p) is rounded to the nearest multiple of 2^-32 (ties to even) and the sums are
+// exact 64-bit integer sums, so they do not depend on the order of summation; the result
+// is rounded to float.  |g| < 2^31 is required.
+inline void recon_grad_fixed(const float* g, const int32_t* prov, int64_t n, float* dmarker, float* dmask) {
+  std::vector<int64_t> am((size_t)n, 0), ak((size_t)n, 0);
+  for (int64_t p = 0; p < n; ++p) {
+    const int32_t v = prov[p];
+    if (v == INT32_MIN) continue;
+    const int64_t q = v >= 0 ? v : ~(int64_t)v;
+    if (q >= n) continue;
+    const int64_t f = (int64_t)std::nearbyint((double)g[p] * 4294967296.0);
+    if (v >= 0) am[q] += f;
+    else ak[q] += f;
+  }
+  for (int64_t q = 0; q < n; ++q) {
+    dmarker[q] = (float)((double)am[q] * 2.3283064365386962890625e-10);
+    dmask[q] = (float)((double)ak[q] * 2.3283064365386962890625e-10);
+  }
 }
 
 }  // namespace orc
