@@ -55,6 +55,9 @@ def parse_args():
     p.add_argument("--batch-steps", type=int, default=5)
     p.add_argument("--batch-dtypes", default="u8,u16,i32")
     p.add_argument("--no-batch", action="store_true")
+    p.add_argument("--no-grad", action="store_true")
+    p.add_argument("--no-large", action="store_true")
+    p.add_argument("--large-size", type=int, default=16384)
     return p.parse_args()
 
 
@@ -385,6 +388,10 @@ def run_nsgb(args):
         line["cpu_baseline"] = cpu_baseline_port(marker_h, mask_h)
     if not args.no_batch:
         line["batched"] = batched_section(args, dev)
+    if not args.no_grad:
+        line["differentiable"] = grad_section(dev)
+    if not args.no_large:
+        line["large"] = large_section(args, dev)
     if rank == 0:
         print(json.dumps(line))
     if dist:
@@ -584,6 +591,133 @@ def batched_section(args, dev):
         res[d] = run_batched(args, dev, tiles, d)
     if not args.no_cpu_baseline:
         res["cpu_tile_parallel"] = cpu_tile_parallel(tiles, 2 * (os.cpu_count() or 1))
+    return res
+
+
+# -- differentiable float32 reconstruction ----------------------------------------------------
+def event_ms(fn, steps, warmup, stream):
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(steps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def grad_section(dev, steps=5):
+    """16 x 2048 x 2048 float32: forward with provenance, adjoint of an N(0,1) upstream gradient."""
+    import numpy as np
+    import torch
+
+    from nsgb import _ffi, synth
+
+    lib = _ffi.lib
+    B, H, W = 16, 2048, 2048
+    mask_h, marker_h = synth.float_pair((B, H, W), 0)
+    g_h = np.random.default_rng(0).standard_normal((B, H, W)).astype(np.float32)
+    marker, mask, g = (torch.from_numpy(a).to(dev) for a in (marker_h, mask_h, g_h))
+    out = torch.empty_like(mask)
+    prov = torch.empty((B, H, W), dtype=torch.int32, device=dev)
+    dm, dk = torch.empty_like(mask), torch.empty_like(mask)
+    wsz = [lib.nsgb_recon_f32_workspace_size(B, H, W, k) for k in (0, 1)]
+    wst = [torch.empty(n + 256, dtype=torch.uint8, device=dev) for n in wsz]
+    ws = [(t.data_ptr() + 255) & ~255 for t in wst]
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    opts = _ffi.Opts(0, 0, 0)
+
+    def fwd():
+        _ffi.check(lib.nsgb_recon_f32_fwd(marker.data_ptr(), mask.data_ptr(), out.data_ptr(), prov.data_ptr(), B, H, W,
+                                          W * 4, H * W * 4, 8, ws[0], wsz[0], sp, C.byref(opts)), "recon_f32_fwd")
+
+    def bwd():
+        _ffi.check(lib.nsgb_recon_f32_bwd(g.data_ptr(), prov.data_ptr(), dm.data_ptr(), dk.data_ptr(), B, H, W, W * 4,
+                                          H * W * 4, ws[1], wsz[1], sp, C.byref(opts)), "recon_f32_bwd")
+
+    t_fwd = event_ms(fwd, steps, 3, stream)
+    t_bwd = event_ms(bwd, steps, 3, stream)
+    for w in ws:
+        st = lib.nsgb_device_status(C.c_void_p(w), sp)
+        if st != 0:
+            raise RuntimeError(f"recon_f32 device status {_ffi.STATUS.get(st, st)}")
+    px = B * H * W
+    return {"workload": "16 x 2048 x 2048 float32, mask U[0,1), marker = mask * U[0.5,1), 8-connected; "
+                        "upstream gradient N(0,1)",
+            "forward_ms": t_fwd, "backward_ms": t_bwd, "backward_over_forward": t_bwd / t_fwd,
+            "forward_mpix_s": px / 1e6 / (t_fwd / 1e3), "backward_mpix_s": px / 1e6 / (t_bwd / 1e3),
+            "forward_algorithmic_GBps": 16 * px / (t_fwd / 1e3) / 1e9,
+            "backward_algorithmic_GBps": 16 * px / (t_bwd / 1e3) / 1e9,
+            "bytes_per_px": "16 each way (fwd: marker, mask, out, prov; bwd: g, prov, dmarker, dmask)"}
+
+
+# -- large single image -------------------------------------------------------------------------
+def large_section(args, dev, steps=3):
+    """16384 x 16384 with ~102k ellipses: hole filling (reconstruction by erosion), threshold,
+    bwlabel (8-conn), per dtype and fill connectivity; per-stage algorithmic GB/s."""
+    import torch
+
+    from nsgb import _ffi, synth
+
+    lib = _ffi.lib
+    N = args.large_size
+    img8, _ = synth.tile_u8(N, N, int(round(N * N / 2621)), 0)
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    opts = _ffi.Opts(0, 0, 0)
+    binary = torch.empty((N, N), dtype=torch.uint8, device=dev)
+    labels = torch.empty((N, N), dtype=torch.int32, device=dev)
+    lws_n = lib.nsgb_workspace_size(_ffi.OP_BWLABEL, _ffi.U8, N, N)
+    lws_t = torch.empty(lws_n + 256, dtype=torch.uint8, device=dev)
+    lws = (lws_t.data_ptr() + 255) & ~255
+    res = {"workload": f"{N}x{N}, {int(round(N * N / 2621))} ellipses; imfillHoles (grayscale, reconstruction by "
+                       f"erosion), threshold > 128 x scale, bwlabel 8-conn relabel; device-resident",
+           "bytes_per_px": "fill 2*s (image read, result written), threshold s+1, bwlabel 5"}
+    peak, _ = read_peaks()
+    for dt in ("u8", "u16", "i32"):
+        img_h = img8 if dt == "u8" else synth.scale(img8, dt)[0]
+        code = {"u8": _ffi.U8, "u16": _ffi.U16, "i32": _ffi.I32}[dt]
+        esz = img_h.dtype.itemsize
+        img = torch.from_numpy(img_h).to(dev)
+        fill = torch.empty_like(img)
+        fws_n = lib.nsgb_workspace_size(_ffi.OP_FILL_HOLES, code, N, N)
+        fws_t = torch.empty(fws_n + 256, dtype=torch.uint8, device=dev)
+        fws = (fws_t.data_ptr() + 255) & ~255
+        thr = 128.0 * BATCH_SCALE[dt]
+        for conn in (4, 8):
+            def f_fill():
+                _ffi.check(lib.nsgb_imfill_holes(code, img.data_ptr(), fill.data_ptr(), N, N, N * esz, 0, conn, fws,
+                                                 fws_n, sp, C.byref(opts)), "imfill_holes")
+
+            def f_thr():
+                _ffi.check(lib.nsgb_threshold(code, fill.data_ptr(), binary.data_ptr(), N, N, N * esz, N, thr, sp),
+                           "threshold")
+
+            def f_lab():
+                _ffi.check(lib.nsgb_bwlabel(binary.data_ptr(), labels.data_ptr(), N, N, N, N * 4, 8, 1, None, lws,
+                                            lws_n, sp, C.byref(opts)), "bwlabel")
+
+            t_fill = event_ms(f_fill, steps, 3, stream)
+            t_thr = event_ms(f_thr, steps, 3, stream)
+            t_lab = event_ms(f_lab, steps, 3, stream)
+            for w in (fws, lws):
+                st = lib.nsgb_device_status(C.c_void_p(w), sp)
+                if st != 0:
+                    raise RuntimeError(f"large {dt}: device status {_ffi.STATUS.get(st, st)}")
+            px = N * N
+            gbs = {"fill": 2 * esz * px / (t_fill / 1e3) / 1e9, "threshold": (esz + 1) * px / (t_thr / 1e3) / 1e9,
+                   "bwlabel": 5 * px / (t_lab / 1e3) / 1e9}
+            res[f"{dt}_conn{conn}"] = {
+                "fill_ms": t_fill, "threshold_ms": t_thr, "bwlabel_ms": t_lab,
+                "chain_mpix_s": px / 1e6 / ((t_fill + t_thr + t_lab) / 1e3),
+                "GBps": gbs, "frac_of_hbm": {k: v / peak for k, v in gbs.items()}}
+        del img, fill, fws_t
+        torch.cuda.empty_cache()
     return res
 
 
