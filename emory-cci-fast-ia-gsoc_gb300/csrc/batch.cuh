@@ -51,6 +51,7 @@ struct RTileBase { __device__ int operator()(const Img& m) const { return m.r_ti
 struct CTileBase { __device__ int operator()(const Img& m) const { return m.c_tile_base; } };
 struct BlkBase { __device__ int operator()(const Img& m) const { return m.blk_base; } };
 struct RowBase { __device__ int operator()(const Img& m) const { return m.row_base; } };
+struct PxBase { __device__ int operator()(const Img& m) const { return m.px_base; } };
 
 // Totals of a batch, known on the host (grid sizes).
 struct BatchTotals {

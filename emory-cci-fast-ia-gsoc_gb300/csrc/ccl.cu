@@ -1,9 +1,10 @@
 // Root ranking for the raster-order relabel (ConnComponents::relabel, ConnComponents.cpp:
 // 89-118: roots numbered 1..n in raster order) and the kept-component count of the area
 // filter (areaThresholdLabeled, ConnComponents.cpp:205-239).  Replaces the reference GPU's
-// Thrust transform / inclusive_scan / sort passes (cuda/ccl_uf.cu:285-479, 684-794) with a
-// three-kernel count / scan / assign over 1024-pixel blocks; every image of a batch is ranked
-// on its own (one scan CTA per image).
+// Thrust transform / inclusive_scan / sort passes (cuda/ccl_uf.cu:285-479, 684-794): the
+// global roots are picked out of the list of local roots into a one-bit-per-pixel map, which
+// is counted per 1024-pixel block and scanned (one CTA per image); a root's rank is its
+// block's offset plus the set bits before it.  No pass reads the label plane.
 #include "ccl.cuh"
 
 namespace nsgb {
@@ -13,141 +14,150 @@ namespace {
 
 constexpr int kRankThreads = 256;
 
-__device__ __forceinline__ bool in_range(int a, int lo, int hi) { return a >= lo && a < hi; }
+// Bits of pixels p .. p+31 (the bitmap has a spare word at the end).
+__device__ __forceinline__ unsigned bits_at(const unsigned* bits, int p) {
+  const int w = p >> 5, sh = p & 31;
+  const unsigned lo = __ldcg(bits + w);
+  return sh ? __funnelshift_r(lo, __ldcg(bits + w + 1), sh) : lo;
+}
 
-// Pixel range [begin, end) of rank block b (global pixel indices).
-struct BlockRange {
-  int begin, end;
-};
-__device__ __forceinline__ BlockRange block_range(const Imgs& I, int b) {
+// Global roots among the local roots: set their bit, count them (and the kept ones) per image.
+__global__ void __launch_bounds__(kRankThreads) mark_roots(Imgs I, Forest f, int max_roots, int lo, int hi,
+                                                           unsigned* __restrict__ bits, int* __restrict__ counts) {
+  const int n = min(__ldcg(f.nroots), max_roots);
+  const int lane = threadIdx.x & 31;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const int k = base + threadIdx.x;
+    int img = -1;
+    bool keep = false;
+    if (k < n) {
+      const int lr = __ldcg(f.roots + k);
+      if (__ldcg(f.L + lr) == lr) {
+        atomicOr(bits + (lr >> 5), 1u << (lr & 31));
+        img = img_of(I, lr, PxBase());
+        if (f.A) {
+          const int a = __ldcg(f.A + lr);
+          keep = a >= lo && a < hi;
+        }
+      }
+    }
+    // one atomic per image present in the warp
+    const unsigned peers = __match_any_sync(NSGB_FULL, img);
+    const unsigned kept = __ballot_sync(NSGB_FULL, keep) & peers;
+    if (img >= 0 && (__ffs(peers) - 1) == lane) {
+      atomicAdd(counts + 2 * img, __popc(peers));
+      if (kept) atomicAdd(counts + 2 * img + 1, __popc(kept));
+    }
+  }
+}
+
+// Roots per 1024-pixel rank block (one warp per block), and per 32-pixel word of the block the
+// number of roots before it in the block (wpre[32 * b + j]).
+__global__ void __launch_bounds__(kRankThreads) count_blocks(Imgs I, int nblocks, const unsigned* __restrict__ bits,
+                                                             int* __restrict__ cnt, int* __restrict__ wpre) {
+  const int b = blockIdx.x * (kRankThreads / 32) + (threadIdx.x >> 5);
+  if (b >= nblocks) return;
+  const int lane = threadIdx.x & 31;
   const Img m = img_at(I, img_of(I, b, BlkBase()));
-  BlockRange r;
-  r.begin = m.px_base + (b - m.blk_base) * kBlockPx;
-  r.end = m.px_base + m.H * m.W;
-  return r;
+  const int begin = m.px_base + (b - m.blk_base) * kBlockPx;
+  const int end = min(begin + kBlockPx, m.px_base + m.H * m.W);
+  const int p = begin + 32 * lane;
+  int c = 0;
+  if (p < end) {
+    unsigned w = bits_at(bits, p);
+    if (end - p < 32) w &= (1u << (end - p)) - 1u;
+    c = __popc(w);
+  }
+  int x = c;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(NSGB_FULL, x, o);
+    if (lane >= o) x += y;
+  }
+  wpre[32 * b + lane] = x - c;
+  if (lane == 31) cnt[b] = x;
 }
 
-__global__ void __launch_bounds__(kRankThreads) count_roots(Imgs I, const int* __restrict__ L,
-                                                            const int* __restrict__ A, int lo, int hi,
-                                                            int* __restrict__ cnt, int* __restrict__ kept) {
-  __shared__ int s[2][kRankThreads / 32];
-  const BlockRange br = block_range(I, blockIdx.x);
-  int c = 0, k = 0;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const int i = br.begin + j * kRankThreads + threadIdx.x;
-    if (i < br.end && __ldcg(&L[i]) == i) {
-      ++c;
-      if (A && in_range(__ldcg(&A[i]), lo, hi)) ++k;
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    c += __shfl_down_sync(NSGB_FULL, c, o);
-    k += __shfl_down_sync(NSGB_FULL, k, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    s[0][threadIdx.x >> 5] = c;
-    s[1][threadIdx.x >> 5] = k;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int tc = 0, tk = 0;
-    for (int w = 0; w < kRankThreads / 32; ++w) {
-      tc += s[0][w];
-      tk += s[1][w];
-    }
-    cnt[blockIdx.x] = tc;
-    kept[blockIdx.x] = tk;
-  }
-}
-
-// One CTA per image: exclusive scan of the image's block counts in place; totals into
-// counts[2*i] (roots) and counts[2*i+1] (kept).
-__global__ void __launch_bounds__(1024) scan_counts(Imgs I, int* __restrict__ cnt, const int* __restrict__ kept,
-                                                    int* __restrict__ counts) {
-  __shared__ int s_warp[32];
-  __shared__ int s_carry;
-  __shared__ int s_kept[32];
+// One CTA per image: exclusive scan of the image's block counts in place.  The counts are
+// taken in passes of 8 x 1024 (coalesced, all loads of a pass in flight at once); thread t
+// holds elements j * 1024 + t of the pass.
+__global__ void __launch_bounds__(1024) scan_blocks(Imgs I, int* __restrict__ cnt) {
+  constexpr int J = 8;
+  __shared__ int s_tot[J][32];
+  __shared__ int s_chunk[J + 1];
   const Img m = img_at(I, blockIdx.x);
-  const int b0 = m.blk_base;
+  int* c = cnt + m.blk_base;
   const int nb = (m.H * m.W + kBlockPx - 1) / kBlockPx;
-  if (threadIdx.x == 0) s_carry = 0;
-  int ksum = 0;
-  __syncthreads();
-  for (int base = 0; base < nb; base += 1024) {
-    const int i = base + threadIdx.x;
-    const int v = i < nb ? cnt[b0 + i] : 0;
-    if (i < nb) ksum += kept[b0 + i];
-    int x = v;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(NSGB_FULL, x, o);
-      if ((threadIdx.x & 31) >= o) x += y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int carry = 0;
+  for (int base = 0; base < nb; base += J * 1024) {
+    int v[J], x[J];
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      const int b = base + j * 1024 + threadIdx.x;
+      v[j] = b < nb ? c[b] : 0;
     }
-    if ((threadIdx.x & 31) == 31) s_warp[threadIdx.x >> 5] = x;
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      x[j] = v[j];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(NSGB_FULL, x[j], o);
+        if (lane >= o) x[j] += y;
+      }
+      if (lane == 31) s_tot[j][warp] = x[j];
+    }
     __syncthreads();
-    if (threadIdx.x < 32) {
-      int w = s_warp[threadIdx.x];
+    if (warp < J) {  // warp j scans the warp totals of chunk j
+      int w = s_tot[warp][lane];
+#pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const int y = __shfl_up_sync(NSGB_FULL, w, o);
-        if (threadIdx.x >= o) w += y;
+        if (lane >= o) w += y;
       }
-      s_warp[threadIdx.x] = w;
+      s_tot[warp][lane] = w;  // inclusive over warps
     }
     __syncthreads();
-    const int warp_off = (threadIdx.x >> 5) ? s_warp[(threadIdx.x >> 5) - 1] : 0;
-    if (i < nb) cnt[b0 + i] = s_carry + warp_off + x - v;
+    if (threadIdx.x == 0) {
+      int run = carry;
+      for (int j = 0; j < J; ++j) {
+        s_chunk[j] = run;
+        run += s_tot[j][31];
+      }
+      s_chunk[J] = run;
+    }
     __syncthreads();
-    if (threadIdx.x == 1023) s_carry += warp_off + x;
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      const int b = base + j * 1024 + threadIdx.x;
+      if (b < nb) c[b] = s_chunk[j] + (warp ? s_tot[j][warp - 1] : 0) + x[j] - v[j];
+    }
+    carry = s_chunk[J];
     __syncthreads();
-  }
-  for (int o = 16; o > 0; o >>= 1) ksum += __shfl_down_sync(NSGB_FULL, ksum, o);
-  if ((threadIdx.x & 31) == 0) s_kept[threadIdx.x >> 5] = ksum;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int t = 0;
-    for (int w = 0; w < 32; ++w) t += s_kept[w];
-    counts[2 * blockIdx.x] = s_carry;
-    counts[2 * blockIdx.x + 1] = t;
   }
 }
 
-__global__ void __launch_bounds__(kRankThreads) assign_ranks(Imgs I, const int* __restrict__ L,
-                                                             const int* __restrict__ off, int* __restrict__ rank) {
-  __shared__ int s_warp[kRankThreads / 32 * 4];
-  const BlockRange br = block_range(I, blockIdx.x);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // Pixel order inside the block: j-major (j*256 + tid); warp w, chunk j covers
-  // [j*256 + 32w, j*256 + 32w + 32).  Rank order follows the raster index.
-  bool isroot[4];
-  int pre[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const int i = br.begin + j * kRankThreads + threadIdx.x;
-    isroot[j] = i < br.end && __ldcg(&L[i]) == i;
-    const unsigned b = __ballot_sync(NSGB_FULL, isroot[j]);
-    pre[j] = __popc(b & ((1u << lane) - 1u));
-    if (lane == 0) s_warp[j * (kRankThreads / 32) + warp] = __popc(b);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int run = 0;
-    for (int t = 0; t < 4 * (kRankThreads / 32); ++t) {
-      const int c = s_warp[t];
-      s_warp[t] = run;
-      run += c;
-    }
-  }
-  __syncthreads();
-  const int o = off[blockIdx.x];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    if (!isroot[j]) continue;
-    const int i = br.begin + j * kRankThreads + threadIdx.x;
-    rank[i] = o + s_warp[j * (kRankThreads / 32) + warp] + pre[j];
+__global__ void __launch_bounds__(kRankThreads) assign_ranks(Imgs I, Forest f, int max_roots,
+                                                             const unsigned* __restrict__ bits,
+                                                             const int* __restrict__ off, const int* __restrict__ wpre,
+                                                             int* __restrict__ rank) {
+  const int n = min(__ldcg(f.nroots), max_roots);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int r = __ldcg(f.roots + k);
+    if (__ldcg(f.L + r) != r) continue;
+    const Img m = img_at(I, img_of(I, r, PxBase()));
+    const int local = r - m.px_base;
+    const int b = m.blk_base + local / kBlockPx;
+    const int j = (local % kBlockPx) >> 5;
+    const int p = m.px_base + (local / kBlockPx) * kBlockPx + 32 * j;
+    int c = __ldcg(off + b) + __ldcg(wpre + 32 * b + j);
+    if (r > p) c += __popc(bits_at(bits, p) & ((1u << (r - p)) - 1u));
+    rank[r] = c;
   }
 }
 
 }  // namespace
+
+int list_grid() { return 2 * 152; }
 
 int flat_grid(int64_t n) {
   int64_t b = (n + 255) / 256;
@@ -156,13 +166,17 @@ int flat_grid(int64_t n) {
   return (int)b;
 }
 
-cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const int* L, const int* A, int lo, int hi, int* rank,
-                       int* block_tmp, int* counts, cudaStream_t s) {
-  int* cnt = block_tmp;
-  int* kept = block_tmp + t.blocks;
-  count_roots<<<t.blocks, kRankThreads, 0, s>>>(I, L, A, lo, hi, cnt, kept);
-  scan_counts<<<t.n, 1024, 0, s>>>(I, cnt, kept, counts);
-  assign_ranks<<<t.blocks, kRankThreads, 0, s>>>(I, L, cnt, rank);
+cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, int* rank,
+                       unsigned* bits, size_t bits_bytes, int* block_tmp, int* wpre, int* counts, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(bits, 0, bits_bytes, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, sizeof(int) * 2 * (size_t)t.n, s);
+  if (e != cudaSuccess) return e;
+  const int g = list_grid();
+  mark_roots<<<g, kRankThreads, 0, s>>>(I, f, (int)t.px, lo, hi, bits, counts);
+  count_blocks<<<(t.blocks + kRankThreads / 32 - 1) / (kRankThreads / 32), kRankThreads, 0, s>>>(I, t.blocks, bits,
+                                                                                                  block_tmp, wpre);
+  scan_blocks<<<t.n, 1024, 0, s>>>(I, block_tmp);
+  assign_ranks<<<g, kRankThreads, 0, s>>>(I, f, (int)t.px, bits, block_tmp, wpre, rank);
   return cudaGetLastError();
 }
 

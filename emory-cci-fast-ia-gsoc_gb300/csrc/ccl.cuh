@@ -113,6 +113,13 @@ __device__ __forceinline__ int root_of(const int* L, int64_t i) {
   return l < 0 ? -1 : __ldcg(L + l);
 }
 
+// The same, for kernels that do not write L: the second load goes through L1, where the
+// pixels of one run (and of one component in a tile) find their shared root.
+__device__ __forceinline__ int root_of_ro(const int* L, int64_t i) {
+  const int l = __ldg(L + i);
+  return l < 0 ? -1 : __ldg(L + l);
+}
+
 // Labelling tile of CTA `b`: image, tile origin.
 struct TileAt {
   Img m;
@@ -312,6 +319,34 @@ __device__ __forceinline__ void for_batch_pixels(const Imgs& I, int total_rows, 
   }
 }
 
+// The same with four consecutive pixels per thread: f(image, y, x, n) for pixels x .. x+n-1
+// (n <= 4) of row y; x grid over max_w / 4.
+template <class F>
+__device__ __forceinline__ void for_batch_quads(const Imgs& I, int total_rows, F&& f) {
+  const int x = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+  for (int gr = blockIdx.y; gr < total_rows; gr += gridDim.y) {
+    const Img m = img_at(I, img_of(I, gr, RowBase()));
+    if (x < m.W) f(m, gr - m.row_base, x, min(4, m.W - x));
+  }
+}
+
+// Roots of four consecutive pixels (L read-only): one 16-byte load when aligned.
+__device__ __forceinline__ void roots4_ro(const int* L, int64_t i, int n, int (&r)[4]) {
+  int l[4];
+  if (n == 4 && ((i & 3) == 0)) {
+    const int4 v = __ldg((const int4*)(L + i));
+    l[0] = v.x, l[1] = v.y, l[2] = v.z, l[3] = v.w;
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) l[k] = k < n ? __ldg(L + i + k) : -1;
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) r[k] = l[k] < 0 ? -1 : (k > 0 && l[k] == l[k - 1] ? -2 : __ldg(L + l[k]));
+#pragma unroll
+  for (int k = 1; k < 4; ++k)
+    if (r[k] == -2) r[k] = r[k - 1];
+}
+
 // Seed pixels set bit root(p) in `bits`.
 template <class Seed>
 __global__ void ccl_seed_pixels(Imgs I, int total_rows, const int* __restrict__ L, Seed seed,
@@ -359,9 +394,14 @@ __device__ __forceinline__ bool test_bit(const unsigned* bits, int r) {
 
 // Host helpers (ccl.cu).
 int flat_grid(int64_t n);
+// Grid for kernels that walk a device-side list (length unknown on the host).
+int list_grid();
 // Row grids: x covers the widest image (256 columns per block), y strides the rows.
 inline dim3 rowcol_grid(int total_rows, int max_w) {
   return dim3((max_w + 255) / 256, (unsigned)(total_rows < 65535 ? total_rows : 65535));
+}
+inline dim3 quadrow_grid(int total_rows, int max_w) {
+  return dim3((max_w / 4 + 256) / 256, (unsigned)(total_rows < 65535 ? total_rows : 65535));
 }
 
 // Labels every image of the batch: local pass, edge merge, root flattening.  Afterwards
@@ -377,15 +417,17 @@ cudaError_t label(const Cls& cls, const Imgs& I, const BatchTotals& t, int conn,
     ccl_local<Cls, 4><<<t.c_tiles, kThreads, 0, s>>>(cls, I, f);
     ccl_merge<Cls, 4><<<t.c_tiles, 64, 0, s>>>(cls, I, f.L);
   }
-  ccl_flatten_roots<<<flat_grid(t.px / 4 + 1), 256, 0, s>>>(f, (int)t.px);
+  ccl_flatten_roots<<<list_grid(), 256, 0, s>>>(f, (int)t.px);
   return cudaGetLastError();
 }
 
-// Raster-order ranks of the roots: rank[r] = number of roots before r (only written at roots),
-// total roots and (if A) the number of roots whose area lies in [lo, hi) go to counts[0..1].
-// counts[2*i] / counts[2*i+1] for image i.  block_tmp: 2 ints per rank block.
-cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const int* L, const int* A, int lo, int hi, int* rank,
-                       int* block_tmp, int* counts, cudaStream_t s);
+// Raster-order ranks of the global roots, from the list of local roots: rank[r] = number of
+// roots of r's image before r (written at roots only).  counts[2*i] = roots of image i,
+// counts[2*i+1] = roots whose area (A, if given) lies in [lo, hi).  `bits` (one bit per
+// pixel, px/32 + 2 words), `block_tmp` (one int per rank block) and `wpre` (32 ints per rank
+// block) are scratch.
+cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, int* rank,
+                       unsigned* bits, size_t bits_bytes, int* block_tmp, int* wpre, int* counts, cudaStream_t s);
 constexpr int kBlockPx = 1024;
 
 }  // namespace ccl

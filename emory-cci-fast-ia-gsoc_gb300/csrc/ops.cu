@@ -8,7 +8,9 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <cmath>
 #include <limits>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/nsgb.h"
@@ -34,6 +36,34 @@ template <typename T>
 __device__ __forceinline__ T* pxp(void* base, int64_t pitch, int y, int x) {
   return (T*)((char*)base + (int64_t)y * pitch) + x;
 }
+
+// ------------------------------------------------------------------------------------------
+// `x > thr` with thr a double, as OpenCV's `Mat > k` compares (HistologicalEntities.cpp:214),
+// without double arithmetic on the device: for integer x it equals x > floor(thr), for float x
+// it equals x > (the largest float <= thr); both are prepared on the host.
+template <typename T>
+struct GtThr {
+  using K = std::conditional_t<std::is_floating_point<T>::value, float, int64_t>;
+  K k;
+  static GtThr make(double thr) {
+    GtThr g;
+    if constexpr (std::is_floating_point<T>::value) {
+      float f = (float)thr;
+      if ((double)f > thr) f = nextafterf(f, -INFINITY);
+      g.k = f;
+    } else {
+      if (thr != thr) g.k = INT64_MAX;  // NaN: nothing is greater
+      else if (thr >= 9.0e18) g.k = INT64_MAX;
+      else if (thr <= -9.0e18) g.k = INT64_MIN;
+      else g.k = (int64_t)floor(thr);
+    }
+    return g;
+  }
+  __device__ __forceinline__ bool operator()(T x) const {
+    if constexpr (std::is_floating_point<T>::value) return x > k;
+    else return (int64_t)x > k;
+  }
+};
 
 // ------------------------------------------------------------------------------------------
 // Classifiers (class 0 = background; equal non-zero classes are joined).  They read the
@@ -62,9 +92,9 @@ struct ClsNotMax {  // binary hole filling: pixels that are not foreground (max<
 };
 template <typename T>
 struct ClsNotAbove {  // hole filling of (R > thr): the complement class !(R > thr); R = plane
-  double thr;
+  GtThr<T> gt;
   __device__ uint32_t operator()(const Img& m, int y, int x) const {
-    return !((double)pxcg<T>(m.plane, m.pitch, y, x) > thr) ? 1u : 0u;
+    return gt(pxcg<T>(m.plane, m.pitch, y, x)) ? 0u : 1u;
   }
 };
 
@@ -90,19 +120,41 @@ struct SeedBoth {  // a != 0 and b != 0, with a = plane or aux as selected
 // Binary hole filling: 0 where the non-foreground pixel's component touches the border.
 // Writes the workspace plane F (dense, if given) and the caller's output (single image:
 // `out` / `pitch_out`; batch: Img::fill, dense).
+// Stores of four consecutive outputs (one vector store when aligned).
+__device__ __forceinline__ void store4_u8(uint8_t* p, int n, const uint8_t (&v)[4]) {
+  if (n == 4 && (((uintptr_t)p & 3) == 0)) {
+    *(uchar4*)p = make_uchar4(v[0], v[1], v[2], v[3]);
+  } else {
+    for (int k = 0; k < n; ++k) p[k] = v[k];
+  }
+}
+__device__ __forceinline__ void store4_i32(int32_t* p, int n, const int (&v)[4]) {
+  if (n == 4 && (((uintptr_t)p & 15) == 0)) {
+    *(int4*)p = make_int4(v[0], v[1], v[2], v[3]);
+  } else {
+    for (int k = 0; k < n; ++k) p[k] = v[k];
+  }
+}
+
 template <typename TO>
 __global__ void fill_out_kernel(Imgs I, int total_rows, const int* __restrict__ L, const unsigned* __restrict__ bits,
                                 uint8_t* F, TO* out, int64_t pitch_out, TO fg) {
-  ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
+  ccl::for_batch_quads(I, total_rows, [&](const Img& m, int y, int x, int n) {
     const int64_t gi = (int64_t)m.px_base + (int64_t)y * m.W + x;
-    const int r = ccl::root_of(L, gi);
-    const bool hole_free = r >= 0 && ccl::test_bit(bits, r);
-    const TO v = hole_free ? (TO)0 : fg;
-    if (F) F[gi] = (uint8_t)v;
-    if (!I.d) {
-      if (out) *pxp<TO>(out, pitch_out, y, x) = v;
-    } else if (m.fill) {
-      ((TO*)m.fill)[(int64_t)y * m.W + x] = v;
+    int r[4];
+    ccl::roots4_ro(L, gi, n, r);
+    uint8_t f[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) f[k] = (r[k] >= 0 && ccl::test_bit(bits, r[k])) ? 0 : (uint8_t)fg;
+    if (F) store4_u8(F + gi, n, f);
+    TO* o = nullptr;
+    if (!I.d) o = out ? pxp<TO>(out, pitch_out, y, x) : nullptr;
+    else if (m.fill) o = (TO*)m.fill + (int64_t)y * m.W + x;
+    if (!o) return;
+    if constexpr (sizeof(TO) == 1) {
+      store4_u8((uint8_t*)o, n, f);
+    } else {
+      for (int k = 0; k < n; ++k) o[k] = f[k] ? fg : (TO)0;
     }
   });
 }
@@ -114,7 +166,7 @@ __global__ void binrecon_out_kernel(Imgs I, int total_rows, const int* __restric
   ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
     T* p = pxp<T>(m.plane, m.pitch, y, x);
     if (*p != (T)0) return;
-    const int r = ccl::root_of(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
+    const int r = ccl::root_of_ro(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
     if (r >= 0 && ccl::test_bit(bits, r)) *p = std::numeric_limits<T>::max();
   });
 }
@@ -124,7 +176,7 @@ __global__ void bwselect_out_kernel(Imgs I, int total_rows, void* out, const int
                                     const unsigned* __restrict__ bits) {
   ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
     const T v = px<T>(m.plane, m.pitch, y, x);
-    const int r = ccl::root_of(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
+    const int r = ccl::root_of_ro(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
     *pxp<T>(out, m.pitch, y, x) = (v != (T)0 && r >= 0 && ccl::test_bit(bits, r)) ? v : (T)0;
   });
 }
@@ -136,22 +188,35 @@ __global__ void bwselect_out_kernel(Imgs I, int total_rows, void* out, const int
 __global__ void label_out_kernel(Imgs I, int total_rows, const int* __restrict__ L, const int* __restrict__ rank,
                                  int relabel, int32_t* labels, int64_t pitch_labels, const int* __restrict__ A, int lo,
                                  int hi, int32_t* kept_labels, int64_t pitch_kept, uint8_t* flat, int64_t pitch_flat) {
-  ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
-    const int r = ccl::root_of(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
-    const int lab = relabel ? (r < 0 ? 0 : __ldg(&rank[r]) + 1) : (r < 0 ? -1 : r - m.px_base);
-    bool keep = false;
-    if (A) {
-      const int a = r >= 0 ? __ldg(&A[r]) : 0;
-      keep = r >= 0 && a >= lo && a < hi;
+  ccl::for_batch_quads(I, total_rows, [&](const Img& m, int y, int x, int n) {
+    int r[4], lab[4], kl[4];
+    uint8_t fl[4];
+    ccl::roots4_ro(L, (int64_t)m.px_base + (int64_t)y * m.W + x, n, r);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const bool same = k > 0 && r[k] == r[k - 1];
+      lab[k] = same ? lab[k - 1]
+                    : (relabel ? (r[k] < 0 ? 0 : __ldg(&rank[r[k]]) + 1) : (r[k] < 0 ? -1 : r[k] - m.px_base));
+      bool keep = false;
+      if (A) {
+        if (same) {
+          keep = fl[k - 1] != 0;
+        } else {
+          const int a = r[k] >= 0 ? __ldg(&A[r[k]]) : 0;
+          keep = r[k] >= 0 && a >= lo && a < hi;
+        }
+      }
+      fl[k] = keep ? 255 : 0;
+      kl[k] = keep ? r[k] - m.px_base : -1;
     }
     if (!I.d) {
-      if (labels) *pxp<int32_t>(labels, pitch_labels, y, x) = lab;
-      if (A && kept_labels) *pxp<int32_t>(kept_labels, pitch_kept, y, x) = keep ? r - m.px_base : -1;
-      if (A && flat) *pxp<uint8_t>(flat, pitch_flat, y, x) = keep ? 255 : 0;
+      if (labels) store4_i32(pxp<int32_t>(labels, pitch_labels, y, x), n, lab);
+      if (A && kept_labels) store4_i32(pxp<int32_t>(kept_labels, pitch_kept, y, x), n, kl);
+      if (A && flat) store4_u8(pxp<uint8_t>(flat, pitch_flat, y, x), n, fl);
     } else {
       const int64_t li = (int64_t)y * m.W + x;
-      if (m.labels) m.labels[li] = lab;
-      if (A && m.area) m.area[li] = keep ? 255 : 0;
+      if (m.labels) store4_i32(m.labels + li, n, lab);
+      if (A && m.area) store4_u8(m.area + li, n, fl);
     }
   });
 }
@@ -200,9 +265,35 @@ __global__ void count_labels_in_range_kernel(const int* __restrict__ A, int64_t 
   for (int y = blockIdx.y; y < H; y += gridDim.y)
 
 template <typename T>
+struct alignas(4 * sizeof(T)) Vec4 {
+  T v[4];
+};
+
+// Four pixels per thread (x grid over W / 4); VEC: rows and bases allow one vector load and
+// one 32-bit store per thread.
+#define NSGB_FOR_QUADS                                        \
+  const int x = 4 * (blockIdx.x * blockDim.x + threadIdx.x);  \
+  if (x >= W) return;                                         \
+  for (int y = blockIdx.y; y < H; y += gridDim.y)
+
+template <typename T, bool VEC>
 __global__ void threshold_kernel(const T* in, int64_t pitch_in, uint8_t* out, int64_t pitch_out, int H, int W,
-                                 double thr) {
-  NSGB_FOR_PIXELS { *pxp<uint8_t>(out, pitch_out, y, x) = (double)px<T>(in, pitch_in, y, x) > thr ? 255 : 0; }
+                                 GtThr<T> gt) {
+  NSGB_FOR_QUADS {
+    const T* r = (const T*)((const char*)in + (int64_t)y * pitch_in) + x;
+    uint8_t* o = out + (int64_t)y * pitch_out + x;
+    if (VEC && x + 4 <= W) {
+      const Vec4<T> v = *(const Vec4<T>*)r;
+      uchar4 q;
+      q.x = gt(v.v[0]) ? 255 : 0;
+      q.y = gt(v.v[1]) ? 255 : 0;
+      q.z = gt(v.v[2]) ? 255 : 0;
+      q.w = gt(v.v[3]) ? 255 : 0;
+      *(uchar4*)o = q;
+    } else {
+      for (int k = 0; k < 4 && x + k < W; ++k) o[k] = gt(r[k]) ? 255 : 0;
+    }
+  }
 }
 
 template <typename T>
@@ -218,9 +309,24 @@ __device__ __forceinline__ T invert_value(T v) {
   }
 }
 
-template <typename T>
+template <typename T, bool VEC>
 __global__ void invert_kernel(const T* in, T* out, int64_t pitch, int H, int W) {
-  NSGB_FOR_PIXELS { *pxp<T>(out, pitch, y, x) = invert_value(px<T>(in, pitch, y, x)); }
+  NSGB_FOR_QUADS {
+    const T* r = (const T*)((const char*)in + (int64_t)y * pitch) + x;
+    T* o = (T*)((char*)out + (int64_t)y * pitch) + x;
+    if (VEC && x + 4 <= W) {
+      Vec4<T> v = *(const Vec4<T>*)r;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) v.v[k] = invert_value(v.v[k]);
+      *(Vec4<T>*)o = v;
+    } else {
+      for (int k = 0; k < 4 && x + k < W; ++k) o[k] = invert_value(r[k]);
+    }
+  }
+}
+
+inline dim3 quad_grid(int64_t rows, int64_t cols) {
+  return dim3((unsigned)((cols / 4 + 1 + 255) / 256), (unsigned)(rows < 65535 ? rows : 65535));
 }
 
 // Hole-filling marker: the image on the border, max<T> inside.
@@ -293,7 +399,7 @@ Plan single_plan(int dtype, void* plane, const void* aux, int64_t H, int64_t W, 
 }
 
 struct WsSizes {
-  size_t recon, L, A, R, bits, tmp, F, table, total;
+  size_t recon, L, A, R, roots, bits, tmp, wpre, F, table, total;
 };
 
 WsSizes ws_sizes(const BatchTotals& t) {
@@ -302,11 +408,13 @@ WsSizes ws_sizes(const BatchTotals& t) {
   z.L = align256(sizeof(int) * (size_t)t.px);
   z.A = z.L;
   z.R = z.L;
-  z.bits = align256(sizeof(unsigned) * (size_t)(t.px / 32 + 1));
+  z.roots = z.L;
+  z.bits = align256(sizeof(unsigned) * (size_t)(t.px / 32 + 2));
   z.tmp = align256(sizeof(int) * (size_t)(2 * (int64_t)t.blocks + 2 * (int64_t)t.n + 8));
+  z.wpre = align256(sizeof(int) * 32 * (size_t)t.blocks);
   z.F = align256((size_t)t.px);
   z.table = t.n > 1 ? align256(sizeof(Img) * (size_t)t.n) : 0;
-  z.total = z.recon + z.L + z.A + z.R + z.bits + z.tmp + z.F + z.table;
+  z.total = z.recon + z.L + z.A + z.R + z.roots + z.bits + z.tmp + z.wpre + z.F + z.table;
   return z;
 }
 
@@ -315,15 +423,17 @@ struct Ws {
   void* recon;
   int* L;
   int* A;
-  int* R;        // root ranks; before ranking, the list of local roots
+  int* R;        // root ranks (at roots)
+  int* roots;    // list of local roots
   unsigned* bits;
   int* tmp;      // 2 ints per rank block
   int* counts;   // 2 per image
   int* nroots;   // [1]
+  int* wpre;     // 32 per rank block
   uint8_t* F;
   Img* table;
   size_t bits_bytes;
-  ccl::Forest forest(bool areas) const { return ccl::Forest{L, areas ? A : nullptr, R, nroots}; }
+  ccl::Forest forest(bool areas) const { return ccl::Forest{L, areas ? A : nullptr, roots, nroots}; }
 };
 
 Ws carve(void* ws, const BatchTotals& t) {
@@ -339,13 +449,17 @@ Ws carve(void* ws, const BatchTotals& t) {
   p += z.A;
   w.R = (int*)p;
   p += z.R;
+  w.roots = (int*)p;
+  p += z.roots;
   w.bits = (unsigned*)p;
-  w.bits_bytes = sizeof(unsigned) * (size_t)(t.px / 32 + 1);
+  w.bits_bytes = sizeof(unsigned) * (size_t)(t.px / 32 + 2);
   p += z.bits;
   w.tmp = (int*)p;
   w.counts = w.tmp + 2 * (int64_t)t.blocks;
   w.nroots = w.counts + 2 * (int64_t)t.n;
   p += z.tmp;
+  w.wpre = (int*)p;
+  p += z.wpre;
   w.F = (uint8_t*)p;
   p += z.F;
   w.table = t.n > 1 ? (Img*)p : nullptr;
@@ -355,6 +469,8 @@ Ws carve(void* ws, const BatchTotals& t) {
 inline int grid1d(int64_t n) { return ccl::flat_grid(n); }
 inline dim3 rc(int64_t rows, int64_t cols) { return ccl::rowcol_grid((int)rows, (int)cols); }
 inline dim3 rcb(const BatchTotals& t) { return ccl::rowcol_grid(t.rows, t.max_w); }
+inline dim3 qr(int64_t rows, int64_t cols) { return ccl::quadrow_grid((int)rows, (int)cols); }
+inline dim3 qrb(const BatchTotals& t) { return ccl::quadrow_grid(t.rows, t.max_w); }
 
 // Records the caller's optional timing event around the reconstruction kernel.
 cudaError_t record(const nsgb_opts* o, bool begin, cudaStream_t s) {
@@ -372,6 +488,17 @@ cudaError_t recon_timed(const nsgb_opts* o, int dtype, const Plan& P, int conn, 
                          o ? o->max_visit_iters : 0);
   if (e != cudaSuccess) return e;
   return record(o, false, s);
+}
+
+template <typename F>
+void dispatch_all(int dtype, F&& f) {
+  switch (dtype) {
+    case NSGB_U8: f((uint8_t*)nullptr); break;
+    case NSGB_U16: f((uint16_t*)nullptr); break;
+    case NSGB_I32: f((int32_t*)nullptr); break;
+    case NSGB_F32: f((float*)nullptr); break;
+    default: break;
+  }
 }
 
 template <typename F>
@@ -396,22 +523,22 @@ cudaError_t chain_impl(int dtype, const Plan& P, const Ws& w, int recon_conn, do
   if (e == cudaSuccess) {
     e = dispatch_int(dtype, [&](auto* tag) -> cudaError_t {
       using T = std::remove_pointer_t<decltype(tag)>;
-      ClsNotAbove<T> cls{thr};
+      ClsNotAbove<T> cls{GtThr<T>::make(thr)};
       cudaError_t r = ccl::label(cls, P.I, t, fill_conn, w.forest(false), s);
       if (r != cudaSuccess) return r;
       const int gx = grid1d(t.perimeter_max) > 64 ? 64 : grid1d(t.perimeter_max);
       ccl::ccl_seed_border<SeedBorder<ClsNotAbove<T>>><<<dim3(gx, t.n), 256, 0, s>>>(
           P.I, w.L, SeedBorder<ClsNotAbove<T>>{cls}, w.bits);
-      fill_out_kernel<uint8_t><<<rcb(t), 256, 0, s>>>(P.I, t.rows, w.L, w.bits, w.F, fill_out,
+      fill_out_kernel<uint8_t><<<qrb(t), 256, 0, s>>>(P.I, t.rows, w.L, w.bits, w.F, fill_out,
                                                       P.I.d ? 0 : (int64_t)P.I.one.W, (uint8_t)255);
       return cudaGetLastError();
     });
   }
   if (e == cudaSuccess) e = ccl::label(ClsDenseU8{w.F}, P.I, t, label_conn, w.forest(true), s);
-  if (e == cudaSuccess) e = ccl::rank_roots(P.I, t, w.L, w.A, area_min, area_max, w.R, w.tmp, w.counts, s);
+  if (e == cudaSuccess) e = ccl::rank_roots(P.I, t, w.forest(true), area_min, area_max, w.R, w.bits, w.bits_bytes, w.tmp, w.wpre, w.counts, s);
   if (e == cudaSuccess) {
     const int64_t W1 = P.I.d ? 0 : P.I.one.W;
-    label_out_kernel<<<rcb(t), 256, 0, s>>>(P.I, t.rows, w.L, w.R, 1, labels_out, W1 * 4, w.A, area_min, area_max,
+    label_out_kernel<<<qrb(t), 256, 0, s>>>(P.I, t.rows, w.L, w.R, 1, labels_out, W1 * 4, w.A, area_min, area_max,
                                             nullptr, 0, area_out, W1);
     e = cudaGetLastError();
   }
@@ -574,7 +701,7 @@ nsgb_status nsgb_imfill_holes(int dtype, const void* image, void* out, int64_t r
         if (r != cudaSuccess) return r;
         ccl::ccl_seed_border<SeedBorder<ClsNotMax<T>>><<<dim3(grid1d(2 * (rows + cols)), 1), 256, 0, s>>>(
             P.I, w.L, SeedBorder<ClsNotMax<T>>{cls}, w.bits);
-        fill_out_kernel<T><<<rc(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.bits, nullptr, (T*)out, pitch,
+        fill_out_kernel<T><<<qr(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.bits, nullptr, (T*)out, pitch,
                                                           std::numeric_limits<T>::max());
         return cudaGetLastError();
       });
@@ -661,9 +788,9 @@ nsgb_status nsgb_bwlabel(const uint8_t* bin, int32_t* labels, int64_t rows, int6
   cudaError_t e = cudaMemsetAsync(w.status, 0, sizeof(int), s);
   if (e != cudaSuccess) return NSGB_ERR_CUDA;
   e = ccl::label(ClsValueU8{}, P.I, P.t, conn, w.forest(false), s);
-  if (e == cudaSuccess) e = ccl::rank_roots(P.I, P.t, w.L, nullptr, 0, 0, w.R, w.tmp, w.counts, s);
+  if (e == cudaSuccess) e = ccl::rank_roots(P.I, P.t, w.forest(false), 0, 0, w.R, w.bits, w.bits_bytes, w.tmp, w.wpre, w.counts, s);
   if (e == cudaSuccess) {
-    label_out_kernel<<<rc(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.R, relabel, labels, pitch_labels, nullptr,
+    label_out_kernel<<<qr(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.R, relabel, labels, pitch_labels, nullptr,
                                                      0, 0, nullptr, 0, nullptr, 0);
     e = cudaGetLastError();
   }
@@ -692,9 +819,9 @@ nsgb_status nsgb_bwareaopen(const void* in, int labeled, int32_t* labels_out, ui
   if (e != cudaSuccess) return NSGB_ERR_CUDA;
   if (!labeled) {
     e = ccl::label(ClsValueU8{}, P.I, P.t, conn, w.forest(true), s);
-    if (e == cudaSuccess) e = ccl::rank_roots(P.I, P.t, w.L, w.A, min_size, max_size, w.R, w.tmp, w.counts, s);
+    if (e == cudaSuccess) e = ccl::rank_roots(P.I, P.t, w.forest(true), min_size, max_size, w.R, w.bits, w.bits_bytes, w.tmp, w.wpre, w.counts, s);
     if (e == cudaSuccess) {
-      label_out_kernel<<<rc(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.R, 0, nullptr, 0, w.A, min_size, max_size,
+      label_out_kernel<<<qr(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.R, 0, nullptr, 0, w.A, min_size, max_size,
                                                        labels_out, pitch_labels, flat_out, pitch_flat);
       e = cudaGetLastError();
     }
@@ -728,12 +855,14 @@ nsgb_status nsgb_threshold(int dtype, const void* in, uint8_t* out, int64_t rows
     return NSGB_ERR_BAD_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   const int H = (int)rows, W = (int)cols;
-  switch (dtype) {
-    case NSGB_U8: threshold_kernel<uint8_t><<<rc(rows, cols), 256, 0, s>>>((const uint8_t*)in, pitch_in, out, pitch_out, H, W, thr); break;
-    case NSGB_U16: threshold_kernel<uint16_t><<<rc(rows, cols), 256, 0, s>>>((const uint16_t*)in, pitch_in, out, pitch_out, H, W, thr); break;
-    case NSGB_I32: threshold_kernel<int32_t><<<rc(rows, cols), 256, 0, s>>>((const int32_t*)in, pitch_in, out, pitch_out, H, W, thr); break;
-    case NSGB_F32: threshold_kernel<float><<<rc(rows, cols), 256, 0, s>>>((const float*)in, pitch_in, out, pitch_out, H, W, thr); break;
-  }
+  const bool vec = ((uintptr_t)in % (4 * esz)) == 0 && pitch_in % (4 * esz) == 0 && ((uintptr_t)out % 4) == 0 &&
+                   pitch_out % 4 == 0;
+  dispatch_all(dtype, [&](auto* tag) {
+    using T = std::remove_pointer_t<decltype(tag)>;
+    const GtThr<T> gt = GtThr<T>::make(thr);
+    if (vec) threshold_kernel<T, true><<<quad_grid(rows, cols), 256, 0, s>>>((const T*)in, pitch_in, out, pitch_out, H, W, gt);
+    else threshold_kernel<T, false><<<quad_grid(rows, cols), 256, 0, s>>>((const T*)in, pitch_in, out, pitch_out, H, W, gt);
+  });
   return cuda_status(cudaGetLastError());
 }
 
@@ -744,12 +873,12 @@ nsgb_status nsgb_invert(int dtype, const void* in, void* out, int64_t rows, int6
   if (!in || !out || !valid_dims(rows, cols) || !valid_pitch(pitch, cols, esz)) return NSGB_ERR_BAD_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   const int H = (int)rows, W = (int)cols;
-  switch (dtype) {
-    case NSGB_U8: invert_kernel<uint8_t><<<rc(rows, cols), 256, 0, s>>>((const uint8_t*)in, (uint8_t*)out, pitch, H, W); break;
-    case NSGB_U16: invert_kernel<uint16_t><<<rc(rows, cols), 256, 0, s>>>((const uint16_t*)in, (uint16_t*)out, pitch, H, W); break;
-    case NSGB_I32: invert_kernel<int32_t><<<rc(rows, cols), 256, 0, s>>>((const int32_t*)in, (int32_t*)out, pitch, H, W); break;
-    case NSGB_F32: invert_kernel<float><<<rc(rows, cols), 256, 0, s>>>((const float*)in, (float*)out, pitch, H, W); break;
-  }
+  const bool vec = ((uintptr_t)in % (4 * esz)) == 0 && ((uintptr_t)out % (4 * esz)) == 0 && pitch % (4 * esz) == 0;
+  dispatch_all(dtype, [&](auto* tag) {
+    using T = std::remove_pointer_t<decltype(tag)>;
+    if (vec) invert_kernel<T, true><<<quad_grid(rows, cols), 256, 0, s>>>((const T*)in, (T*)out, pitch, H, W);
+    else invert_kernel<T, false><<<quad_grid(rows, cols), 256, 0, s>>>((const T*)in, (T*)out, pitch, H, W);
+  });
   return cuda_status(cudaGetLastError());
 }
 
@@ -975,7 +1104,7 @@ __global__ void source_best_kernel(Imgs I, int total_rows, int64_t marker_off, c
 __global__ void prov_out_kernel(Imgs I, int total_rows, const int* __restrict__ L, const int* __restrict__ best,
                                 int64_t prov_off, int* status) {
   ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
-    const int r = ccl::root_of(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
+    const int r = ccl::root_of_ro(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
     const int key = __ldg(&best[r]);
     const int n = m.H * m.W;
     int32_t p;

@@ -64,6 +64,12 @@ enum TileState : int { kIdle = 0, kQueued = 1, kRunning = 2, kRunningDirty = 3 }
     if (lane == 0) atomicAdd(a.c.prof + (slot), (unsigned long long)(_now - _pt)); \
     _pt = _now;                                                                \
   } while (0)
+__device__ unsigned long long g_prof_times[1 << 20];  // per-visit start times (ns)
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 #else
 #define PROF_T0() \
   do {            \
@@ -623,14 +629,12 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   __threadfence();
   __syncwarp();
   PROF_MARK(5);
-  if (lane == 0 && dirs) {
-#pragma unroll
-    for (int d = 0; d < 9; ++d) {
-      if (!((dirs >> d) & 1u)) continue;
-      const int ny = ty + d / 3 - 1, nx = tx + d % 3 - 1;
-      if (ny < 0 || ny >= IMF(r_tiles_y) || nx < 0 || nx >= IMF(r_tiles_x)) continue;
+  // Lane d marks the neighbour in direction d (one copy of the marking code, up to eight
+  // neighbours marked in parallel).
+  if (lane < 9 && ((dirs >> lane) & 1u)) {
+    const int ny = ty + lane / 3 - 1, nx = tx + lane % 3 - 1;
+    if (ny >= 0 && ny < IMF(r_tiles_y) && nx >= 0 && nx < IMF(r_tiles_x))
       mark_tile(a.c, IMF(r_tile_base) + ny * IMF(r_tiles_x) + nx);
-    }
   }
   __syncwarp();
   PROF_MARK(6);
@@ -652,6 +656,12 @@ __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args a) {
     if (lane == 0) atomicAdd(a.c.prof + 0, (unsigned long long)(clock64() - _pp));
 #endif
     if (t < 0) break;
+#ifdef NSGB_RECON_PROFILE
+    if (lane == 0) {
+      const unsigned k = atomicAdd((unsigned*)&a.c.stats[4], 1u);
+      if (k < (1u << 20)) g_prof_times[k] = global_ns();
+    }
+#endif
     if (lane == 0) atomicExch(&a.c.state[t], kRunning);
     visit<T, CONN, BATCH>(a, B, t, lane);
 #ifdef NSGB_RECON_PROFILE
@@ -685,18 +695,23 @@ __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args a) {
 __device__ __forceinline__ int initial_tile(int i, int ntiles, int tiles_x, int order) {
   const int tiles_y = ntiles / tiles_x;
   if (order == 1) {
-    int even = 0;
-    for (int ty = 0; ty < tiles_y; ++ty) even += (tiles_x + ((ty & 1) ? 0 : 1)) / 2;
+    // tiles (ty, tx) with (ty + tx) even first, then the odd ones, each in raster order; row ty
+    // holds ceil(tiles_x / 2) of its first colour and floor(tiles_x / 2) of the other
+    const int hi = (tiles_x + 1) / 2, lo = tiles_x / 2;
+    const int even_total = ((tiles_y + 1) / 2) * hi + (tiles_y / 2) * lo;
     int k = i, parity = 0;
-    if (k >= even) {
-      k -= even;
+    if (k >= even_total) {
+      k -= even_total;
       parity = 1;
     }
-    int ty = 0;
-    for (;; ++ty) {
-      const int cnt = (tiles_x + (((ty & 1) ^ parity) ? 0 : 1)) / 2;
-      if (k < cnt) break;
-      k -= cnt;
+    // rows alternate between `a` tiles (ty even for parity 0) and `b` tiles
+    const int a = parity ? lo : hi, b = parity ? hi : lo;
+    const int pair = a + b;
+    int ty = pair ? 2 * (k / pair) : 0;
+    k = pair ? k % pair : k;
+    if (k >= a) {
+      k -= a;
+      ++ty;
     }
     const int first = ((ty & 1) ^ parity) ? 1 : 0;
     return ty * tiles_x + first + 2 * k;
@@ -888,3 +903,9 @@ cudaError_t recon_launch(int dtype, void* out, const void* marker, const void* m
 }
 
 }  // namespace nsgb
+
+#ifdef NSGB_RECON_PROFILE
+extern "C" int nsgb_prof_times(void* dst, int n) {
+  return (int)cudaMemcpyFromSymbol(dst, nsgb::g_prof_times, sizeof(unsigned long long) * (size_t)n);
+}
+#endif
