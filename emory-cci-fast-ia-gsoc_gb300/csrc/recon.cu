@@ -50,6 +50,7 @@ struct alignas(16) WarpBuf {
   uint32_t lv[36], rv[36];  // halo columns (values), index r + 1 for rows r = -1 .. 32
   uint32_t lm[36], rm[36];  // halo columns (masks)
   uint32_t c0[32], c1[32];  // final first / last tile column, for the neighbour test
+  uint32_t hl[32], hr[32];  // per row: what the halo columns give the first / last column
 };
 
 enum TileState : int { kIdle = 0, kQueued = 1, kRunning = 2, kRunningDirty = 3 };
@@ -172,6 +173,27 @@ __device__ __forceinline__ void store_word(T* base, int64_t pitch, int y, int x,
   }
 }
 
+// Interior-tile word access at a precomputed address (flip = xor with fx).
+template <typename T>
+__device__ __forceinline__ uint32_t fast_word(const char* p, bool coherent, uint32_t fx) {
+  if constexpr (sizeof(T) == 1) {
+    const unsigned short v = coherent ? __ldcg((const unsigned short*)p) : __ldg((const unsigned short*)p);
+    return __byte_perm((uint32_t)v, 0u, 0x7170) ^ fx;  // bytes b0,b1 -> 16-bit lanes
+  } else {
+    return (coherent ? __ldcg((const unsigned int*)p) : __ldg((const unsigned int*)p)) ^ fx;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void fast_store(char* p, uint32_t w, uint32_t fx) {
+  w ^= fx;
+  if constexpr (sizeof(T) == 1) {
+    __stcg((unsigned short*)p, (unsigned short)__byte_perm(w, 0u, 0x0020));
+  } else {
+    __stcg((unsigned int*)p, w);
+  }
+}
+
 // Initial value rule applied to every loaded value: min(v, mask), and on the image border
 // (signed / float dilation only) max with min(0, mask) -- the reference's 0-valued padding.
 template <typename T>
@@ -267,8 +289,8 @@ __device__ __forceinline__ uint32_t row_pass(uint32_t (&O)[32], const uint32_t* 
       lo2 = P::vmin(P::vmax(lo2, O[31 - j]), m2);
       hi2 = P::vmin(P::vmax(hi2, O[31 - j]), m2);
     }
-    const uint32_t carry_l = P::pack(B.lv[2 * q + 1], B.lv[2 * q + 2]);
-    const uint32_t carry_r = P::pack(B.rv[2 * q + 1], B.rv[2 * q + 2]);
+    const uint32_t carry_l = P::pack(B.hl[2 * q], B.hl[2 * q + 1]);
+    const uint32_t carry_r = P::pack(B.hr[2 * q], B.hr[2 * q + 1]);
     const uint32_t ex_l = P::vmin(P::vmax(carry_l, lo), hi);     // leaves the left half rightwards
     const uint32_t ex_r = P::vmin(P::vmax(carry_r, lo2), hi2);   // leaves the right half leftwards
     const uint32_t from0 = __shfl_up_sync(NSGB_FULL, ex_l, 16);
@@ -292,7 +314,7 @@ __device__ __forceinline__ uint32_t row_pass(uint32_t (&O)[32], const uint32_t* 
       v = n;
     }
   } else {
-    uint32_t v = B.lv[lane + 1];
+    uint32_t v = B.hl[lane];
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
       const uint32_t m = mh[lane * 33 + j];
@@ -301,7 +323,7 @@ __device__ __forceinline__ uint32_t row_pass(uint32_t (&O)[32], const uint32_t* 
       O[j] = n;
       v = n;
     }
-    v = B.rv[lane + 1];
+    v = B.hr[lane];
 #pragma unroll
     for (int j = 31; j >= 0; --j) {
       const uint32_t m = mh[lane * 33 + j];
@@ -315,7 +337,9 @@ __device__ __forceinline__ uint32_t row_pass(uint32_t (&O)[32], const uint32_t* 
 }
 
 // Column pass on the column layout: top-to-bottom then bottom-to-top, each step taking the
-// previous row's new values (and their left/right neighbours for 8-connectivity).
+// previous row's new values (and their left/right neighbours for 8-connectivity).  The halo
+// columns' contributions (diagonals and corners included) enter through the row pass's
+// carries, so the first and last lanes see nothing beyond the tile here.
 template <typename T, int CONN>
 __device__ __forceinline__ uint32_t col_pass(uint32_t (&O)[32], const WarpBuf& B, uint32_t top, uint32_t bot,
                                              int lane) {
@@ -328,8 +352,8 @@ __device__ __forceinline__ uint32_t col_pass(uint32_t (&O)[32], const WarpBuf& B
     if constexpr (CONN == 8) {
       uint32_t l = __shfl_up_sync(NSGB_FULL, up, 1);
       uint32_t r = __shfl_down_sync(NSGB_FULL, up, 1);
-      if (lane == 0) l = P::as_last(B.lv[i]);
-      if (lane == 31) r = P::as_first(B.rv[i]);
+      if (lane == 0) l = P::LOW;
+      if (lane == 31) r = P::LOW;
       a = P::vmax(a, P::vmax(P::from_left(l, up), P::from_right(up, r)));
     }
     const uint32_t m = B.mv[lane * 33 + i];
@@ -345,8 +369,8 @@ __device__ __forceinline__ uint32_t col_pass(uint32_t (&O)[32], const WarpBuf& B
     if constexpr (CONN == 8) {
       uint32_t l = __shfl_up_sync(NSGB_FULL, dn, 1);
       uint32_t r = __shfl_down_sync(NSGB_FULL, dn, 1);
-      if (lane == 0) l = P::as_last(B.lv[i + 2]);
-      if (lane == 31) r = P::as_first(B.rv[i + 2]);
+      if (lane == 0) l = P::LOW;
+      if (lane == 31) r = P::LOW;
       a = P::vmax(a, P::vmax(P::from_left(l, dn), P::from_right(dn, r)));
     }
     const uint32_t m = B.mv[lane * 33 + i];
@@ -452,15 +476,18 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   const bool interior = (y0 + kRows <= H) && (x0 + TW <= W);
   const bool fast = interior && IMF(aligned);
   const int xl = x0 + E * lane;
+  const uint32_t fx = flip ? P::FLIP : 0u;
 
   // All loads of the tile and its halo are issued before any is used, so the visit waits for
   // about one L2 round trip instead of a chain of them.
   uint32_t O[32], M[32];
-  if (fast) {  // interior tile: straight-line vector loads, no per-element checks
+  if (fast) {  // interior tile: straight-line loads through running row pointers, no checks
+    const char* mp = (const char*)mask + (int64_t)y0 * pitch + (int64_t)xl * sizeof(T);
+    const char* op = (const char*)src + (int64_t)y0 * pitch + (int64_t)xl * sizeof(T);
 #pragma unroll
-    for (int i = 0; i < 32; ++i) M[i] = load_word<T>(mask, pitch, y0 + i, xl, H, W, true, false, flip);
+    for (int i = 0; i < 32; ++i) M[i] = fast_word<T>(mp + i * pitch, false, fx);
 #pragma unroll
-    for (int i = 0; i < 32; ++i) O[i] = load_word<T>(src, pitch, y0 + i, xl, H, W, true, true, flip);
+    for (int i = 0; i < 32; ++i) O[i] = fast_word<T>(op + i * pitch, true, fx);
   } else {
     // Edge or unaligned tile: bounds-checked loads in a rolled loop through shared memory
     // (keeps this rarely used path out of the instruction cache's way).
@@ -518,6 +545,18 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
     }
   }
   __syncwarp();
+  // What the (constant) halo columns give each row's first / last pixel: the same-row halo
+  // pixel, and for 8-connectivity also the ones above and below (corners included).
+  {
+    uint32_t hl = B.lv[lane + 1], hr = B.rv[lane + 1];
+    if constexpr (CONN == 8) {
+      hl = P::emax(hl, P::emax(B.lv[lane], B.lv[lane + 2]));
+      hr = P::emax(hr, P::emax(B.rv[lane], B.rv[lane + 2]));
+    }
+    B.hl[lane] = hl;
+    B.hr[lane] = hr;
+  }
+  __syncwarp();
   // Mask in the row layout.
   if constexpr (E == 2) {
     const int q = lane & 15, half = lane >> 4;
@@ -558,8 +597,9 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   // Write the tile back, unless the visit changed nothing.
   if (__any_sync(NSGB_FULL, any_change != 0)) {
     if (fast) {
+      char* sp = (char*)out + (int64_t)y0 * pitch + (int64_t)xl * sizeof(T);
 #pragma unroll
-      for (int i = 0; i < 32; ++i) store_word<T>(out, pitch, y0 + i, xl, H, W, O[i], true, flip);
+      for (int i = 0; i < 32; ++i) fast_store<T>(sp + i * pitch, O[i], fx);
     } else {
 #pragma unroll
       for (int i = 0; i < 32; ++i) B.xp[lane * 33 + i] = O[i];
@@ -757,14 +797,17 @@ constexpr int kHdrInts = 64;
 template <typename T>
 int tiles_x_for(int64_t W) { return (int)((W + 32 * Px<T>::E - 1) / (32 * Px<T>::E)); }
 
-// Initial queue order (see initial_tile); NSGB_RECON_ORDER overrides it for experiments.
-inline int recon_order() {
-  static int order = -1;
-  if (order < 0) {
+// Initial queue order (see initial_tile): checkerboard for the 32 x 64 tiles of 8/16-bit
+// pixels, four colours for the 32 x 32 tiles of 32-bit pixels (measured best on the synthetic
+// tiles); NSGB_RECON_ORDER overrides it for experiments.
+inline int recon_order(int elems_per_word) {
+  static int order = -2;
+  if (order == -2) {
     const char* e = getenv("NSGB_RECON_ORDER");
-    order = (e && *e) ? atoi(e) : 1;
+    order = (e && *e) ? atoi(e) : -1;
   }
-  return order;
+  if (order >= 0) return order;
+  return elems_per_word == 2 ? 1 : 2;
 }
 
 inline unsigned ring_cap(int64_t ntiles) {
@@ -797,7 +840,7 @@ cudaError_t launch_typed(const Imgs& I, int ntiles, bool erode, bool ring, void*
 
   cudaError_t e = cudaMemsetAsync(wi, 0, sizeof(int) * kHdrInts, s);
   if (e != cudaSuccess) return e;
-  recon_init_kernel<<<(a.c.cap + 255) / 256, 256, 0, s>>>(a.c, I, ntiles, recon_order());
+  recon_init_kernel<<<(a.c.cap + 255) / 256, 256, 0, s>>>(a.c, I, ntiles, recon_order(Px<T>::E));
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
 
