@@ -146,7 +146,9 @@ struct class_type<Cls, std::void_t<typename Cls::class_t>> {
   using type = typename Cls::class_t;
 };
 
-// Each warp owns tile rows (lane = column).  Runs of equal class along a row are found with a
+// Each warp owns four consecutive tile rows (lane = column) and joins them top-down, so a
+// row's runs hook straight onto the root already found for the row above; only the four
+// warps' blocks meet concurrently, which keeps the trees (and every later find) shallow.  Runs of equal class along a row are found with a
 // ballot and start out joined (label = run start), so unions are only needed where runs of
 // adjacent rows touch: at a pixel that starts its run or sits under the start of a run above
 // (and, for 8-connectivity, diagonally past the two ends of the run).  That is one union per
@@ -164,7 +166,7 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
   CT c[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const int ly = ty + 8 * k, i = ly * kTile + tx;
+    const int ly = 4 * ty + k, i = ly * kTile + tx;
     const int gy = y0 + ly, gx = x0 + tx;
     c[k] = (CT)((gy < H && gx < W) ? cls(T.m, gy, gx) : 0u);
     s_c[i] = c[k];
@@ -173,7 +175,7 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
   unsigned same_left[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const int ly = ty + 8 * k, i = ly * kTile + tx;
+    const int ly = 4 * ty + k, i = ly * kTile + tx;
     const CT left = (CT)__shfl_up_sync(NSGB_FULL, (uint32_t)c[k], 1);
     same_left[k] = __ballot_sync(NSGB_FULL, tx > 0 && c[k] != 0 && left == c[k]);
     // run start: highest lane <= tx whose pixel does not continue a run from the left
@@ -184,7 +186,7 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const int ly = ty + 8 * k, i = ly * kTile + tx;
+    const int ly = 4 * ty + k, i = ly * kTile + tx;
     const CT v = c[k];
     if (!v || ly == 0) continue;
     const bool run_start = !((same_left[k] >> tx) & 1u);
@@ -202,7 +204,7 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
   int root[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const int ly = ty + 8 * k, i = ly * kTile + tx;
+    const int ly = 4 * ty + k, i = ly * kTile + tx;
     root[k] = c[k] ? s_find(s_lab, i) : -1;
   }
   if (f.A) {
@@ -216,7 +218,7 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
   }
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const int ly = ty + 8 * k, i = ly * kTile + tx;
+    const int ly = 4 * ty + k, i = ly * kTile + tx;
     const int gy = y0 + ly, gx = x0 + tx;
     const bool in = gy < H && gx < W;
     const int r = root[k];

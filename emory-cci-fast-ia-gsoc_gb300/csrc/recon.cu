@@ -97,6 +97,7 @@ struct Ctl {
   unsigned long long* prof;         // [8] phase cycle counters (profiling builds only)
   unsigned cap;       // ring capacity (power of two >= ntiles)
   long long max_visits;
+  int budget_step;
 };
 
 // Images of the batch: Img::plane is reconstructed in place (it holds the marker on entry),
@@ -427,21 +428,19 @@ __device__ __forceinline__ int queue_pop(const Ctl& c) {
   }
 }
 
-// A neighbour's values may have become stale: make sure it (re)reads them.
+// A neighbour's values may have become stale: make sure it (re)reads them.  The common case
+// (an idle neighbour) takes one atomic.
 __device__ __forceinline__ void mark_tile(const Ctl& c, int nt) {
-  int s = ld_relaxed(&c.state[nt]);
+  int s = atomicCAS(&c.state[nt], kIdle, kQueued);
   for (int guard = 0; guard < 1024; ++guard) {
-    if (s == kQueued || s == kRunningDirty) return;  // will load after our stores
-    const int want = (s == kIdle) ? kQueued : kRunningDirty;
-    const int old = atomicCAS(&c.state[nt], s, want);
-    if (old == s) {
-      if (want == kQueued) {
-        atomicAdd(c.pending, 1);
-        queue_push(c, nt);
-      }
+    if (s == kIdle) {  // this call queued it
+      atomicAdd(c.pending, 1);
+      queue_push(c, nt);
       return;
     }
-    s = old;
+    if (s == kQueued || s == kRunningDirty) return;  // will load after our stores
+    s = atomicCAS(&c.state[nt], kRunning, kRunningDirty);
+    if (s == kRunning) return;  // its owner re-runs it
   }
   set_status(c.status, kDevTimeout);
 }
@@ -466,11 +465,6 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   const int64_t pitch = IMF(pitch);
 
   PROF_T0();
-  // The caller has set the tile RUNNING; order that before reading the neighbours' pixels.
-  __syncwarp();
-  __threadfence();
-  PROF_MARK(1);
-
   const T* src = out;
   const bool coh = true;
   const bool interior = (y0 + kRows <= H) && (x0 + TW <= W);
@@ -478,14 +472,23 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   const int xl = x0 + E * lane;
   const uint32_t fx = flip ? P::FLIP : 0u;
 
-  // All loads of the tile and its halo are issued before any is used, so the visit waits for
-  // about one L2 round trip instead of a chain of them.
+  // The mask never changes: an interior tile's mask loads are issued before the fence below,
+  // so that their latency overlaps it.
   uint32_t O[32], M[32];
-  if (fast) {  // interior tile: straight-line loads through running row pointers, no checks
+  if (fast) {
     const char* mp = (const char*)mask + (int64_t)y0 * pitch + (int64_t)xl * sizeof(T);
-    const char* op = (const char*)src + (int64_t)y0 * pitch + (int64_t)xl * sizeof(T);
 #pragma unroll
     for (int i = 0; i < 32; ++i) M[i] = fast_word<T>(mp + i * pitch, false, fx);
+  }
+  // The caller has set the tile RUNNING; order that before reading the neighbours' pixels.
+  __syncwarp();
+  __threadfence();
+  PROF_MARK(1);
+
+  // All loads of the tile and its halo are issued before any is used, so the visit waits for
+  // about one L2 round trip instead of a chain of them.
+  if (fast) {  // interior tile: straight-line loads through running row pointers, no checks
+    const char* op = (const char*)src + (int64_t)y0 * pitch + (int64_t)xl * sizeof(T);
 #pragma unroll
     for (int i = 0; i < 32; ++i) O[i] = fast_word<T>(op + i * pitch, true, fx);
   } else {
@@ -573,12 +576,18 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   __syncwarp();
 
   PROF_MARK(2);
-  // Sweep to the local fixed point.
+  // Sweep to the local fixed point.  A row pass is idempotent (exact left / right scans); with
+  // 4-connectivity so is a column pass, so once a row pass after a column pass changes nothing
+  // the tile is stable and the final column pass can be skipped.  With 8-connectivity the
+  // diagonals make the column pass order-dependent and the loop ends on an unchanged column
+  // pass.
   int it = 0;
   for (;;) {
     col_to_row<E>(O, B.xp, lane);
-    any_change |= row_pass<T>(O, B.mh, B, lane);
+    const uint32_t racc = row_pass<T>(O, B.mh, B, lane);
+    any_change |= racc;
     row_to_col<E>(O, B.xp, lane);
+    if (CONN == 4 && it > 0 && !__any_sync(NSGB_FULL, racc != 0)) break;
     const uint32_t acc = col_pass<T, CONN>(O, B, topv, botv, lane);
     any_change |= acc;
     ++it;
@@ -685,6 +694,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   WarpBuf& B = reinterpret_cast<WarpBuf*>(smem_raw)[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
+  int visits_here = 0;
   for (;;) {
     int t = 0;
 #ifdef NSGB_RECON_PROFILE
@@ -717,8 +727,14 @@ __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args a) {
         atomicAdd(&a.c.stats[2], 1);
         queue_push(a.c, t);
       }
-      if (atomicAdd(a.c.visit_count, 1ull) >= (unsigned long long)a.c.max_visits)
-        set_status(a.c.status, kDevNotConverged);
+      // the visit budget is checked every `budget_step` visits of this warp (every visit
+      // when the caller set a budget, every 16 against the default one)
+      if (++visits_here == a.c.budget_step) {
+        if (atomicAdd(a.c.visit_count, (unsigned long long)visits_here) + (unsigned long long)visits_here >
+            (unsigned long long)a.c.max_visits)
+          set_status(a.c.status, kDevNotConverged);
+        visits_here = 0;
+      }
     }
     __syncwarp();
 #ifdef NSGB_RECON_PROFILE
@@ -837,6 +853,7 @@ cudaError_t launch_typed(const Imgs& I, int ntiles, bool erode, bool ring, void*
   a.c.cap = ring_cap(ntiles);
   a.c.slots = (Slot*)(a.c.state + ((ntiles + 1) & ~1));
   a.c.max_visits = (long long)(max_visits_per_tile > 0 ? max_visits_per_tile : 1 << 20) * ntiles;
+  a.c.budget_step = max_visits_per_tile > 0 ? 1 : 16;
 
   cudaError_t e = cudaMemsetAsync(wi, 0, sizeof(int) * kHdrInts, s);
   if (e != cudaSuccess) return e;

@@ -31,9 +31,23 @@
 #include "nsgb.h"
 
 #ifndef NSGB_USE_OPENCV
-namespace cv {
+// OpenCV's depth / type constants (macros at global scope, as OpenCV defines them; single
+// channel types equal their depth).
+#ifndef CV_8U
+#define CV_8U 0
+#define CV_8S 1
+#define CV_16U 2
+#define CV_16S 3
+#define CV_32S 4
+#define CV_32F 5
+#define CV_64F 6
+#define CV_8UC1 CV_8U
+#define CV_16UC1 CV_16U
+#define CV_32SC1 CV_32S
+#define CV_32FC1 CV_32F
+#endif
 
-enum { CV_8U = 0, CV_8S = 1, CV_16U = 2, CV_16S = 3, CV_32S = 4, CV_32F = 5, CV_64F = 6 };
+namespace cv {
 
 struct Exception : public std::runtime_error {
   int code;
@@ -173,10 +187,10 @@ namespace detail {
 
 template <typename T>
 struct DType;
-template <> struct DType<unsigned char> { static constexpr int code = NSGB_U8; static constexpr int cv = cv::CV_8U; };
-template <> struct DType<unsigned short> { static constexpr int code = NSGB_U16; static constexpr int cv = cv::CV_16U; };
-template <> struct DType<int> { static constexpr int code = NSGB_I32; static constexpr int cv = cv::CV_32S; };
-template <> struct DType<float> { static constexpr int code = NSGB_F32; static constexpr int cv = cv::CV_32F; };
+template <> struct DType<unsigned char> { static constexpr int code = NSGB_U8; static constexpr int cv = CV_8U; };
+template <> struct DType<unsigned short> { static constexpr int code = NSGB_U16; static constexpr int cv = CV_16U; };
+template <> struct DType<int> { static constexpr int code = NSGB_I32; static constexpr int cv = CV_32S; };
+template <> struct DType<float> { static constexpr int code = NSGB_F32; static constexpr int cv = CV_32F; };
 
 inline void check(nsgb_status st, const char* where) {
   if (st != NSGB_OK) throw cv::Exception(-(int)st, std::string(where) + ": " + nsgb_status_string(st));
@@ -208,7 +222,7 @@ using cv::gpu::GpuMat;
 using cv::gpu::Stream;
 
 // nscale::gpu::imreconstruct<T> (MorphologicOperations.h:102-119).  `iter` receives the
-// number of work-list rounds the reconstruction used (the reference reported scan iterations).
+// number of tile visits the reconstruction used (the reference reported scan iterations).
 template <typename T>
 GpuMat imreconstruct(const GpuMat& seeds, const GpuMat& image, int connectivity, Stream& stream, unsigned int& iter) {
   NSGB_CV_ASSERT(image.channels() == 1 && seeds.channels() == 1);
@@ -253,13 +267,31 @@ template <typename T>
 GpuMat imreconstructQ(const GpuMat& seeds, const GpuMat& image, int connectivity, Stream& stream) {
   return imreconstruct<T>(seeds, image, connectivity, stream);
 }
+// nscale::gpu::imreconstructQueueThroughput<T> (MorphologicOperationsGPU.cpp:447-545): all
+// images in one batched launch (nsgb_batch_prepare + nsgb_imreconstruct_batch).
 template <typename T>
 std::vector<GpuMat> imreconstructQueueThroughput(std::vector<GpuMat>& seeds, std::vector<GpuMat>& image,
                                                  int connectivity, int /*nItFirstPass*/, Stream& stream) {
   NSGB_CV_ASSERT(seeds.size() == image.size());
   std::vector<GpuMat> out;
+  if (seeds.empty()) return out;
+  std::vector<nsgb_tile> tiles(seeds.size());
   out.reserve(seeds.size());
-  for (size_t i = 0; i < seeds.size(); ++i) out.push_back(imreconstruct<T>(seeds[i], image[i], connectivity, stream));
+  for (size_t i = 0; i < seeds.size(); ++i) {
+    NSGB_CV_ASSERT(image[i].type() == detail::DType<T>::cv && seeds[i].type() == image[i].type());
+    NSGB_CV_ASSERT(image[i].rows == seeds[i].rows && image[i].cols == seeds[i].cols && image[i].step == seeds[i].step);
+    out.push_back(seeds[i].clone());
+    tiles[i] = nsgb_tile{out[i].data, image[i].data, image[i].rows, image[i].cols, (int64_t)image[i].step,
+                         nullptr, nullptr, nullptr};
+  }
+  const size_t nb = nsgb_batch_workspace_size(detail::DType<T>::code, tiles.data(), (int)tiles.size());
+  NSGB_CV_ASSERT(nb > 0);
+  nsgb_batch batch;
+  detail::check(nsgb_batch_prepare(detail::DType<T>::code, tiles.data(), (int)tiles.size(), detail::workspace(nb), nb,
+                                   &batch),
+                "imreconstructQueueThroughput");
+  detail::check(nsgb_imreconstruct_batch(&batch, connectivity, 0, detail::raw(stream), nullptr),
+                "imreconstructQueueThroughput");
   return out;
 }
 
@@ -313,8 +345,8 @@ GpuMat bwselect(const GpuMat& binaryImage, const GpuMat& seeds, int connectivity
 
 // nscale::gpu::bwlabel (MorphologicOperations.h:154).  int32 labels.
 inline GpuMat bwlabel(const GpuMat& binaryImage, int connectivity, bool relab, Stream& stream) {
-  NSGB_CV_ASSERT(binaryImage.channels() == 1 && binaryImage.type() == cv::CV_8U);
-  GpuMat out(binaryImage.rows, binaryImage.cols, cv::CV_32S);
+  NSGB_CV_ASSERT(binaryImage.channels() == 1 && binaryImage.type() == CV_8U);
+  GpuMat out(binaryImage.rows, binaryImage.cols, CV_32S);
   const size_t nb = nsgb_workspace_size(NSGB_OP_BWLABEL, NSGB_U8, binaryImage.rows, binaryImage.cols);
   detail::check(nsgb_bwlabel(binaryImage.data, (int32_t*)out.data, binaryImage.rows, binaryImage.cols,
                              (int64_t)binaryImage.step, (int64_t)out.step, connectivity, relab ? 1 : 0, nullptr,
@@ -327,8 +359,8 @@ inline GpuMat bwlabel(const GpuMat& binaryImage, int connectivity, bool relab, S
 inline GpuMat bwareaopen2(const GpuMat& binaryImage, bool labeled, bool flatten, int minSize, int maxSize,
                           int connectivity, int& count, Stream& stream) {
   NSGB_CV_ASSERT(binaryImage.channels() == 1);
-  NSGB_CV_ASSERT(binaryImage.type() == (labeled ? cv::CV_32S : cv::CV_8U));
-  GpuMat out(binaryImage.rows, binaryImage.cols, flatten ? cv::CV_8U : cv::CV_32S);
+  NSGB_CV_ASSERT(binaryImage.type() == (labeled ? CV_32S : CV_8U));
+  GpuMat out(binaryImage.rows, binaryImage.cols, flatten ? CV_8U : CV_32S);
   const size_t nb = nsgb_workspace_size(NSGB_OP_BWAREAOPEN, NSGB_U8, binaryImage.rows, binaryImage.cols);
   int32_t c = 0;
   detail::check(nsgb_bwareaopen(binaryImage.data, labeled ? 1 : 0, flatten ? nullptr : (int32_t*)out.data,

@@ -1,0 +1,37 @@
+"""The C++ API mirror run on the GPU: nscale::imreconstruct / imfillHoles / bwlabel2 /
+bwareaopen2 / imhmin and nscale::gpu::imreconstruct / imreconstructQueueThroughput give the
+oracle's results; a type mismatch raises cv::Exception."""
+import subprocess
+
+import numpy as np
+import pytest
+
+from cpp_api import build
+
+pytestmark = pytest.mark.gpu
+
+
+def test_cpp_api_matches_oracle(nsgb, oracle, tmp_path):
+    exe = tmp_path / "nscale_api_test"
+    build(str(exe))
+    r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    H, W = 300, 400
+
+    def load(name, dt):
+        return np.fromfile(tmp_path / name, dtype=dt).reshape(H, W)
+
+    mask, marker = load("mask.u8", np.uint8), load("marker.u8", np.uint8)
+    rec8 = oracle.imreconstruct(marker, mask, 8)
+    assert np.array_equal(load("recon8.u8", np.uint8), rec8)
+    assert np.array_equal(load("recon4.u8", np.uint8), oracle.imreconstruct(marker, mask, 4))
+    assert np.array_equal(load("batch0.u8", np.uint8), rec8)
+    assert np.array_equal(load("batch1.u8", np.uint8), rec8)
+    fill = oracle.imfill_holes(oracle.threshold_gt(rec8, 128.0), True, 4)
+    assert np.array_equal(load("fill4.u8", np.uint8), fill)
+    lab, _ = oracle.bwlabel2(fill, 8, True)
+    assert np.array_equal(load("labels8.i32", np.int32), lab)
+    flat, count = oracle.bwareaopen2(fill, False, True, 11, 1000, 8)
+    assert np.array_equal(load("area.u8", np.uint8), flat)
+    assert f"count {count} " in r.stdout
+    assert np.array_equal(load("hmin8.u8", np.uint8), oracle.imhmin(mask, 10, 8))
