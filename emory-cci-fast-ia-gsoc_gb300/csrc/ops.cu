@@ -481,11 +481,11 @@ cudaError_t record(const nsgb_opts* o, bool begin, cudaStream_t s) {
 
 // Reconstruction of the whole plan bracketed by the optional timing events.
 cudaError_t recon_timed(const nsgb_opts* o, int dtype, const Plan& P, int conn, bool erode, bool ring, void* ws,
-                        cudaStream_t s) {
+                        cudaStream_t s, int resweeps = 0) {
   cudaError_t e = record(o, true, s);
   if (e != cudaSuccess) return e;
   e = recon_launch_batch(dtype, P.I, P.t.r_tiles, conn, erode, ring, ws, s, o ? o->max_visits_per_tile : 0,
-                         o ? o->max_visit_iters : 0);
+                         o ? o->max_visit_iters : 0, resweeps);
   if (e != cudaSuccess) return e;
   return record(o, false, s);
 }
@@ -717,7 +717,7 @@ nsgb_status nsgb_imfill_holes(int dtype, const void* image, void* out, int64_t r
     case NSGB_F32: fill_marker_kernel<float><<<rc(rows, cols), 256, 0, s>>>((const float*)image, (float*)out, pitch, H, W); break;
   }
   const Plan R = single_plan(dtype, out, image, rows, cols, pitch);
-  e = recon_timed(opts, dtype, R, conn, true, false, ws, s);
+  e = recon_timed(opts, dtype, R, conn, true, false, ws, s, 2);  // front from the border: re-sweep
   return finish(e, ws, s, opts);
 }
 

@@ -107,6 +107,7 @@ struct Args {
   int ntiles;
   int flip, ring;
   int max_iters;
+  int resweeps;  // in-register re-sweeps of a tile marked dirty while it ran
   Ctl c;
 };
 
@@ -445,6 +446,19 @@ __device__ __forceinline__ void mark_tile(const Ctl& c, int nt) {
   set_status(c.status, kDevTimeout);
 }
 
+template <typename T, int CONN>
+__device__ __forceinline__ void halo_carries(WarpBuf& B, int lane) {
+  using P = Px<T>;
+  uint32_t hl = B.lv[lane + 1], hr = B.rv[lane + 1];
+  if constexpr (CONN == 8) {
+    hl = P::emax(hl, P::emax(B.lv[lane], B.lv[lane + 2]));
+    hr = P::emax(hr, P::emax(B.rv[lane], B.rv[lane + 2]));
+  }
+  B.hl[lane] = hl;
+  B.hr[lane] = hr;
+  __syncwarp();
+}
+
 // Image fields: from the kernel parameters for a single image (constant bank, nothing pinned
 // in registers), from the device table for a batch.
 #define IMF(field) (BATCH ? a.I.d[ii].field : a.I.one.field)
@@ -534,8 +548,8 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
     any_change |= v ^ O[i];
     O[i] = v;
   }
-  const uint32_t topv = init_word<T>(topv_raw, topm, y0 - 1, xl, H, W, ring);
-  const uint32_t botv = init_word<T>(botv_raw, botm, y0 + kRows, xl, H, W, ring);
+  uint32_t topv = init_word<T>(topv_raw, topm, y0 - 1, xl, H, W, ring);
+  uint32_t botv = init_word<T>(botv_raw, botm, y0 + kRows, xl, H, W, ring);
 #pragma unroll
   for (int j = 0; j < 2; ++j) {
     const int k = lane + 32 * j;
@@ -550,16 +564,7 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   __syncwarp();
   // What the (constant) halo columns give each row's first / last pixel: the same-row halo
   // pixel, and for 8-connectivity also the ones above and below (corners included).
-  {
-    uint32_t hl = B.lv[lane + 1], hr = B.rv[lane + 1];
-    if constexpr (CONN == 8) {
-      hl = P::emax(hl, P::emax(B.lv[lane], B.lv[lane + 2]));
-      hr = P::emax(hr, P::emax(B.rv[lane], B.rv[lane + 2]));
-    }
-    B.hl[lane] = hl;
-    B.hr[lane] = hr;
-  }
-  __syncwarp();
+  halo_carries<T, CONN>(B, lane);
   // Mask in the row layout.
   if constexpr (E == 2) {
     const int q = lane & 15, half = lane >> 4;
@@ -576,6 +581,7 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   __syncwarp();
 
   PROF_MARK(2);
+  for (int round = 0;; ++round) {
   // Sweep to the local fixed point.  A row pass is idempotent (exact left / right scans); with
   // 4-connectivity so is a column pass, so once a row pass after a column pass changes nothing
   // the tile is stable and the final column pass can be skipped.  With 8-connectivity the
@@ -687,6 +693,61 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   }
   __syncwarp();
   PROF_MARK(6);
+
+  // Release the tile.  If a neighbour changed while it ran, only its halo can be stale (no
+  // other warp writes its pixels).  Up to `resweeps` times the warp then takes the tile back,
+  // reloads just the halo and sweeps again from the values in its registers; otherwise the
+  // tile goes to the back of the queue, so that the neighbours still running finish first.
+  // Re-sweeping pays off where a front crosses the image (hole filling from the border: about
+  // a third less time at 16384^2) and costs time where many neighbours run at once (the
+  // h-maxima style marker of the chain: about 8% more), so the caller chooses.
+  int st = 0;
+  if (lane == 0) {
+    if (atomicCAS(&a.c.state[t], kRunning, kIdle) == kRunning) {
+      atomicSub(a.c.pending, 1);
+      st = 0;
+    } else if (round < a.resweeps) {
+      atomicExch(&a.c.state[t], kRunning);
+      atomicAdd(&a.c.stats[3], 1);
+      st = 1;
+    } else {
+      atomicExch(&a.c.state[t], kQueued);
+      atomicAdd(&a.c.stats[2], 1);
+      queue_push(a.c, t);
+      st = 0;
+    }
+  }
+  if (__shfl_sync(NSGB_FULL, st, 0) == 0) return;
+  // order the state change before reading the halo again, as at the start of a visit
+  __syncwarp();
+  __threadfence();
+  {
+    const uint32_t tv = load_word<T>(src, pitch, y0 - 1, xl, H, W, fast_top, coh, flip);
+    const uint32_t bv = load_word<T>(src, pitch, y0 + kRows, xl, H, W, fast_bot, coh, flip);
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int k = lane + 32 * j;
+      const int y = y0 - 1 + k;
+      const bool ok = k < 34;
+      hv[2 * j] = ok ? load_elem_at<T>(src, pitch, y, x0 - 1, H, W, coh, flip) : P::LOW;
+      hv[2 * j + 1] = ok ? load_elem_at<T>(src, pitch, y, x0 + TW, H, W, coh, flip) : P::LOW;
+    }
+    topv = init_word<T>(tv, topm, y0 - 1, xl, H, W, ring);
+    botv = init_word<T>(bv, botm, y0 + kRows, xl, H, W, ring);
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int k = lane + 32 * j;
+      if (k < 34) {
+        const int y = y0 - 1 + k;
+        B.lv[k] = init_elem<T>(hv[2 * j], B.lm[k], y, x0 - 1, H, W, ring);
+        B.rv[k] = init_elem<T>(hv[2 * j + 1], B.rm[k], y, x0 + TW, H, W, ring);
+      }
+    }
+    __syncwarp();
+    halo_carries<T, CONN>(B, lane);
+  }
+  any_change = 0;
+  }
 }
 
 template <typename T, int CONN, bool BATCH>
@@ -718,15 +779,6 @@ __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args a) {
     const long long _pe = clock64();
 #endif
     if (lane == 0) {
-      if (atomicCAS(&a.c.state[t], kRunning, kIdle) == kRunning) {
-        atomicSub(a.c.pending, 1);
-      } else {
-        // A neighbour changed while this tile ran: queue it again at the back, so the
-        // neighbours still running finish first (it stays counted in `pending`).
-        atomicExch(&a.c.state[t], kQueued);
-        atomicAdd(&a.c.stats[2], 1);
-        queue_push(a.c, t);
-      }
       // the visit budget is checked every `budget_step` visits of this warp (every visit
       // when the caller set a budget, every 16 against the default one)
       if (++visits_here == a.c.budget_step) {
@@ -805,7 +857,7 @@ __global__ void recon_init_kernel(Ctl c, Imgs I, int ntiles, int order) {
   }
 }
 
-// Workspace layout (ints): [0] status, [1..3] stats (visits, sweeps, re-runs), [6..7] visit
+// Workspace layout (ints): [0] status, [1..4] stats (visits, sweeps, re-runs, re-sweeps), [6..7] visit
 // counter (64-bit), [8] head, [9] tail, [10] pending, [16..31] phase timers (8 x 64-bit);
 // from int kHdrInts: state[ntiles], then the ring (2 ints per slot, cap slots).
 constexpr int kHdrInts = 64;
@@ -834,13 +886,14 @@ inline unsigned ring_cap(int64_t ntiles) {
 
 template <typename T, int CONN, bool BATCH>
 cudaError_t launch_typed(const Imgs& I, int ntiles, bool erode, bool ring, void* ws, cudaStream_t s,
-                         int max_visits_per_tile, int max_iters) {
+                         int max_visits_per_tile, int max_iters, int resweeps) {
   Args a;
   a.I = I;
   a.ntiles = ntiles;
   a.flip = erode ? 1 : 0;
   a.ring = ring ? 1 : 0;
   a.max_iters = max_iters > 0 ? max_iters : 4096;
+  a.resweeps = resweeps;
   int* wi = (int*)ws;
   a.c.status = wi + 0;
   a.c.stats = wi + 1;
@@ -912,15 +965,15 @@ size_t recon_workspace_bytes(int dtype, int64_t H, int64_t W) {
 }
 
 cudaError_t recon_launch_batch(int dtype, const Imgs& I, int ntiles, int conn, bool erode, bool ring, void* ws,
-                               cudaStream_t s, int max_visits, int max_iters) {
+                               cudaStream_t s, int max_visits, int max_iters, int resweeps) {
   switch (dtype) {
 #define NSGB_RECON_CASE(CODE, TYPE)                                                                       \
   case CODE:                                                                                               \
     if (I.d)                                                                                               \
-      return conn == 8 ? launch_typed<TYPE, 8, true>(I, ntiles, erode, ring, ws, s, max_visits, max_iters) \
-                       : launch_typed<TYPE, 4, true>(I, ntiles, erode, ring, ws, s, max_visits, max_iters);\
-    return conn == 8 ? launch_typed<TYPE, 8, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters)  \
-                     : launch_typed<TYPE, 4, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters);
+      return conn == 8 ? launch_typed<TYPE, 8, true>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps) \
+                       : launch_typed<TYPE, 4, true>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps);\
+    return conn == 8 ? launch_typed<TYPE, 8, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps)  \
+                     : launch_typed<TYPE, 4, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps);
     NSGB_RECON_CASE(NSGB_U8, uint8_t)
     NSGB_RECON_CASE(NSGB_U16, uint16_t)
     NSGB_RECON_CASE(NSGB_I32, int32_t)

@@ -16,9 +16,11 @@ size_t recon_workspace_bytes_tiles(int64_t ntiles);
 // An image descriptor for reconstruction (tile bases left at 0).
 Img recon_image(int dtype, void* plane, const void* mask, int64_t H, int64_t W, int64_t pitch);
 // Reconstructs every image of the batch in place (Img::plane holds the marker, Img::aux the
-// mask) in one persistent launch over all their tiles.
+// mask) in one persistent launch over all their tiles.  resweeps: how often a tile marked
+// dirty while it ran is swept again at once from its registers (after a halo reload) instead
+// of being queued again -- worth it for front-like propagation such as hole filling.
 cudaError_t recon_launch_batch(int dtype, const Imgs& I, int ntiles, int conn, bool erode, bool ring, void* ws,
-                               cudaStream_t s, int max_visits, int max_iters);
+                               cudaStream_t s, int max_visits, int max_iters, int resweeps = 0);
 
 // Workspace bytes for a reconstruction of an H x W image of `dtype`.
 size_t recon_workspace_bytes(int dtype, int64_t H, int64_t W);
