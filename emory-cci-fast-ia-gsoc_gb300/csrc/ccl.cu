@@ -157,7 +157,12 @@ __global__ void __launch_bounds__(kRankThreads) assign_ranks(Imgs I, Forest f, i
 
 }  // namespace
 
-int list_grid() { return 2 * 152; }
+int list_grid(int64_t max_items) {
+  int64_t g = max_items / 65536;
+  if (g < 2 * 152) g = 2 * 152;
+  if (g > 16 * 152) g = 16 * 152;
+  return (int)g;
+}
 
 int flat_grid(int64_t n) {
   int64_t b = (n + 255) / 256;
@@ -171,7 +176,7 @@ cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int
   cudaError_t e = cudaMemsetAsync(bits, 0, bits_bytes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, sizeof(int) * 2 * (size_t)t.n, s);
   if (e != cudaSuccess) return e;
-  const int g = list_grid();
+  const int g = list_grid(t.px);
   mark_roots<<<g, kRankThreads, 0, s>>>(I, f, (int)t.px, lo, hi, bits, counts);
   count_blocks<<<(t.blocks + kRankThreads / 32 - 1) / (kRankThreads / 32), kRankThreads, 0, s>>>(I, t.blocks, bits,
                                                                                                   block_tmp, wpre);

@@ -216,6 +216,8 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
     }
     __syncthreads();
   }
+  unsigned rb[4];
+  int nr = 0;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int ly = 4 * ty + k, i = ly * kTile + tx;
@@ -224,17 +226,35 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
     const int r = root[k];
     const int g = pb + gy * W + gx;
     if (in) f.L[g] = r < 0 ? -1 : pb + (y0 + r / kTile) * W + x0 + (r % kTile);
-    const bool is_root = in && r == i;
-    const unsigned rb = __ballot_sync(NSGB_FULL, is_root);
-    if (rb) {
-      int base = 0;
-      if (tx == 0) base = atomicAdd(f.nroots, __popc(rb));
-      base = __shfl_sync(NSGB_FULL, base, 0);
-      if (is_root) {
-        f.roots[base + __popc(rb & ((1u << tx) - 1u))] = g;
-        if (f.A) f.A[g] = s_cnt[i];
-      }
+    rb[k] = __ballot_sync(NSGB_FULL, in && r == i);
+    nr += __popc(rb[k]);
+  }
+  // The tile's local roots go to the list with one atomic per CTA (a tile of singleton
+  // components has 1024 roots; per-warp atomics on the one counter would serialise).
+  __shared__ int s_nr[kThreads / 32];
+  __shared__ int s_base;
+  if (tx == 0) s_nr[ty] = nr;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int tot = 0;
+    for (int w = 0; w < kThreads / 32; ++w) {
+      const int c = s_nr[w];
+      s_nr[w] = tot;
+      tot += c;
     }
+    s_base = tot ? atomicAdd(f.nroots, tot) : 0;
+  }
+  __syncthreads();
+  int base = s_base + s_nr[ty];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if ((rb[k] >> tx) & 1u) {
+      const int ly = 4 * ty + k, i = ly * kTile + tx;
+      const int g = pb + (y0 + ly) * W + x0 + tx;
+      f.roots[base + __popc(rb[k] & ((1u << tx) - 1u))] = g;
+      if (f.A) f.A[g] = s_cnt[i];
+    }
+    base += __popc(rb[k]);
   }
 }
 
@@ -293,14 +313,25 @@ __global__ void __launch_bounds__(64) ccl_merge(Cls cls, Imgs I, int* __restrict
 }
 
 // Every local root points directly at its global root; local-root areas move into the root.
+// Four list entries per thread and iteration, their loads issued together: most local roots
+// are global roots already (one load to see it), so the kernel is load-latency bound.
 static __global__ void ccl_flatten_roots(Forest f, int max_roots) {
   const int n = min(__ldcg(f.nroots), max_roots);
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const int lr = __ldcg(f.roots + k);
-    const int r = g_find(f.L, lr);
-    if (r != lr) {
-      atomicMin(f.L + lr, r);
-      if (f.A) atomicAdd(f.A + r, __ldcg(f.A + lr));
+  const int stride = gridDim.x * blockDim.x;
+  for (int k0 = blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += 4 * stride) {
+    int lr[4], p[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) lr[j] = k0 + j * stride < n ? __ldcg(f.roots + k0 + j * stride) : -1;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) p[j] = lr[j] >= 0 ? __ldcg(f.L + lr[j]) : -1;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (lr[j] < 0 || p[j] == lr[j]) continue;
+      const int r = g_find(f.L, lr[j]);
+      if (r != lr[j]) {
+        atomicMin(f.L + lr[j], r);
+        if (f.A) atomicAdd(f.A + r, __ldcg(f.A + lr[j]));
+      }
     }
   }
 }
@@ -396,8 +427,9 @@ __device__ __forceinline__ bool test_bit(const unsigned* bits, int r) {
 
 // Host helpers (ccl.cu).
 int flat_grid(int64_t n);
-// Grid for kernels that walk a device-side list (length unknown on the host).
-int list_grid();
+// Grid for kernels that walk a device-side list whose length (unknown on the host) is at most
+// max_items.
+int list_grid(int64_t max_items);
 // Row grids: x covers the widest image (256 columns per block), y strides the rows.
 inline dim3 rowcol_grid(int total_rows, int max_w) {
   return dim3((max_w + 255) / 256, (unsigned)(total_rows < 65535 ? total_rows : 65535));
@@ -419,7 +451,7 @@ cudaError_t label(const Cls& cls, const Imgs& I, const BatchTotals& t, int conn,
     ccl_local<Cls, 4><<<t.c_tiles, kThreads, 0, s>>>(cls, I, f);
     ccl_merge<Cls, 4><<<t.c_tiles, 64, 0, s>>>(cls, I, f.L);
   }
-  ccl_flatten_roots<<<list_grid(), 256, 0, s>>>(f, (int)t.px);
+  ccl_flatten_roots<<<list_grid(t.px), 256, 0, s>>>(f, (int)t.px);
   return cudaGetLastError();
 }
 

@@ -1135,7 +1135,9 @@ __global__ void grad_scatter_kernel(Imgs I, int total_rows, unsigned long long* 
       if (p != INT_MIN) {
         const int64_t q = p >= 0 ? (int64_t)p : ~(int64_t)p;
         if (q < (int64_t)m.H * m.W) {
-          v = __double2ll_rn((double)px<float>(m.plane, m.pitch, y, x) * 4294967296.0);
+          // g * 2^32 is exact in float; the conversion rounds to nearest, ties to even (no
+          // double arithmetic, which is slow on this GPU)
+          v = __float2ll_rn(px<float>(m.plane, m.pitch, y, x) * 4294967296.0f);
           key = ((int64_t)m.px_base + q) | (p < 0 ? (1ll << 40) : 0ll);
         } else {
           set_status(status, NSGB_ERR_BAD_ARG);
@@ -1162,16 +1164,30 @@ __global__ void grad_scatter_kernel(Imgs I, int total_rows, unsigned long long* 
   }
 }
 
-// Adjoint, pass 2: accumulators to float.  plane = g; dmarker / dmask at byte offsets.
+// Adjoint, pass 2: accumulators to float.  plane = g; dmarker / dmask at byte offsets.  One
+// rounding: the integer sum rounds to float, and the scaling by 2^-32 is exact.
 __global__ void grad_out_kernel(Imgs I, int total_rows, const long long* __restrict__ acc_marker,
                                 const long long* __restrict__ acc_mask, int64_t dmarker_off, int64_t dmask_off) {
-  ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
+  ccl::for_batch_quads(I, total_rows, [&](const Img& m, int y, int x, int n) {
     const int64_t gi = (int64_t)m.px_base + (int64_t)y * m.W + x;
-    const double s = 2.3283064365386962890625e-10;  // 2^-32
-    *pxp<float>((void*)shifted(m.plane, dmarker_off), m.pitch, y, x) =
-        __double2float_rn(__ll2double_rn(__ldcs(acc_marker + gi)) * s);
-    *pxp<float>((void*)shifted(m.plane, dmask_off), m.pitch, y, x) =
-        __double2float_rn(__ll2double_rn(__ldcs(acc_mask + gi)) * s);
+    const float s = 2.3283064365386962890625e-10f;  // 2^-32
+    float* dm = pxp<float>((void*)shifted(m.plane, dmarker_off), m.pitch, y, x);
+    float* dk = pxp<float>((void*)shifted(m.plane, dmask_off), m.pitch, y, x);
+    float a[4], b[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      a[k] = k < n ? __ll2float_rn(__ldcs(acc_marker + gi + k)) * s : 0.f;
+      b[k] = k < n ? __ll2float_rn(__ldcs(acc_mask + gi + k)) * s : 0.f;
+    }
+    if (n == 4 && (((uintptr_t)dm | (uintptr_t)dk) & 15) == 0) {
+      *(float4*)dm = make_float4(a[0], a[1], a[2], a[3]);
+      *(float4*)dk = make_float4(b[0], b[1], b[2], b[3]);
+    } else {
+      for (int k = 0; k < n; ++k) {
+        dm[k] = a[k];
+        dk[k] = b[k];
+      }
+    }
   });
 }
 
@@ -1300,7 +1316,7 @@ nsgb_status nsgb_recon_f32_bwd(const float* grad_out, const int32_t* prov, float
     grad_scatter_kernel<<<rcb(P.t), 256, 0, s>>>(P.I, P.t.rows, am, ak, status);
     const int64_t dmo = (int64_t)((uintptr_t)grad_marker - (uintptr_t)grad_out);
     const int64_t dko = (int64_t)((uintptr_t)grad_mask - (uintptr_t)grad_out);
-    grad_out_kernel<<<rcb(P.t), 256, 0, s>>>(P.I, P.t.rows, (const long long*)am, (const long long*)ak, dmo, dko);
+    grad_out_kernel<<<qrb(P.t), 256, 0, s>>>(P.I, P.t.rows, (const long long*)am, (const long long*)ak, dmo, dko);
     e = cudaGetLastError();
   }
   return finish(e, ws, s, opts);

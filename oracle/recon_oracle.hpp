@@ -489,7 +489,7 @@ bool recon_provenance(const T* marker, const T* mask, const T* R, int64_t H, int
 //   dmarker(q) = sum of g(p) over p with prov(p) = q,  dmask(q) = sum over prov(p) = ~q.
 // Each g(p) is rounded to the nearest multiple of 2^-32 (ties to even) and the sums are
 // exact 64-bit integer sums, so they do not depend on the order of summation; the result
-// is rounded to float.  |g| < 2^31 is required.
+// is rounded to float once.  |g| < 2^31 is required.
 inline void recon_grad_fixed(const float* g, const int32_t* prov, int64_t n, float* dmarker, float* dmask) {
   std::vector<int64_t> am((size_t)n, 0), ak((size_t)n, 0);
   for (int64_t p = 0; p < n; ++p) {
@@ -501,9 +501,10 @@ inline void recon_grad_fixed(const float* g, const int32_t* prov, int64_t n, flo
     if (v >= 0) am[q] += f;
     else ak[q] += f;
   }
+  // one rounding: the integer sum to float (round to nearest), then an exact scaling by 2^-32
   for (int64_t q = 0; q < n; ++q) {
-    dmarker[q] = (float)((double)am[q] * 2.3283064365386962890625e-10);
-    dmask[q] = (float)((double)ak[q] * 2.3283064365386962890625e-10);
+    dmarker[q] = (float)am[q] * 2.3283064365386962890625e-10f;
+    dmask[q] = (float)ak[q] * 2.3283064365386962890625e-10f;
   }
 }
 
