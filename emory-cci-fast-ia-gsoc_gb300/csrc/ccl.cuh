@@ -229,23 +229,12 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
     rb[k] = __ballot_sync(NSGB_FULL, in && r == i);
     nr += __popc(rb[k]);
   }
-  // The tile's local roots go to the list with one atomic per CTA (a tile of singleton
-  // components has 1024 roots; per-warp atomics on the one counter would serialise).
-  __shared__ int s_nr[kThreads / 32];
-  __shared__ int s_base;
-  if (tx == 0) s_nr[ty] = nr;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int tot = 0;
-    for (int w = 0; w < kThreads / 32; ++w) {
-      const int c = s_nr[w];
-      s_nr[w] = tot;
-      tot += c;
-    }
-    s_base = tot ? atomicAdd(f.nroots, tot) : 0;
-  }
-  __syncthreads();
-  int base = s_base + s_nr[ty];
+  // The warp's local roots (all four rows) go to the list with one atomic: a tile of singleton
+  // components has 1024 roots, and per-row atomics on the one counter would serialise.
+  if (nr == 0) return;  // warp-uniform: most warps of a labelling hold no root
+  int base = 0;
+  if (tx == 0) base = atomicAdd(f.nroots, nr);
+  base = __shfl_sync(NSGB_FULL, base, 0);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     if ((rb[k] >> tx) & 1u) {

@@ -1091,30 +1091,52 @@ __device__ __forceinline__ int source_key(const Img& m, int64_t marker_off, int 
   return kKeyNone;
 }
 
+// Four pixels per thread; equal roots among them (one plateau) are merged before the atomic.
 __global__ void source_best_kernel(Imgs I, int total_rows, int64_t marker_off, const int* __restrict__ L,
                                    int* __restrict__ best) {
-  ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
-    const int key = source_key(m, marker_off, y, x);
-    if (key == kKeyNone) return;
-    const int r = ccl::root_of(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
-    if (key < __ldcg(&best[r])) atomicMin(&best[r], key);
+  ccl::for_batch_quads(I, total_rows, [&](const Img& m, int y, int x, int n) {
+    int key[4], r[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) key[k] = k < n ? source_key(m, marker_off, y, x + k) : kKeyNone;
+    if (key[0] == kKeyNone && key[1] == kKeyNone && key[2] == kKeyNone && key[3] == kKeyNone) return;
+    ccl::roots4_ro(L, (int64_t)m.px_base + (int64_t)y * m.W + x, n, r);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (key[k] == kKeyNone) continue;
+      if (k < 3 && r[k + 1] == r[k]) {  // pass the smaller key on to the next pixel of the plateau
+        key[k + 1] = min(key[k + 1], key[k]);
+        continue;
+      }
+      if (key[k] < __ldcg(&best[r[k]])) atomicMin(&best[r[k]], key[k]);
+    }
   });
 }
 
 __global__ void prov_out_kernel(Imgs I, int total_rows, const int* __restrict__ L, const int* __restrict__ best,
                                 int64_t prov_off, int* status) {
-  ccl::for_batch_pixels(I, total_rows, [&](const Img& m, int y, int x) {
-    const int r = ccl::root_of_ro(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
-    const int key = __ldg(&best[r]);
-    const int n = m.H * m.W;
-    int32_t p;
-    if (key < n) p = ~key;
-    else if (key < 2 * n) p = key - n;
-    else {
-      p = INT_MIN;
-      if (key != 2 * n) set_status(status, NSGB_ERR_BAD_ARG);  // a plateau without a source: NaN input
+  ccl::for_batch_quads(I, total_rows, [&](const Img& m, int y, int x, int n) {
+    int r[4], p[4];
+    ccl::roots4_ro(L, (int64_t)m.px_base + (int64_t)y * m.W + x, n, r);
+    const int np = m.H * m.W;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (k >= n) {
+        p[k] = INT_MIN;
+        continue;
+      }
+      const int key = (k > 0 && r[k] == r[k - 1]) ? -1 : __ldg(&best[r[k]]);
+      if (key < 0) {
+        p[k] = p[k - 1];
+      } else if (key < np) {
+        p[k] = ~key;
+      } else if (key < 2 * np) {
+        p[k] = key - np;
+      } else {
+        p[k] = INT_MIN;
+        if (key != 2 * np) set_status(status, NSGB_ERR_BAD_ARG);  // a plateau without a source: NaN input
+      }
     }
-    *pxp<int32_t>((void*)shifted(m.plane, prov_off), m.pitch, y, x) = p;
+    store4_i32(pxp<int32_t>((void*)shifted(m.plane, prov_off), m.pitch, y, x), n, p);
   });
 }
 
@@ -1287,8 +1309,8 @@ nsgb_status nsgb_recon_f32_fwd(const float* marker, const float* mask, float* ou
   if (e == cudaSuccess) {
     const int64_t moff = (int64_t)((uintptr_t)marker - (uintptr_t)out);
     const int64_t poff = (int64_t)((uintptr_t)prov - (uintptr_t)out);
-    source_best_kernel<<<rcb(P.t), 256, 0, s>>>(P.I, P.t.rows, moff, w.L, w.A);
-    prov_out_kernel<<<rcb(P.t), 256, 0, s>>>(P.I, P.t.rows, w.L, w.A, poff, w.status);
+    source_best_kernel<<<qrb(P.t), 256, 0, s>>>(P.I, P.t.rows, moff, w.L, w.A);
+    prov_out_kernel<<<qrb(P.t), 256, 0, s>>>(P.I, P.t.rows, w.L, w.A, poff, w.status);
     e = cudaGetLastError();
   }
   return finish(e, ws, s, opts);
