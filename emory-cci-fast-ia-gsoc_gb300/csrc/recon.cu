@@ -176,21 +176,48 @@ __device__ __forceinline__ void store_word(T* base, int64_t pitch, int y, int x,
 }
 
 // Interior-tile word access at a precomputed address (flip = xor with fx).
+// `pairs`: the two elements of a 16-bit-lane word are loaded (stored) separately, for images
+// whose rows are not word aligned (an odd u8 width, say); the choice is the same for the whole
+// image, so it never diverges.
 template <typename T>
-__device__ __forceinline__ uint32_t fast_word(const char* p, bool coherent, uint32_t fx) {
+__device__ __forceinline__ uint32_t fast_word(const char* p, bool coherent, uint32_t fx, bool pairs) {
   if constexpr (sizeof(T) == 1) {
+    if (pairs) {
+      const uint32_t b0 = coherent ? __ldcg((const unsigned char*)p) : __ldg((const unsigned char*)p);
+      const uint32_t b1 = coherent ? __ldcg((const unsigned char*)p + 1) : __ldg((const unsigned char*)p + 1);
+      return (b0 | (b1 << 16)) ^ fx;
+    }
     const unsigned short v = coherent ? __ldcg((const unsigned short*)p) : __ldg((const unsigned short*)p);
     return __byte_perm((uint32_t)v, 0u, 0x7170) ^ fx;  // bytes b0,b1 -> 16-bit lanes
+  } else if constexpr (sizeof(T) == 2) {
+    if (pairs) {
+      const uint32_t h0 = coherent ? __ldcg((const unsigned short*)p) : __ldg((const unsigned short*)p);
+      const uint32_t h1 = coherent ? __ldcg((const unsigned short*)p + 1) : __ldg((const unsigned short*)p + 1);
+      return (h0 | (h1 << 16)) ^ fx;
+    }
+    return (coherent ? __ldcg((const unsigned int*)p) : __ldg((const unsigned int*)p)) ^ fx;
   } else {
     return (coherent ? __ldcg((const unsigned int*)p) : __ldg((const unsigned int*)p)) ^ fx;
   }
 }
 
 template <typename T>
-__device__ __forceinline__ void fast_store(char* p, uint32_t w, uint32_t fx) {
+__device__ __forceinline__ void fast_store(char* p, uint32_t w, uint32_t fx, bool pairs) {
   w ^= fx;
   if constexpr (sizeof(T) == 1) {
+    if (pairs) {
+      __stcg((unsigned char*)p, (unsigned char)(w & 0xFFu));
+      __stcg((unsigned char*)p + 1, (unsigned char)((w >> 16) & 0xFFu));
+      return;
+    }
     __stcg((unsigned short*)p, (unsigned short)__byte_perm(w, 0u, 0x0020));
+  } else if constexpr (sizeof(T) == 2) {
+    if (pairs) {
+      __stcg((unsigned short*)p, (unsigned short)(w & 0xFFFFu));
+      __stcg((unsigned short*)p + 1, (unsigned short)(w >> 16));
+      return;
+    }
+    __stcg((unsigned int*)p, w);
   } else {
     __stcg((unsigned int*)p, w);
   }
@@ -463,7 +490,7 @@ __device__ __forceinline__ void halo_carries(WarpBuf& B, int lane) {
 // in registers), from the device table for a batch.
 #define IMF(field) (BATCH ? a.I.d[ii].field : a.I.one.field)
 
-template <typename T, int CONN, bool BATCH>
+template <typename T, int CONN, bool BATCH, bool RS>
 __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane) {
   using P = Px<T>;
   constexpr int E = P::E;
@@ -483,6 +510,7 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   const bool coh = true;
   const bool interior = (y0 + kRows <= H) && (x0 + TW <= W);
   const bool fast = interior && IMF(aligned);
+  const bool pairs = false;  // word-aligned rows only on the straight-line path
   const int xl = x0 + E * lane;
   const uint32_t fx = flip ? P::FLIP : 0u;
 
@@ -492,7 +520,7 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   if (fast) {
     const char* mp = (const char*)mask + (int64_t)y0 * pitch + (int64_t)xl * sizeof(T);
 #pragma unroll
-    for (int i = 0; i < 32; ++i) M[i] = fast_word<T>(mp + i * pitch, false, fx);
+    for (int i = 0; i < 32; ++i) M[i] = fast_word<T>(mp + i * pitch, false, fx, pairs);
   }
   // The caller has set the tile RUNNING; order that before reading the neighbours' pixels.
   __syncwarp();
@@ -504,9 +532,9 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   if (fast) {  // interior tile: straight-line loads through running row pointers, no checks
     const char* op = (const char*)src + (int64_t)y0 * pitch + (int64_t)xl * sizeof(T);
 #pragma unroll
-    for (int i = 0; i < 32; ++i) O[i] = fast_word<T>(op + i * pitch, true, fx);
+    for (int i = 0; i < 32; ++i) O[i] = fast_word<T>(op + i * pitch, true, fx, pairs);
   } else {
-    // Edge or unaligned tile: bounds-checked loads in a rolled loop through shared memory
+    // Edge tile: bounds-checked loads in a rolled loop through shared memory
     // (keeps this rarely used path out of the instruction cache's way).
 #pragma unroll 1
     for (int i = 0; i < 32; ++i) {
@@ -522,8 +550,8 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
     __syncwarp();
   }
   // Halo rows (column layout words) and halo columns (single elements).
-  const bool fast_top = fast && y0 > 0;
-  const bool fast_bot = fast && y0 + kRows < H;
+  const bool fast_top = fast && !pairs && y0 > 0;
+  const bool fast_bot = fast && !pairs && y0 + kRows < H;
   const uint32_t topm = load_word<T>(mask, pitch, y0 - 1, xl, H, W, fast_top, false, flip);
   const uint32_t topv_raw = load_word<T>(src, pitch, y0 - 1, xl, H, W, fast_top, coh, flip);
   const uint32_t botm = load_word<T>(mask, pitch, y0 + kRows, xl, H, W, fast_bot, false, flip);
@@ -581,6 +609,7 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   __syncwarp();
 
   PROF_MARK(2);
+#pragma unroll 1
   for (int round = 0;; ++round) {
   // Sweep to the local fixed point.  A row pass is idempotent (exact left / right scans); with
   // 4-connectivity so is a column pass, so once a row pass after a column pass changes nothing
@@ -614,7 +643,7 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
     if (fast) {
       char* sp = (char*)out + (int64_t)y0 * pitch + (int64_t)xl * sizeof(T);
 #pragma unroll
-      for (int i = 0; i < 32; ++i) fast_store<T>(sp + i * pitch, O[i], fx);
+      for (int i = 0; i < 32; ++i) fast_store<T>(sp + i * pitch, O[i], fx, pairs);
     } else {
 #pragma unroll
       for (int i = 0; i < 32; ++i) B.xp[lane * 33 + i] = O[i];
@@ -701,6 +730,21 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   // Re-sweeping pays off where a front crosses the image (hole filling from the border: about
   // a third less time at 16384^2) and costs time where many neighbours run at once (the
   // h-maxima style marker of the chain: about 8% more), so the caller chooses.
+  if constexpr (!RS) {
+    // (without re-sweeps the loop body runs once: kept separate so that the compiler emits
+    // one copy of the sweep code)
+    if (lane == 0) {
+      if (atomicCAS(&a.c.state[t], kRunning, kIdle) == kRunning) {
+        atomicSub(a.c.pending, 1);
+      } else {
+        atomicExch(&a.c.state[t], kQueued);
+        atomicAdd(&a.c.stats[2], 1);
+        queue_push(a.c, t);
+      }
+    }
+    __syncwarp();
+    return;
+  }
   int st = 0;
   if (lane == 0) {
     if (atomicCAS(&a.c.state[t], kRunning, kIdle) == kRunning) {
@@ -750,7 +794,7 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   }
 }
 
-template <typename T, int CONN, bool BATCH>
+template <typename T, int CONN, bool BATCH, bool RS>
 __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   WarpBuf& B = reinterpret_cast<WarpBuf*>(smem_raw)[threadIdx.x >> 5];
@@ -774,7 +818,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args a) {
     }
 #endif
     if (lane == 0) atomicExch(&a.c.state[t], kRunning);
-    visit<T, CONN, BATCH>(a, B, t, lane);
+    visit<T, CONN, BATCH, RS>(a, B, t, lane);
 #ifdef NSGB_RECON_PROFILE
     const long long _pe = clock64();
 #endif
@@ -884,7 +928,7 @@ inline unsigned ring_cap(int64_t ntiles) {
   return c;
 }
 
-template <typename T, int CONN, bool BATCH>
+template <typename T, int CONN, bool BATCH, bool RS>
 cudaError_t launch_typed(const Imgs& I, int ntiles, bool erode, bool ring, void* ws, cudaStream_t s,
                          int max_visits_per_tile, int max_iters, int resweeps) {
   Args a;
@@ -920,10 +964,10 @@ cudaError_t launch_typed(const Imgs& I, int ntiles, bool erode, bool ring, void*
   cudaGetDevice(&dev);
   int& occ = occ_cache[dev & 7];
   if (occ == 0) {
-    e = cudaFuncSetAttribute(recon_kernel<T, CONN, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(recon_kernel<T, CONN, BATCH, RS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int bps = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, recon_kernel<T, CONN, BATCH>, kWarps * 32, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, recon_kernel<T, CONN, BATCH, RS>, kWarps * 32, smem);
     if (e != cudaSuccess) return e;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -936,7 +980,7 @@ cudaError_t launch_typed(const Imgs& I, int ntiles, bool erode, bool ring, void*
   void* args[] = {&a};
   // Cooperative launch: all CTAs are co-resident, so warps waiting on the queue never block
   // warps that still have to be scheduled.
-  return cudaLaunchCooperativeKernel((const void*)recon_kernel<T, CONN, BATCH>, dim3(grid), dim3(kWarps * 32), args, smem,
+  return cudaLaunchCooperativeKernel((const void*)recon_kernel<T, CONN, BATCH, RS>, dim3(grid), dim3(kWarps * 32), args, smem,
                                      s);
 }
 
@@ -964,16 +1008,30 @@ size_t recon_workspace_bytes(int dtype, int64_t H, int64_t W) {
   return recon_workspace_bytes_tiles((int64_t)tx * recon_tiles_y(H));
 }
 
+namespace {
+// Kernel instantiation for a call: image table or single image, connectivity, and re-sweeps
+// (their loop is a separate kernel, so that the common path keeps one copy of the sweep code;
+// re-sweeps are offered for single images, where hole filling uses them).
+template <typename T, bool RS>
+cudaError_t dispatch_conn(const Imgs& I, int ntiles, int conn, bool erode, bool ring, void* ws, cudaStream_t s,
+                          int max_visits, int max_iters, int resweeps) {
+  if (I.d)
+    return conn == 8 ? launch_typed<T, 8, true, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, 0)
+                     : launch_typed<T, 4, true, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, 0);
+  return conn == 8 ? launch_typed<T, 8, false, RS>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps)
+                   : launch_typed<T, 4, false, RS>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps);
+}
+}  // namespace
+
 cudaError_t recon_launch_batch(int dtype, const Imgs& I, int ntiles, int conn, bool erode, bool ring, void* ws,
                                cudaStream_t s, int max_visits, int max_iters, int resweeps) {
   switch (dtype) {
-#define NSGB_RECON_CASE(CODE, TYPE)                                                                       \
-  case CODE:                                                                                               \
-    if (I.d)                                                                                               \
-      return conn == 8 ? launch_typed<TYPE, 8, true>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps) \
-                       : launch_typed<TYPE, 4, true>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps);\
-    return conn == 8 ? launch_typed<TYPE, 8, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps)  \
-                     : launch_typed<TYPE, 4, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps);
+#define NSGB_RECON_CASE(CODE, TYPE)                                                                           \
+  case CODE:                                                                                                   \
+    return resweeps > 0 ? dispatch_conn<TYPE, true>(I, ntiles, conn, erode, ring, ws, s, max_visits, max_iters,  \
+                                                    resweeps)                                                   \
+                        : dispatch_conn<TYPE, false>(I, ntiles, conn, erode, ring, ws, s, max_visits, max_iters, \
+                                                     resweeps);
     NSGB_RECON_CASE(NSGB_U8, uint8_t)
     NSGB_RECON_CASE(NSGB_U16, uint16_t)
     NSGB_RECON_CASE(NSGB_I32, int32_t)
