@@ -35,10 +35,13 @@
 #include "batch.cuh"
 #include "common.cuh"
 #include "recon.cuh"
+#include "tilequeue.cuh"
 
 namespace nsgb {
 
 namespace {
+
+using namespace tq;
 
 constexpr int kWarps = 4;   // warps (independent tile workers) per CTA
 constexpr int kRows = 32;   // rows per tile
@@ -52,8 +55,6 @@ struct alignas(16) WarpBuf {
   uint32_t c0[32], c1[32];  // final first / last tile column, for the neighbour test
   uint32_t hl[32], hr[32];  // per row: what the halo columns give the first / last column
 };
-
-enum TileState : int { kIdle = 0, kQueued = 1, kRunning = 2, kRunningDirty = 3 };
 
 // Optional phase timers (compile with -DNSGB_RECON_PROFILE): lane 0 of every warp adds the
 // clock cycles spent per phase into 64-bit counters in the workspace header.
@@ -79,26 +80,6 @@ __device__ __forceinline__ unsigned long long global_ns() {
   do {                  \
   } while (0)
 #endif
-
-struct Slot {
-  int val;
-  unsigned seq;
-};
-
-struct Ctl {
-  int* state;         // [ntiles] TileState
-  Slot* slots;        // [cap] work ring
-  unsigned* head;     // consumer ticket counter
-  unsigned* tail;     // producer ticket counter
-  int* pending;       // queued + running tiles
-  int* status;
-  int* stats;         // [0] visits, [1] sweeps, [2] re-runs
-  unsigned long long* visit_count;  // budget counter
-  unsigned long long* prof;         // [8] phase cycle counters (profiling builds only)
-  unsigned cap;       // ring capacity (power of two >= ntiles)
-  long long max_visits;
-  int budget_step;
-};
 
 // Images of the batch: Img::plane is reconstructed in place (it holds the marker on entry),
 // Img::aux is the mask.  Tiles of all images are numbered consecutively.
@@ -409,68 +390,6 @@ __device__ __forceinline__ uint32_t col_pass(uint32_t (&O)[32], const WarpBuf& B
     dn = n;
   }
   return acc;
-}
-
-__device__ __forceinline__ void st_release_u(unsigned* p, unsigned v) {
-  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-// Producer side of the ring (Vyukov's bounded queue): wait until slot `p` is free for this
-// lap, fill it, publish it.
-__device__ __forceinline__ bool queue_push(const Ctl& c, int t) {
-  const unsigned p = atomicAdd(c.tail, 1u);
-  Slot* sl = &c.slots[p & (c.cap - 1)];
-  long long spins = 0;
-  while (ld_acquire_u(&sl->seq) != p) {
-    if (++spins > kSpinLimit || ld_relaxed(c.status) != 0) {
-      set_status(c.status, kDevTimeout);
-      return false;
-    }
-    __nanosleep(64);
-  }
-  sl->val = t;
-  st_release_u(&sl->seq, p + 1u);
-  return true;
-}
-
-// Consumer side: claim a ticket and wait for its item; returns -1 when no tile is queued or
-// running any more (pending == 0: nothing can be pushed again) or after an error.
-__device__ __forceinline__ int queue_pop(const Ctl& c) {
-  const unsigned tk = atomicAdd(c.head, 1u);
-  Slot* sl = &c.slots[tk & (c.cap - 1)];
-  long long spins = 0;
-  unsigned ns = 32;
-  for (;;) {
-    if (ld_acquire_u(&sl->seq) == tk + 1u) {
-      const int t = *(volatile int*)&sl->val;
-      st_release_u(&sl->seq, tk + c.cap);
-      return t;
-    }
-    if (ld_acquire(c.pending) == 0 || ld_relaxed(c.status) != 0) return -1;
-    if (++spins > kSpinLimit) {
-      set_status(c.status, kDevTimeout);
-      return -1;
-    }
-    __nanosleep(ns);
-    if (ns < 1024) ns <<= 1;
-  }
-}
-
-// A neighbour's values may have become stale: make sure it (re)reads them.  The common case
-// (an idle neighbour) takes one atomic.
-__device__ __forceinline__ void mark_tile(const Ctl& c, int nt) {
-  int s = atomicCAS(&c.state[nt], kIdle, kQueued);
-  for (int guard = 0; guard < 1024; ++guard) {
-    if (s == kIdle) {  // this call queued it
-      atomicAdd(c.pending, 1);
-      queue_push(c, nt);
-      return;
-    }
-    if (s == kQueued || s == kRunningDirty) return;  // will load after our stores
-    s = atomicCAS(&c.state[nt], kRunning, kRunningDirty);
-    if (s == kRunning) return;  // its owner re-runs it
-  }
-  set_status(c.status, kDevTimeout);
 }
 
 template <typename T, int CONN>
@@ -844,47 +763,6 @@ __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args a) {
   }
 }
 
-// Initial queue order.  order 0: raster.  order 1: checkerboard, even tiles first.  order 2:
-// four colours by (row parity, column parity) in the sequence (0,0), (1,1), (0,1), (1,0), so
-// that no two tiles of one colour touch, not even diagonally.  Tiles taken from the queue at
-// the same time are then rarely neighbours, and later colours read finished neighbours.
-__device__ __forceinline__ int initial_tile(int i, int ntiles, int tiles_x, int order) {
-  const int tiles_y = ntiles / tiles_x;
-  if (order == 1) {
-    // tiles (ty, tx) with (ty + tx) even first, then the odd ones, each in raster order; row ty
-    // holds ceil(tiles_x / 2) of its first colour and floor(tiles_x / 2) of the other
-    const int hi = (tiles_x + 1) / 2, lo = tiles_x / 2;
-    const int even_total = ((tiles_y + 1) / 2) * hi + (tiles_y / 2) * lo;
-    int k = i, parity = 0;
-    if (k >= even_total) {
-      k -= even_total;
-      parity = 1;
-    }
-    // rows alternate between `a` tiles (ty even for parity 0) and `b` tiles
-    const int a = parity ? lo : hi, b = parity ? hi : lo;
-    const int pair = a + b;
-    int ty = pair ? 2 * (k / pair) : 0;
-    k = pair ? k % pair : k;
-    if (k >= a) {
-      k -= a;
-      ++ty;
-    }
-    const int first = ((ty & 1) ^ parity) ? 1 : 0;
-    return ty * tiles_x + first + 2 * k;
-  }
-  if (order == 2) {
-    const int seq_py[4] = {0, 1, 0, 1}, seq_px[4] = {0, 1, 1, 0};
-    int k = i;
-    for (int c = 0; c < 4; ++c) {
-      const int py = seq_py[c], px = seq_px[c];
-      const int ny = (tiles_y - py + 1) / 2, nx = (tiles_x - px + 1) / 2;
-      if (k < ny * nx) return (py + 2 * (k / nx)) * tiles_x + px + 2 * (k % nx);
-      k -= ny * nx;
-    }
-  }
-  return i;
-}
-
 __global__ void recon_init_kernel(Ctl c, Imgs I, int ntiles, int order) {
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < c.cap; i += gridDim.x * blockDim.x) {
     if ((int)i < ntiles) {
@@ -924,12 +802,6 @@ inline int recon_order(int elems_per_word) {
   }
   if (order >= 0) return order;
   return elems_per_word == 2 ? 1 : 2;
-}
-
-inline unsigned ring_cap(int64_t ntiles) {
-  unsigned c = 32;
-  while ((int64_t)c < ntiles) c <<= 1;
-  return c;
 }
 
 template <typename T, int CONN, bool BATCH, bool RS>
