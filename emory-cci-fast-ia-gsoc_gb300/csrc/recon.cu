@@ -46,10 +46,15 @@ using namespace tq;
 constexpr int kWarps = 4;   // warps (independent tile workers) per CTA
 constexpr int kRows = 32;   // rows per tile
 
+// Shared-memory rows are kS = 34 words apart: pairs of words (even index) are 8-byte aligned
+// and move as one 64-bit access, and the 16 lanes of each half-warp phase of such an access
+// hit 32 distinct banks.
+constexpr int kS = 34;
+
 struct alignas(16) WarpBuf {
-  uint32_t xp[32 * 33];  // transpose scratch
-  uint32_t mh[32 * 33];  // mask, row-pass layout  [lane*33 + j]
-  uint32_t mv[32 * 33];  // mask, column-pass layout [lane*33 + i]
+  uint32_t xp[32 * kS];  // transpose scratch
+  uint32_t mh[32 * kS];  // mask, row-pass layout  [lane*kS + j]
+  uint32_t mv[32 * kS];  // mask, column-pass layout [lane*kS + i]
   uint32_t lv[36], rv[36];  // halo columns (values), index r + 1 for rows r = -1 .. 32
   uint32_t lm[36], rm[36];  // halo columns (masks)
   uint32_t c0[32], c1[32];  // final first / last tile column, for the neighbour test
@@ -231,6 +236,11 @@ __device__ __forceinline__ uint32_t load_elem_at(const T* base, int64_t pitch, i
   return (coherent ? P::load_elem(r) : P::load_elem_ro(r)) ^ (flip ? P::ELEM_FLIP : 0u);
 }
 
+__device__ __forceinline__ void sts2(uint32_t* p, uint32_t a, uint32_t b) {
+  *reinterpret_cast<uint2*>(p) = make_uint2(a, b);
+}
+__device__ __forceinline__ uint2 lds2(const uint32_t* p) { return *reinterpret_cast<const uint2*>(p); }
+
 // ------------------------------------------------------------------------------------------
 // Layout changes.  Column layout: lane l holds words O[i] = (row i, cols E*l .. E*l+E-1).
 // Row layout (E = 2): lane h = q + 16*half holds words OH[j] = (rows 2q, 2q+1; col 32*half+j).
@@ -239,19 +249,19 @@ __device__ __forceinline__ uint32_t load_elem_at(const T* base, int64_t pitch, i
 template <int E>
 __device__ __forceinline__ void col_to_row(uint32_t (&O)[32], uint32_t* xp, int lane) {
 #pragma unroll
-  for (int i = 0; i < 32; ++i) xp[lane * 33 + i] = O[i];
+  for (int i = 0; i < 32; i += 2) sts2(xp + lane * kS + i, O[i], O[i + 1]);
   __syncwarp();
   if constexpr (E == 2) {
     const int q = lane & 15, half = lane >> 4;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const int l = 16 * half + (j >> 1);
-      uint32_t a = xp[l * 33 + 2 * q], b = xp[l * 33 + 2 * q + 1];
-      O[j] = (j & 1) ? __byte_perm(a, b, 0x7632) : __byte_perm(a, b, 0x5410);
+    for (int j = 0; j < 32; j += 2) {
+      const uint2 ab = lds2(xp + (16 * half + (j >> 1)) * kS + 2 * q);
+      O[j] = __byte_perm(ab.x, ab.y, 0x5410);
+      O[j + 1] = __byte_perm(ab.x, ab.y, 0x7632);
     }
   } else {
 #pragma unroll
-    for (int j = 0; j < 32; ++j) O[j] = xp[j * 33 + lane];
+    for (int j = 0; j < 32; ++j) O[j] = xp[j * kS + lane];
   }
   __syncwarp();
 }
@@ -259,20 +269,20 @@ __device__ __forceinline__ void col_to_row(uint32_t (&O)[32], uint32_t* xp, int 
 template <int E>
 __device__ __forceinline__ void row_to_col(uint32_t (&O)[32], uint32_t* xp, int lane) {
 #pragma unroll
-  for (int j = 0; j < 32; ++j) xp[lane * 33 + j] = O[j];
+  for (int j = 0; j < 32; j += 2) sts2(xp + lane * kS + j, O[j], O[j + 1]);
   __syncwarp();
   if constexpr (E == 2) {
     const int h0 = 16 * (lane >> 4);
     const int j0 = (2 * lane) & 31;
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
-      uint32_t w0 = xp[(h0 + q) * 33 + j0], w1 = xp[(h0 + q) * 33 + j0 + 1];
-      O[2 * q] = __byte_perm(w0, w1, 0x5410);
-      O[2 * q + 1] = __byte_perm(w0, w1, 0x7632);
+      const uint2 w = lds2(xp + (h0 + q) * kS + j0);
+      O[2 * q] = __byte_perm(w.x, w.y, 0x5410);
+      O[2 * q + 1] = __byte_perm(w.x, w.y, 0x7632);
     }
   } else {
 #pragma unroll
-    for (int i = 0; i < 32; ++i) O[i] = xp[i * 33 + lane];
+    for (int i = 0; i < 32; ++i) O[i] = xp[i * kS + lane];
   }
   __syncwarp();
 }
@@ -291,13 +301,17 @@ __device__ __forceinline__ uint32_t row_pass(uint32_t (&O)[32], const uint32_t* 
     const int q = lane & 15, half = lane >> 4;
     uint32_t lo = P::LOW, hi = P::HIGH, lo2 = P::LOW, hi2 = P::HIGH;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const uint32_t m = mh[lane * 33 + j];
-      lo = P::vmin(P::vmax(lo, O[j]), m);
-      hi = P::vmin(P::vmax(hi, O[j]), m);
-      const uint32_t m2 = mh[lane * 33 + 31 - j];
-      lo2 = P::vmin(P::vmax(lo2, O[31 - j]), m2);
-      hi2 = P::vmin(P::vmax(hi2, O[31 - j]), m2);
+    for (int j = 0; j < 32; j += 2) {
+      const uint2 m = lds2(mh + lane * kS + j);
+      lo = P::vmin(P::vmax(lo, O[j]), m.x);
+      hi = P::vmin(P::vmax(hi, O[j]), m.x);
+      lo = P::vmin(P::vmax(lo, O[j + 1]), m.y);
+      hi = P::vmin(P::vmax(hi, O[j + 1]), m.y);
+      const uint2 m2 = lds2(mh + lane * kS + 30 - j);
+      lo2 = P::vmin(P::vmax(lo2, O[31 - j]), m2.y);
+      hi2 = P::vmin(P::vmax(hi2, O[31 - j]), m2.y);
+      lo2 = P::vmin(P::vmax(lo2, O[30 - j]), m2.x);
+      hi2 = P::vmin(P::vmax(hi2, O[30 - j]), m2.x);
     }
     const uint32_t carry_l = P::pack(B.hl[2 * q], B.hl[2 * q + 1]);
     const uint32_t carry_r = P::pack(B.hr[2 * q], B.hr[2 * q + 1]);
@@ -307,43 +321,68 @@ __device__ __forceinline__ uint32_t row_pass(uint32_t (&O)[32], const uint32_t* 
     const uint32_t from1 = __shfl_down_sync(NSGB_FULL, ex_r, 16);
     uint32_t v = half ? from0 : carry_l;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const uint32_t m = mh[lane * 33 + j];
-      const uint32_t n = P::vmin(P::vmax(O[j], v), m);
-      acc |= n ^ O[j];
-      O[j] = n;
-      v = n;
+    for (int j = 0; j < 32; j += 2) {
+      const uint2 m = lds2(mh + lane * kS + j);
+      const uint32_t n0 = P::vmin(P::vmax(O[j], v), m.x);
+      const uint32_t n1 = P::vmin(P::vmax(O[j + 1], n0), m.y);
+      acc |= (n0 ^ O[j]) | (n1 ^ O[j + 1]);
+      O[j] = n0;
+      O[j + 1] = n1;
+      v = n1;
     }
     v = half ? carry_r : from1;
 #pragma unroll
-    for (int j = 31; j >= 0; --j) {
-      const uint32_t m = mh[lane * 33 + j];
-      const uint32_t n = P::vmin(P::vmax(O[j], v), m);
-      acc |= n ^ O[j];
-      O[j] = n;
-      v = n;
+    for (int j = 30; j >= 0; j -= 2) {
+      const uint2 m = lds2(mh + lane * kS + j);
+      const uint32_t n1 = P::vmin(P::vmax(O[j + 1], v), m.y);
+      const uint32_t n0 = P::vmin(P::vmax(O[j], n1), m.x);
+      acc |= (n0 ^ O[j]) | (n1 ^ O[j + 1]);
+      O[j] = n0;
+      O[j + 1] = n1;
+      v = n0;
     }
   } else {
     uint32_t v = B.hl[lane];
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const uint32_t m = mh[lane * 33 + j];
-      const uint32_t n = P::vmin(P::vmax(O[j], v), m);
-      acc |= n ^ O[j];
-      O[j] = n;
-      v = n;
+    for (int j = 0; j < 32; j += 2) {
+      const uint2 m = lds2(mh + lane * kS + j);
+      const uint32_t n0 = P::vmin(P::vmax(O[j], v), m.x);
+      const uint32_t n1 = P::vmin(P::vmax(O[j + 1], n0), m.y);
+      acc |= (n0 ^ O[j]) | (n1 ^ O[j + 1]);
+      O[j] = n0;
+      O[j + 1] = n1;
+      v = n1;
     }
     v = B.hr[lane];
 #pragma unroll
-    for (int j = 31; j >= 0; --j) {
-      const uint32_t m = mh[lane * 33 + j];
-      const uint32_t n = P::vmin(P::vmax(O[j], v), m);
-      acc |= n ^ O[j];
-      O[j] = n;
-      v = n;
+    for (int j = 30; j >= 0; j -= 2) {
+      const uint2 m = lds2(mh + lane * kS + j);
+      const uint32_t n1 = P::vmin(P::vmax(O[j + 1], v), m.y);
+      const uint32_t n0 = P::vmin(P::vmax(O[j], n1), m.x);
+      acc |= (n0 ^ O[j]) | (n1 ^ O[j + 1]);
+      O[j] = n0;
+      O[j + 1] = n1;
+      v = n0;
     }
   }
   return acc;
+}
+
+// What a row of the column layout gives the row below (or above): each pixel itself, and for
+// 8-connectivity its left and right neighbours.  The shuffles return the lane's own word at
+// lanes 0 and 31; the neighbour read there instead of one beyond the tile edge is another
+// 8-neighbour of the target pixel (the pixel two columns over in the row of the source
+// word, or the pixel above it), so it adds nothing beyond the tile.
+template <typename T, int CONN>
+__device__ __forceinline__ uint32_t dilate_row(uint32_t w) {
+  using P = Px<T>;
+  if constexpr (CONN == 8) {
+    const uint32_t l = __shfl_up_sync(NSGB_FULL, w, 1);
+    const uint32_t r = __shfl_down_sync(NSGB_FULL, w, 1);
+    return P::vmax(w, P::vmax(P::from_left(l, w), P::from_right(w, r)));
+  } else {
+    return w;
+  }
 }
 
 // Column pass on the column layout: top-to-bottom then bottom-to-top, each step taking the
@@ -358,16 +397,8 @@ __device__ __forceinline__ uint32_t col_pass(uint32_t (&O)[32], const WarpBuf& B
   uint32_t up = top;
 #pragma unroll
   for (int i = 0; i < 32; ++i) {
-    uint32_t a = up;
-    if constexpr (CONN == 8) {
-      uint32_t l = __shfl_up_sync(NSGB_FULL, up, 1);
-      uint32_t r = __shfl_down_sync(NSGB_FULL, up, 1);
-      if (lane == 0) l = P::LOW;
-      if (lane == 31) r = P::LOW;
-      a = P::vmax(a, P::vmax(P::from_left(l, up), P::from_right(up, r)));
-    }
-    const uint32_t m = B.mv[lane * 33 + i];
-    const uint32_t n = P::vmin(P::vmax(O[i], a), m);
+    const uint32_t m = (i & 1) ? lds2(B.mv + lane * kS + i - 1).y : lds2(B.mv + lane * kS + i).x;
+    const uint32_t n = P::vmin(P::vmax(O[i], dilate_row<T, CONN>(up)), m);
     acc |= n ^ O[i];
     O[i] = n;
     up = n;
@@ -375,16 +406,8 @@ __device__ __forceinline__ uint32_t col_pass(uint32_t (&O)[32], const WarpBuf& B
   uint32_t dn = bot;
 #pragma unroll
   for (int i = 31; i >= 0; --i) {
-    uint32_t a = dn;
-    if constexpr (CONN == 8) {
-      uint32_t l = __shfl_up_sync(NSGB_FULL, dn, 1);
-      uint32_t r = __shfl_down_sync(NSGB_FULL, dn, 1);
-      if (lane == 0) l = P::LOW;
-      if (lane == 31) r = P::LOW;
-      a = P::vmax(a, P::vmax(P::from_left(l, dn), P::from_right(dn, r)));
-    }
-    const uint32_t m = B.mv[lane * 33 + i];
-    const uint32_t n = P::vmin(P::vmax(O[i], a), m);
+    const uint32_t m = (i & 1) ? lds2(B.mv + lane * kS + i - 1).y : lds2(B.mv + lane * kS + i).x;
+    const uint32_t n = P::vmin(P::vmax(O[i], dilate_row<T, CONN>(dn)), m);
     acc |= n ^ O[i];
     O[i] = n;
     dn = n;
@@ -461,14 +484,14 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
     // (keeps this rarely used path out of the instruction cache's way).
 #pragma unroll 1
     for (int i = 0; i < 32; ++i) {
-      B.xp[lane * 33 + i] = load_word<T>(mask, pitch, y0 + i, xl, H, W, false, false, flip);
-      B.mh[lane * 33 + i] = load_word<T>(src, pitch, y0 + i, xl, H, W, false, true, flip);
+      B.xp[lane * kS + i] = load_word<T>(mask, pitch, y0 + i, xl, H, W, false, false, flip);
+      B.mh[lane * kS + i] = load_word<T>(src, pitch, y0 + i, xl, H, W, false, true, flip);
     }
     __syncwarp();
 #pragma unroll
     for (int i = 0; i < 32; ++i) {
-      M[i] = B.xp[lane * 33 + i];
-      O[i] = B.mh[lane * 33 + i];
+      M[i] = B.xp[lane * kS + i];
+      O[i] = B.mh[lane * kS + i];
     }
     __syncwarp();
   }
@@ -493,8 +516,9 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   // any_change: did this visit change a stored value (the clamp to the mask on load counts).
   uint32_t any_change = 0;
 #pragma unroll
+  for (int i = 0; i < 32; i += 2) sts2(B.mv + lane * kS + i, M[i], M[i + 1]);
+#pragma unroll
   for (int i = 0; i < 32; ++i) {
-    B.mv[lane * 33 + i] = M[i];
     const uint32_t v = init_word<T>(O[i], M[i], y0 + i, xl, H, W, ring);
     any_change |= v ^ O[i];
     O[i] = v;
@@ -520,14 +544,13 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   if constexpr (E == 2) {
     const int q = lane & 15, half = lane >> 4;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const int l = 16 * half + (j >> 1);
-      const uint32_t m0 = B.mv[l * 33 + 2 * q], m1 = B.mv[l * 33 + 2 * q + 1];
-      B.mh[lane * 33 + j] = (j & 1) ? __byte_perm(m0, m1, 0x7632) : __byte_perm(m0, m1, 0x5410);
+    for (int j = 0; j < 32; j += 2) {
+      const uint2 m = lds2(B.mv + (16 * half + (j >> 1)) * kS + 2 * q);
+      sts2(B.mh + lane * kS + j, __byte_perm(m.x, m.y, 0x5410), __byte_perm(m.x, m.y, 0x7632));
     }
   } else {
 #pragma unroll
-    for (int j = 0; j < 32; ++j) B.mh[lane * 33 + j] = B.mv[j * 33 + lane];
+    for (int j = 0; j < 32; ++j) B.mh[lane * kS + j] = B.mv[j * kS + lane];
   }
   __syncwarp();
 
@@ -569,10 +592,10 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
       for (int i = 0; i < 32; ++i) fast_store<T>(sp + i * pitch, O[i], fx, pairs);
     } else {
 #pragma unroll
-      for (int i = 0; i < 32; ++i) B.xp[lane * 33 + i] = O[i];
+      for (int i = 0; i < 32; ++i) B.xp[lane * kS + i] = O[i];
       __syncwarp();
 #pragma unroll 1
-      for (int i = 0; i < 32; ++i) store_word<T>(out, pitch, y0 + i, xl, H, W, B.xp[lane * 33 + i], false, flip);
+      for (int i = 0; i < 32; ++i) store_word<T>(out, pitch, y0 + i, xl, H, W, B.xp[lane * kS + i], false, flip);
       __syncwarp();
     }
   }
