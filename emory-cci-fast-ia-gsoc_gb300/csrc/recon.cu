@@ -681,7 +681,7 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
     // one copy of the sweep code)
     if (lane == 0) {
       if (atomicCAS(&a.c.state[t], kRunning, kIdle) == kRunning) {
-        atomicSub(a.c.pending, 1);
+        pending_release(a.c);
       } else {
         atomicExch(&a.c.state[t], kQueued);
         atomicAdd(&a.c.stats[2], 1);
@@ -694,7 +694,7 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   int st = 0;
   if (lane == 0) {
     if (atomicCAS(&a.c.state[t], kRunning, kIdle) == kRunning) {
-      atomicSub(a.c.pending, 1);
+      pending_release(a.c);
       st = 0;
     } else if (round < a.resweeps) {
       atomicExch(&a.c.state[t], kRunning);
@@ -806,10 +806,13 @@ __global__ void recon_init_kernel(Ctl c, Imgs I, int ntiles, int order) {
   }
 }
 
-// Workspace layout (ints): [0] status, [1..4] stats (visits, sweeps, re-runs, re-sweeps), [6..7] visit
-// counter (64-bit), [8] head, [9] tail, [10] pending, [16..31] phase timers (8 x 64-bit);
-// from int kHdrInts: state[ntiles], then the ring (2 ints per slot, cap slots).
-constexpr int kHdrInts = 64;
+// Workspace layout (ints): [0] status, [1..4] stats (visits, sweeps, re-runs, re-sweeps),
+// [5] profiler visit index, [6..7] visit counter (64-bit), [32] head, [64] tail, [96] pending,
+// [128] done flag, [160..175] phase timers (8 x 64-bit); from int kHdrInts: state[ntiles],
+// then the ring (2 ints per slot, cap slots).  Head, tail, pending and the done flag sit on
+// separate 128-byte lines: the atomics of the working warps and the polls of the waiting
+// ones then do not queue behind one another.
+constexpr int kHdrInts = 192;
 
 template <typename T>
 int tiles_x_for(int64_t W) { return (int)((W + 32 * Px<T>::E - 1) / (32 * Px<T>::E)); }
@@ -841,10 +844,11 @@ cudaError_t launch_typed(const Imgs& I, int ntiles, bool erode, bool ring, void*
   a.c.status = wi + 0;
   a.c.stats = wi + 1;
   a.c.visit_count = (unsigned long long*)(wi + 6);
-  a.c.prof = (unsigned long long*)(wi + 16);
-  a.c.head = (unsigned*)(wi + 8);
-  a.c.tail = (unsigned*)(wi + 9);
-  a.c.pending = wi + 10;
+  a.c.prof = (unsigned long long*)(wi + 160);
+  a.c.head = (unsigned*)(wi + 32);
+  a.c.tail = (unsigned*)(wi + 64);
+  a.c.pending = wi + 96;
+  a.c.done = wi + 128;
   a.c.state = wi + kHdrInts;
   a.c.cap = ring_cap(ntiles);
   a.c.slots = (Slot*)(a.c.state + ((ntiles + 1) & ~1));

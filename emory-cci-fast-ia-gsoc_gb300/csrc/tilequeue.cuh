@@ -26,6 +26,7 @@ struct Ctl {
   unsigned* head;     // consumer ticket counter
   unsigned* tail;     // producer ticket counter
   int* pending;       // queued + running tiles
+  int* done;          // set once pending reaches zero
   int* status;
   int* stats;         // [0] visits, [1] sweeps, [2] re-runs
   unsigned long long* visit_count;  // budget counter
@@ -57,27 +58,37 @@ __device__ __forceinline__ bool queue_push(const Ctl& c, int t) {
   return true;
 }
 
-// Consumer side: claim a ticket and wait for its item; returns -1 when no tile is queued or
-// running any more (pending == 0: nothing can be pushed again) or after an error.
+// Consumer side: claim a ticket and wait for its item; returns -1 once no tile is queued or
+// running any more (the done flag: nothing can be pushed again) or after an error.  A waiting
+// warp polls its own slot; the done flag only every fourth wait and the status word every 64th,
+// so that idle warps do not flood the L2 lines that the working warps' atomics use.
 __device__ __forceinline__ int queue_pop(const Ctl& c) {
   const unsigned tk = atomicAdd(c.head, 1u);
   Slot* sl = &c.slots[tk & (c.cap - 1)];
   long long spins = 0;
-  unsigned ns = 32;
+  unsigned ns = 64;
   for (;;) {
     if (ld_acquire_u(&sl->seq) == tk + 1u) {
       const int t = *(volatile int*)&sl->val;
       st_release_u(&sl->seq, tk + c.cap);
       return t;
     }
-    if (ld_acquire(c.pending) == 0 || ld_relaxed(c.status) != 0) return -1;
-    if (++spins > kSpinLimit) {
+    ++spins;
+    if ((spins & 3) == 0 && ld_relaxed(c.done) != 0) return -1;
+    if ((spins & 63) == 0 && ld_relaxed(c.status) != 0) return -1;
+    if (spins > kSpinLimit) {
       set_status(c.status, kDevTimeout);
       return -1;
     }
     __nanosleep(ns);
     if (ns < 1024) ns <<= 1;
   }
+}
+
+// Release of a running or queued tile from the pending count; the call that takes it to zero
+// raises the done flag.
+__device__ __forceinline__ void pending_release(const Ctl& c) {
+  if (atomicSub(c.pending, 1) == 1) atomicExch(c.done, 1);
 }
 
 // A neighbour's values may have become stale: make sure it (re)reads them.  The common case
