@@ -419,12 +419,17 @@ int flat_grid(int64_t n);
 // Grid for kernels that walk a device-side list whose length (unknown on the host) is at most
 // max_items.
 int list_grid(int64_t max_items);
-// Row grids: x covers the widest image (256 columns per block), y strides the rows.
+// Row grids: x covers the widest image (256 columns, or 256 quads of columns, per block), y
+// strides the rows (one block row per image row up to the grid limit: batched kernels look
+// the image of a row up per row, so they want many short row walks).
+inline unsigned row_blocks(int total_rows) { return (unsigned)(total_rows < 65535 ? total_rows : 65535); }
 inline dim3 rowcol_grid(int total_rows, int max_w) {
-  return dim3((max_w + 255) / 256, (unsigned)(total_rows < 65535 ? total_rows : 65535));
+  const unsigned bx = (unsigned)((max_w + 255) / 256);
+  return dim3(bx, row_blocks(total_rows));
 }
 inline dim3 quadrow_grid(int total_rows, int max_w) {
-  return dim3((max_w / 4 + 256) / 256, (unsigned)(total_rows < 65535 ? total_rows : 65535));
+  const unsigned bx = (unsigned)(((max_w + 3) / 4 + 255) / 256);
+  return dim3(bx, row_blocks(total_rows));
 }
 
 // Labels every image of the batch: local pass, edge merge, root flattening.  Afterwards

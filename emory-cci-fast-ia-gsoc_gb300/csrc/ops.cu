@@ -145,7 +145,8 @@ __global__ void fill_out_kernel(Imgs I, int total_rows, const int* __restrict__ 
     ccl::roots4_ro(L, gi, n, r);
     uint8_t f[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) f[k] = (r[k] >= 0 && ccl::test_bit(bits, r[k])) ? 0 : (uint8_t)fg;
+    for (int k = 0; k < 4; ++k)
+      f[k] = (k > 0 && r[k] == r[k - 1]) ? f[k - 1] : ((r[k] >= 0 && ccl::test_bit(bits, r[k])) ? 0 : (uint8_t)fg);
     if (F) store4_u8(F + gi, n, f);
     TO* o = nullptr;
     if (!I.d) o = out ? pxp<TO>(out, pitch_out, y, x) : nullptr;
@@ -325,9 +326,7 @@ __global__ void invert_kernel(const T* in, T* out, int64_t pitch, int H, int W) 
   }
 }
 
-inline dim3 quad_grid(int64_t rows, int64_t cols) {
-  return dim3((unsigned)((cols / 4 + 1 + 255) / 256), (unsigned)(rows < 65535 ? rows : 65535));
-}
+inline dim3 quad_grid(int64_t rows, int64_t cols) { return ccl::quadrow_grid((int)rows, (int)cols); }
 
 // Hole-filling marker: the image on the border, max<T> inside.
 template <typename T>

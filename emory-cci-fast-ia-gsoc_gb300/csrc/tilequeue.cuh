@@ -60,7 +60,7 @@ __device__ __forceinline__ bool queue_push(const Ctl& c, int t) {
 
 // Consumer side: claim a ticket and wait for its item; returns -1 once no tile is queued or
 // running any more (the done flag: nothing can be pushed again) or after an error.  A waiting
-// warp polls its own slot; the done flag only every fourth wait and the status word every 64th,
+// warp polls its own slot; the done flag only every second wait and the status word every 64th,
 // so that idle warps do not flood the L2 lines that the working warps' atomics use.
 __device__ __forceinline__ int queue_pop(const Ctl& c) {
   const unsigned tk = atomicAdd(c.head, 1u);
@@ -74,14 +74,14 @@ __device__ __forceinline__ int queue_pop(const Ctl& c) {
       return t;
     }
     ++spins;
-    if ((spins & 3) == 0 && ld_relaxed(c.done) != 0) return -1;
+    if ((spins & 1) == 0 && ld_relaxed(c.done) != 0) return -1;
     if ((spins & 63) == 0 && ld_relaxed(c.status) != 0) return -1;
     if (spins > kSpinLimit) {
       set_status(c.status, kDevTimeout);
       return -1;
     }
     __nanosleep(ns);
-    if (ns < 1024) ns <<= 1;
+    if (ns < 512) ns <<= 1;
   }
 }
 
