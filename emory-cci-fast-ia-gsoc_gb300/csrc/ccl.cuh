@@ -160,6 +160,8 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
   __shared__ int s_lab[kTile * kTile];
   __shared__ int s_cnt[kTile * kTile];
   __shared__ CT s_c[kTile * kTile];
+  __shared__ int s_wu[kThreads / 32];  // per warp: its four rows hold one class only
+  __shared__ CT s_wv[kThreads / 32];   // ... and that class
   const TileAt T = tile_at(I, blockIdx.x);
   const int x0 = T.x0, y0 = T.y0, H = T.m.H, W = T.m.W, pb = T.m.px_base;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -183,7 +185,37 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
     const int rs = 31 - __clz(starts);
     s_lab[i] = c[k] ? ly * kTile + rs : -1;
   }
+  {
+    const CT ref = (CT)__shfl_sync(NSGB_FULL, (uint32_t)c[0], 0);
+    const bool wu = __all_sync(NSGB_FULL, c[0] == ref && c[1] == ref && c[2] == ref && c[3] == ref);
+    if (tx == 0) {
+      s_wu[ty] = wu;
+      s_wv[ty] = ref;
+    }
+  }
   __syncthreads();
+  // Uniform tile (one class everywhere, pixels outside the image counting as background): the
+  // whole tile is one component rooted at its first pixel, or background.  Common in masks
+  // (empty background, solid foreground), and it needs no unions.
+  {
+    bool uni = true;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) uni = uni && s_wu[w] && s_wv[w] == s_wv[0];
+    if (uni) {
+      const bool fg = s_wv[0] != 0;
+      const int g0 = pb + y0 * W + x0;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int gy = y0 + 4 * ty + k, gx = x0 + tx;
+        if (gy < H && gx < W) f.L[pb + gy * W + gx] = fg ? g0 : -1;
+      }
+      if (fg && threadIdx.x == 0) {
+        f.roots[atomicAdd(f.nroots, 1)] = g0;
+        if (f.A) f.A[g0] = kTile * kTile;
+      }
+      return;
+    }
+  }
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int ly = 4 * ty + k, i = ly * kTile + tx;
