@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
     const int gy = y0 + ly, gx = x0 + tx;
     c[k] = (CT)((gy < H && gx < W) ? cls(T.m, gy, gx) : 0u);
     s_c[i] = c[k];
-    s_cnt[i] = 0;
+    if (f.A) s_cnt[i] = 0;
   }
   unsigned same_left[4];
 #pragma unroll
@@ -320,8 +320,11 @@ __global__ void __launch_bounds__(64) ccl_merge(Cls cls, Imgs I, int* __restrict
   if (cb == 0) return;
   const int qb = pb + by * W + bx;
   if (ca == cb && (a_start || b_start)) g_union(L, qb, pb + ay * W + ax);
-  if (CONN == 8) {
-    // diagonal partners one step before the start / after the end of the far-side run
+  // Diagonal partners one step before the start / after the end of the far-side run.  When
+  // the near pixel at this lane has the far run's class, the partner (its neighbour along the
+  // edge) is joined to it by the near tile's own labelling or by the next tile's edge merge,
+  // and the near pixel is joined to the far run here: the diagonal union adds nothing.
+  if (CONN == 8 && ca != cb) {
     if (b_start) {
       const int dy = bottom ? ay : ay - 1, dx = bottom ? ax - 1 : ax;
       if (dy >= 0 && dx >= 0 && dy < H && dx < W && cls(T.m, dy, dx) == cb) g_union(L, qb, pb + dy * W + dx);
