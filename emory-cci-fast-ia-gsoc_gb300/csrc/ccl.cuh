@@ -32,7 +32,8 @@ namespace nsgb {
 namespace ccl {
 
 constexpr int kTile = 32;      // tile edge (pixels)
-constexpr int kThreads = 256;  // 32 x 8 threads, 4 rows each
+constexpr int kThreads = 256;            // threads per labelling tile (32 columns x 8 warps)
+constexpr int kRows = kTile / (kThreads / 32);  // tile rows per thread (consecutive)
 
 // Root of x in a shared-memory forest, halving the path on the way (every node on it is
 // re-pointed to its grandparent; a concurrent hook of a root is never overwritten because
@@ -67,12 +68,16 @@ __device__ __forceinline__ void s_union(int* s, int a, int b) {
 // Root of x in the global forest with path halving.  The halving write is an atomicMin: a
 // parent link only ever moves to a smaller index (an ancestor), so it can never undo another
 // thread's write of the root itself (the smallest index on the path).
+// A background entry (-1) on the path means the forest is inconsistent with the classifier
+// (never in a correct labelling); the walk then stops with -1 instead of reading before L.
 __device__ __forceinline__ int g_find(int* L, int x) {
   for (;;) {
     const int p = ld_relaxed(L + x);
     if (p == x) return x;
+    if (p < 0) return -1;
     const int g = ld_relaxed(L + p);
     if (g == p) return p;
+    if (g < 0) return -1;
     atomicMin(L + x, g);
     x = g;
   }
@@ -82,7 +87,7 @@ __device__ __forceinline__ void g_union(int* L, int a, int b) {
   for (;;) {
     a = g_find(L, a);
     b = g_find(L, b);
-    if (a == b) return;
+    if (a == b || a < 0 || b < 0) return;
     if (a < b) {
       const int t = a;
       a = b;
@@ -146,7 +151,7 @@ struct class_type<Cls, std::void_t<typename Cls::class_t>> {
   using type = typename Cls::class_t;
 };
 
-// Each warp owns four consecutive tile rows (lane = column) and joins them top-down, so a
+// Each warp owns kRows consecutive tile rows (lane = column) and joins them top-down, so a
 // row's runs hook straight onto the root already found for the row above; only the four
 // warps' blocks meet concurrently, which keeps the trees (and every later find) shallow.  Runs of equal class along a row are found with a
 // ballot and start out joined (label = run start), so unions are only needed where runs of
@@ -160,24 +165,24 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
   __shared__ int s_lab[kTile * kTile];
   __shared__ int s_cnt[kTile * kTile];
   __shared__ CT s_c[kTile * kTile];
-  __shared__ int s_wu[kThreads / 32];  // per warp: its four rows hold one class only
+  __shared__ int s_wu[kThreads / 32];  // per warp: its rows hold one class only
   __shared__ CT s_wv[kThreads / 32];   // ... and that class
   const TileAt T = tile_at(I, blockIdx.x);
   const int x0 = T.x0, y0 = T.y0, H = T.m.H, W = T.m.W, pb = T.m.px_base;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  CT c[4];
+  CT c[kRows];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int ly = 4 * ty + k, i = ly * kTile + tx;
+  for (int k = 0; k < kRows; ++k) {
+    const int ly = kRows * ty + k, i = ly * kTile + tx;
     const int gy = y0 + ly, gx = x0 + tx;
     c[k] = (CT)((gy < H && gx < W) ? cls(T.m, gy, gx) : 0u);
     s_c[i] = c[k];
     if (f.A) s_cnt[i] = 0;
   }
-  unsigned same_left[4];
+  unsigned same_left[kRows];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int ly = 4 * ty + k, i = ly * kTile + tx;
+  for (int k = 0; k < kRows; ++k) {
+    const int ly = kRows * ty + k, i = ly * kTile + tx;
     const CT left = (CT)__shfl_up_sync(NSGB_FULL, (uint32_t)c[k], 1);
     same_left[k] = __ballot_sync(NSGB_FULL, tx > 0 && c[k] != 0 && left == c[k]);
     // run start: highest lane <= tx whose pixel does not continue a run from the left
@@ -187,7 +192,10 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
   }
   {
     const CT ref = (CT)__shfl_sync(NSGB_FULL, (uint32_t)c[0], 0);
-    const bool wu = __all_sync(NSGB_FULL, c[0] == ref && c[1] == ref && c[2] == ref && c[3] == ref);
+    bool same = true;
+#pragma unroll
+    for (int k = 0; k < kRows; ++k) same = same && c[k] == ref;
+    const bool wu = __all_sync(NSGB_FULL, same);
     if (tx == 0) {
       s_wu[ty] = wu;
       s_wv[ty] = ref;
@@ -205,8 +213,8 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
       const bool fg = s_wv[0] != 0;
       const int g0 = pb + y0 * W + x0;
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int gy = y0 + 4 * ty + k, gx = x0 + tx;
+      for (int k = 0; k < kRows; ++k) {
+        const int gy = y0 + kRows * ty + k, gx = x0 + tx;
         if (gy < H && gx < W) f.L[pb + gy * W + gx] = fg ? g0 : -1;
       }
       if (fg && threadIdx.x == 0) {
@@ -217,8 +225,8 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
     }
   }
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int ly = 4 * ty + k, i = ly * kTile + tx;
+  for (int k = 0; k < kRows; ++k) {
+    const int ly = kRows * ty + k, i = ly * kTile + tx;
     const CT v = c[k];
     if (!v || ly == 0) continue;
     const bool run_start = !((same_left[k] >> tx) & 1u);
@@ -233,26 +241,26 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
     }
   }
   __syncthreads();
-  int root[4];
+  int root[kRows];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int ly = 4 * ty + k, i = ly * kTile + tx;
+  for (int k = 0; k < kRows; ++k) {
+    const int ly = kRows * ty + k, i = ly * kTile + tx;
     root[k] = c[k] ? s_find(s_lab, i) : -1;
   }
   if (f.A) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < kRows; ++k) {
       const int r = root[k];
       const unsigned peers = __match_any_sync(NSGB_FULL, r);
       if (r >= 0 && (__ffs(peers) - 1) == tx) atomicAdd(&s_cnt[r], __popc(peers));
     }
     __syncthreads();
   }
-  unsigned rb[4];
+  unsigned rb[kRows];
   int nr = 0;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int ly = 4 * ty + k, i = ly * kTile + tx;
+  for (int k = 0; k < kRows; ++k) {
+    const int ly = kRows * ty + k, i = ly * kTile + tx;
     const int gy = y0 + ly, gx = x0 + tx;
     const bool in = gy < H && gx < W;
     const int r = root[k];
@@ -268,9 +276,9 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
   if (tx == 0) base = atomicAdd(f.nroots, nr);
   base = __shfl_sync(NSGB_FULL, base, 0);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < kRows; ++k) {
     if ((rb[k] >> tx) & 1u) {
-      const int ly = 4 * ty + k, i = ly * kTile + tx;
+      const int ly = kRows * ty + k, i = ly * kTile + tx;
       const int g = pb + (y0 + ly) * W + x0 + tx;
       f.roots[base + __popc(rb[k] & ((1u << tx) - 1u))] = g;
       if (f.A) f.A[g] = s_cnt[i];
@@ -352,7 +360,7 @@ static __global__ void ccl_flatten_roots(Forest f, int max_roots) {
     for (int j = 0; j < 4; ++j) {
       if (lr[j] < 0 || p[j] == lr[j]) continue;
       const int r = g_find(f.L, lr[j]);
-      if (r != lr[j]) {
+      if (r >= 0 && r != lr[j]) {
         atomicMin(f.L + lr[j], r);
         if (f.A) atomicAdd(f.A + r, __ldcg(f.A + lr[j]));
       }
