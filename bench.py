@@ -10,7 +10,8 @@ One step = one pass of the chain over the tile.  `value` is the whole-job throug
 MPix/s with inputs already resident in HBM (marker reset and L2 flushed outside the timed
 events before every step); `e2e` is the same chain through the C ABI with host buffers,
 host->device copies of marker and mask and device->host copies of labels and the area mask
-inside the timed region.  `--impl reference` times the reference's CPU algorithm (the
+inside the timed region (steps alternate between two streams with their own buffers, so the
+copies of one step overlap the kernels of the other).  `--impl reference` times the reference's CPU algorithm (the
 oracle port in oracle/, or the reference's own code where it was compiled) on all host cores.
 
 Multi-GPU (torchrun, one process per GPU): the path does not shard a single tile, so every
@@ -302,29 +303,52 @@ def run_nsgb(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms, rms = float(t[0]), float(t[1])
 
-    # End to end through the C ABI with host buffers.
+    # End to end through the C ABI with host buffers.  Every step copies its marker and mask in
+    # from pinned host memory, runs the chain and copies its labels and area mask out.  Steps
+    # alternate between two streams, each with its own device buffers and workspace, so the
+    # copies of one step overlap the kernels of the other (the way a caller streams tiles).
     pin_marker = torch.from_numpy(marker_h).pin_memory()
     pin_mask = torch.from_numpy(mask_h).pin_memory()
-    pin_labels = torch.empty((H, W), dtype=torch.int32).pin_memory()
-    pin_area = torch.empty((H, W), dtype=torch.uint8).pin_memory()
     e2e_opts = _ffi.Opts(0, 0, 0)
+    lanes = []
+    for j in range(2):
+        st_j = torch.cuda.Stream(dev)
+        ws_j = torch.empty(ws_bytes + 256, dtype=torch.uint8, device=dev)
+        lanes.append({
+            "stream": st_j, "sp": C.c_void_p(st_j.cuda_stream),
+            "work": torch.empty_like(marker_src), "mask": torch.empty_like(mask),
+            "fill": torch.empty_like(fill), "labels": torch.empty_like(labels), "area": torch.empty_like(area),
+            "ws_t": ws_j, "ws": (ws_j.data_ptr() + 255) & ~255,
+            "pin_labels": torch.empty((H, W), dtype=torch.int32).pin_memory(),
+            "pin_area": torch.empty((H, W), dtype=torch.uint8).pin_memory(),
+        })
 
-    def e2e_step():
-        work.copy_(pin_marker, non_blocking=True)
-        mask.copy_(pin_mask, non_blocking=True)
-        chain_call(e2e_opts)
-        pin_labels.copy_(labels, non_blocking=True)
-        pin_area.copy_(area, non_blocking=True)
+    def e2e_step(i):
+        ln = lanes[i % 2]
+        with torch.cuda.stream(ln["stream"]):
+            ln["work"].copy_(pin_marker, non_blocking=True)
+            ln["mask"].copy_(pin_mask, non_blocking=True)
+            st = lib.nsgb_chain(_ffi.U8, ln["work"].data_ptr(), ln["mask"].data_ptr(), H, W, W, 8, 128.0, 4, 8, 11,
+                                1000, ln["fill"].data_ptr(), ln["labels"].data_ptr(), ln["area"].data_ptr(), None,
+                                None, ln["ws"], ws_bytes, ln["sp"], C.byref(e2e_opts))
+            if st != 0:
+                raise RuntimeError(f"nsgb_chain: {_ffi.STATUS.get(st, st)}")
+            ln["pin_labels"].copy_(ln["labels"], non_blocking=True)
+            ln["pin_area"].copy_(ln["area"], non_blocking=True)
 
-    for _ in range(3):
-        e2e_step()
+    for i in range(4):
+        e2e_step(i)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if dist:
         dist.barrier()
     e0.record(stream)
-    for _ in range(args.e2e_steps):
-        e2e_step()
+    for ln in lanes:
+        ln["stream"].wait_event(e0)
+    for i in range(args.e2e_steps):
+        e2e_step(i)
+    for ln in lanes:
+        stream.wait_stream(ln["stream"])
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / args.e2e_steps
@@ -333,8 +357,9 @@ def run_nsgb(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t[0])
     # the e2e outputs are the chain's results: spot-check them against the device-resident run
-    if not torch.equal(pin_labels.to(dev), labels):
-        raise RuntimeError("e2e labels differ from the device-resident run")
+    for ln in lanes:
+        if not torch.equal(ln["pin_labels"].to(dev), labels) or not torch.equal(ln["pin_area"].to(dev), area):
+            raise RuntimeError("e2e outputs differ from the device-resident run")
 
     peak, peak_kind = read_peaks()
     achieved = RECON_BYTES_PER_PX * n_px / (rms / 1e3) / 1e9
@@ -379,7 +404,8 @@ def run_nsgb(args):
             "h2d_bytes_per_step": 2 * n_px,
             "d2h_bytes_per_step": 5 * n_px,
             "ms_per_step": e2e_ms,
-            "path": "nsgb_chain C ABI, pinned host marker/mask in, labels + area mask out",
+            "path": "nsgb_chain C ABI, pinned host marker/mask in, labels + area mask out; steps alternate "
+                    "between two streams with their own buffers, so one step's copies overlap the other's kernels",
         },
         "gpu_launches": KERNELS_PER_CHAIN * args.steps,
         "clocks": clk,
