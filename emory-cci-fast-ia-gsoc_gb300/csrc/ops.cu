@@ -136,24 +136,17 @@ __device__ __forceinline__ void store4_i32(int32_t* p, int n, const int (&v)[4])
   }
 }
 
-// `cls` is the classifier of the labelling: a quad without a pixel of the labelled class is
-// foreground whole, and its labels are not read.
-template <typename TO, class Cls>
+template <typename TO>
 __global__ void fill_out_kernel(Imgs I, int total_rows, const int* __restrict__ L, const unsigned* __restrict__ bits,
-                                uint8_t* F, TO* out, int64_t pitch_out, TO fg, Cls cls) {
+                                uint8_t* F, TO* out, int64_t pitch_out, TO fg) {
   ccl::for_batch_quads(I, total_rows, [&](const Img& m, int y, int x, int n) {
     const int64_t gi = (int64_t)m.px_base + (int64_t)y * m.W + x;
-    bool any = false;
+    int r[4];
+    ccl::roots4_ro(L, gi, n, r);
+    uint8_t f[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) any = any || (k < n && cls(m, y, x + k) != 0u);
-    uint8_t f[4] = {(uint8_t)fg, (uint8_t)fg, (uint8_t)fg, (uint8_t)fg};
-    if (any) {
-      int r[4];
-      ccl::roots4_ro(L, gi, n, r);
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-        f[k] = (k > 0 && r[k] == r[k - 1]) ? f[k - 1] : ((r[k] >= 0 && ccl::test_bit(bits, r[k])) ? 0 : (uint8_t)fg);
-    }
+    for (int k = 0; k < 4; ++k)
+      f[k] = (k > 0 && r[k] == r[k - 1]) ? f[k - 1] : ((r[k] >= 0 && ccl::test_bit(bits, r[k])) ? 0 : (uint8_t)fg);
     if (F) store4_u8(F + gi, n, f);
     TO* o = nullptr;
     if (!I.d) o = out ? pxp<TO>(out, pitch_out, y, x) : nullptr;
@@ -536,7 +529,7 @@ cudaError_t chain_impl(int dtype, const Plan& P, const Ws& w, int recon_conn, do
       ccl::ccl_seed_border<SeedBorder<ClsNotAbove<T>>><<<dim3(gx, t.n), 256, 0, s>>>(
           P.I, w.L, SeedBorder<ClsNotAbove<T>>{cls}, w.bits);
       fill_out_kernel<uint8_t><<<qrb(t), 256, 0, s>>>(P.I, t.rows, w.L, w.bits, w.F, fill_out,
-                                                      P.I.d ? 0 : (int64_t)P.I.one.W, (uint8_t)255, cls);
+                                                      P.I.d ? 0 : (int64_t)P.I.one.W, (uint8_t)255);
       return cudaGetLastError();
     });
   }
@@ -708,7 +701,7 @@ nsgb_status nsgb_imfill_holes(int dtype, const void* image, void* out, int64_t r
         ccl::ccl_seed_border<SeedBorder<ClsNotMax<T>>><<<dim3(grid1d(2 * (rows + cols)), 1), 256, 0, s>>>(
             P.I, w.L, SeedBorder<ClsNotMax<T>>{cls}, w.bits);
         fill_out_kernel<T><<<qr(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.bits, nullptr, (T*)out, pitch,
-                                                          std::numeric_limits<T>::max(), cls);
+                                                          std::numeric_limits<T>::max());
         return cudaGetLastError();
       });
     }
