@@ -56,6 +56,9 @@ def parse_args():
     p.add_argument("--batch-steps", type=int, default=5)
     p.add_argument("--batch-dtypes", default="u8,u16,i32")
     p.add_argument("--no-batch", action="store_true")
+    p.add_argument("--batch-only", action="store_true",
+                   help="profiling aid: only the batched chain replays (no per-tile loop, no headline); "
+                        "prints the batched section alone")
     p.add_argument("--no-grad", action="store_true")
     p.add_argument("--no-large", action="store_true")
     p.add_argument("--large-size", type=int, default=16384)
@@ -206,6 +209,9 @@ def run_nsgb(args):
 
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
+    if args.batch_only:
+        print(json.dumps({"batched": batched_section(args, torch.device("cuda", local))}))
+        return 0
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -561,6 +567,10 @@ def run_batched(args, dev, tiles_u8, dtype):
         return statistics.mean(res)
 
     steps, warm = args.batch_steps, 3
+    mp = total_px / 1e6
+    if args.batch_only:
+        t_batch = timed(graph.replay, steps, warm)
+        return {"batched_graph_mpix_s": mp / (t_batch / 1e3), "batched_ms": t_batch}
     t_plain = timed(lambda: plain(True), steps, warm)
     t_plain_async = timed(lambda: plain(False), steps, warm)
     plain(True)  # leave the plain outputs of an exact run (work restored by the last timed step)
@@ -575,7 +585,6 @@ def run_batched(args, dev, tiles_u8, dtype):
     bc = counts.view(n, 2).tolist()
     same = (all(tuple(x) == y for x, y in zip(bc, pc)) and torch.equal(bf.buf, fo.buf) and torch.equal(bl.buf, lo.buf)
             and torch.equal(ba.buf, ao.buf))
-    mp = total_px / 1e6
     return {
         "plain_mpix_s": mp / (t_plain / 1e3), "plain_ms": t_plain,
         "plain_async_mpix_s": mp / (t_plain_async / 1e3), "plain_async_ms": t_plain_async,

@@ -165,8 +165,7 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
   __shared__ int s_lab[kTile * kTile];
   __shared__ int s_cnt[kTile * kTile];
   __shared__ CT s_c[kTile * kTile];
-  __shared__ int s_wu[kThreads / 32];  // per warp: its rows hold one class only
-  __shared__ CT s_wv[kThreads / 32];   // ... and that class
+  __shared__ CT s_wv[kThreads / 32];  // per warp: the class of its first pixel
   const TileAt T = tile_at(I, blockIdx.x);
   const int x0 = T.x0, y0 = T.y0, H = T.m.H, W = T.m.W, pb = T.m.px_base;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -179,36 +178,41 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
     s_c[i] = c[k];
     if (f.A) s_cnt[i] = 0;
   }
+  // Uniform warp (one class in all its rows): one run per row, or none; no ballots needed.
+  const CT ref = (CT)__shfl_sync(NSGB_FULL, (uint32_t)c[0], 0);
+  bool same = true;
+#pragma unroll
+  for (int k = 0; k < kRows; ++k) same = same && c[k] == ref;
+  const bool wu = __all_sync(NSGB_FULL, same);
+  if (tx == 0) s_wv[ty] = ref;
   unsigned same_left[kRows];
+  if (wu) {
 #pragma unroll
-  for (int k = 0; k < kRows; ++k) {
-    const int ly = kRows * ty + k, i = ly * kTile + tx;
-    const CT left = (CT)__shfl_up_sync(NSGB_FULL, (uint32_t)c[k], 1);
-    same_left[k] = __ballot_sync(NSGB_FULL, tx > 0 && c[k] != 0 && left == c[k]);
-    // run start: highest lane <= tx whose pixel does not continue a run from the left
-    const unsigned starts = ~same_left[k] & (0xFFFFFFFFu >> (31 - tx));
-    const int rs = 31 - __clz(starts);
-    s_lab[i] = c[k] ? ly * kTile + rs : -1;
-  }
-  {
-    const CT ref = (CT)__shfl_sync(NSGB_FULL, (uint32_t)c[0], 0);
-    bool same = true;
+    for (int k = 0; k < kRows; ++k) {
+      const int ly = kRows * ty + k;
+      same_left[k] = ref ? 0xFFFFFFFEu : 0u;
+      s_lab[ly * kTile + tx] = ref ? ly * kTile : -1;
+    }
+  } else {
 #pragma unroll
-    for (int k = 0; k < kRows; ++k) same = same && c[k] == ref;
-    const bool wu = __all_sync(NSGB_FULL, same);
-    if (tx == 0) {
-      s_wu[ty] = wu;
-      s_wv[ty] = ref;
+    for (int k = 0; k < kRows; ++k) {
+      const int ly = kRows * ty + k, i = ly * kTile + tx;
+      const CT left = (CT)__shfl_up_sync(NSGB_FULL, (uint32_t)c[k], 1);
+      same_left[k] = __ballot_sync(NSGB_FULL, tx > 0 && c[k] != 0 && left == c[k]);
+      // run start: highest lane <= tx whose pixel does not continue a run from the left
+      const unsigned starts = ~same_left[k] & (0xFFFFFFFFu >> (31 - tx));
+      const int rs = 31 - __clz(starts);
+      s_lab[i] = c[k] ? ly * kTile + rs : -1;
     }
   }
-  __syncthreads();
+  const bool all_wu = __syncthreads_and(wu) != 0;
   // Uniform tile (one class everywhere, pixels outside the image counting as background): the
   // whole tile is one component rooted at its first pixel, or background.  Common in masks
   // (empty background, solid foreground), and it needs no unions.
-  {
+  if (all_wu) {
     bool uni = true;
 #pragma unroll
-    for (int w = 0; w < kThreads / 32; ++w) uni = uni && s_wu[w] && s_wv[w] == s_wv[0];
+    for (int w = 1; w < kThreads / 32; ++w) uni = uni && s_wv[w] == s_wv[0];
     if (uni) {
       const bool fg = s_wv[0] != 0;
       const int g0 = pb + y0 * W + x0;

@@ -186,8 +186,10 @@ __global__ void bwselect_out_kernel(Imgs I, int total_rows, void* out, const int
 // Optional area-filter outputs from the same pass.  rank / A are read-only here: L1-cached
 // loads, because a giant component's root is read by every one of its pixels.  Single image:
 // explicit output pointers / pitches; batch: Img::labels / Img::area (dense).
+// RELABEL: raster rank labels (else root indices); AREA: area-filter outputs (A non-null).
+template <bool RELABEL, bool AREA>
 __global__ void label_out_kernel(Imgs I, int total_rows, const int* __restrict__ L, const int* __restrict__ rank,
-                                 int relabel, int32_t* labels, int64_t pitch_labels, const int* __restrict__ A, int lo,
+                                 int32_t* labels, int64_t pitch_labels, const int* __restrict__ A, int lo,
                                  int hi, int32_t* kept_labels, int64_t pitch_kept, uint8_t* flat, int64_t pitch_flat) {
   ccl::for_batch_quads(I, total_rows, [&](const Img& m, int y, int x, int n) {
     int r[4], lab[4], kl[4];
@@ -197,9 +199,9 @@ __global__ void label_out_kernel(Imgs I, int total_rows, const int* __restrict__
     for (int k = 0; k < 4; ++k) {
       const bool same = k > 0 && r[k] == r[k - 1];
       lab[k] = same ? lab[k - 1]
-                    : (relabel ? (r[k] < 0 ? 0 : __ldg(&rank[r[k]]) + 1) : (r[k] < 0 ? -1 : r[k] - m.px_base));
+                    : (RELABEL ? (r[k] < 0 ? 0 : __ldg(&rank[r[k]]) + 1) : (r[k] < 0 ? -1 : r[k] - m.px_base));
       bool keep = false;
-      if (A) {
+      if (AREA) {
         if (same) {
           keep = fl[k - 1] != 0;
         } else {
@@ -212,12 +214,12 @@ __global__ void label_out_kernel(Imgs I, int total_rows, const int* __restrict__
     }
     if (!I.d) {
       if (labels) store4_i32(pxp<int32_t>(labels, pitch_labels, y, x), n, lab);
-      if (A && kept_labels) store4_i32(pxp<int32_t>(kept_labels, pitch_kept, y, x), n, kl);
-      if (A && flat) store4_u8(pxp<uint8_t>(flat, pitch_flat, y, x), n, fl);
+      if (AREA && kept_labels) store4_i32(pxp<int32_t>(kept_labels, pitch_kept, y, x), n, kl);
+      if (AREA && flat) store4_u8(pxp<uint8_t>(flat, pitch_flat, y, x), n, fl);
     } else {
       const int64_t li = (int64_t)y * m.W + x;
       if (m.labels) store4_i32(m.labels + li, n, lab);
-      if (A && m.area) store4_u8(m.area + li, n, fl);
+      if (AREA && m.area) store4_u8(m.area + li, n, fl);
     }
   });
 }
@@ -537,8 +539,8 @@ cudaError_t chain_impl(int dtype, const Plan& P, const Ws& w, int recon_conn, do
   if (e == cudaSuccess) e = ccl::rank_roots(P.I, t, w.forest(true), area_min, area_max, w.R, w.bits, w.bits_bytes, w.tmp, w.wpre, w.counts, s);
   if (e == cudaSuccess) {
     const int64_t W1 = P.I.d ? 0 : P.I.one.W;
-    label_out_kernel<<<qrb(t), 256, 0, s>>>(P.I, t.rows, w.L, w.R, 1, labels_out, W1 * 4, w.A, area_min, area_max,
-                                            nullptr, 0, area_out, W1);
+    label_out_kernel<true, true><<<qrb(t), 256, 0, s>>>(P.I, t.rows, w.L, w.R, labels_out, W1 * 4, w.A, area_min,
+                                                        area_max, nullptr, 0, area_out, W1);
     e = cudaGetLastError();
   }
   return e;
@@ -789,8 +791,12 @@ nsgb_status nsgb_bwlabel(const uint8_t* bin, int32_t* labels, int64_t rows, int6
   e = ccl::label(ClsValueU8{}, P.I, P.t, conn, w.forest(false), s);
   if (e == cudaSuccess) e = ccl::rank_roots(P.I, P.t, w.forest(false), 0, 0, w.R, w.bits, w.bits_bytes, w.tmp, w.wpre, w.counts, s);
   if (e == cudaSuccess) {
-    label_out_kernel<<<qr(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.R, relabel, labels, pitch_labels, nullptr,
-                                                     0, 0, nullptr, 0, nullptr, 0);
+    if (relabel)
+      label_out_kernel<true, false><<<qr(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.R, labels, pitch_labels,
+                                                                   nullptr, 0, 0, nullptr, 0, nullptr, 0);
+    else
+      label_out_kernel<false, false><<<qr(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.R, labels, pitch_labels,
+                                                                    nullptr, 0, 0, nullptr, 0, nullptr, 0);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess && count) {
@@ -820,8 +826,9 @@ nsgb_status nsgb_bwareaopen(const void* in, int labeled, int32_t* labels_out, ui
     e = ccl::label(ClsValueU8{}, P.I, P.t, conn, w.forest(true), s);
     if (e == cudaSuccess) e = ccl::rank_roots(P.I, P.t, w.forest(true), min_size, max_size, w.R, w.bits, w.bits_bytes, w.tmp, w.wpre, w.counts, s);
     if (e == cudaSuccess) {
-      label_out_kernel<<<qr(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.R, 0, nullptr, 0, w.A, min_size, max_size,
-                                                       labels_out, pitch_labels, flat_out, pitch_flat);
+      label_out_kernel<false, true><<<qr(rows, cols), 256, 0, s>>>(P.I, P.t.rows, w.L, w.R, nullptr, 0, w.A, min_size,
+                                                                   max_size, labels_out, pitch_labels, flat_out,
+                                                                   pitch_flat);
       e = cudaGetLastError();
     }
     if (e == cudaSuccess && count) {
