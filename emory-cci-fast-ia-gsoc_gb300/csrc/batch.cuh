@@ -16,6 +16,7 @@ struct Img {
   int H, W;
   int aligned;        // plane / aux aligned for vector tile loads
   int r_tiles_x, r_tiles_y, r_tile_base;  // reconstruction tiles
+  int r_even_base;    // first of its checkerboard colour-0 tiles among all images' colour-0 tiles
   int c_tiles_x, c_tile_base;             // 32x32 labelling tiles
   int px_base;        // first pixel in the concatenated label planes
   int blk_base;       // first 1024-pixel rank block
@@ -52,12 +53,20 @@ struct CTileBase { __device__ int operator()(const Img& m) const { return m.c_ti
 struct BlkBase { __device__ int operator()(const Img& m) const { return m.blk_base; } };
 struct RowBase { __device__ int operator()(const Img& m) const { return m.row_base; } };
 struct PxBase { __device__ int operator()(const Img& m) const { return m.px_base; } };
+struct REvenBase { __device__ int operator()(const Img& m) const { return m.r_even_base; } };
+struct ROddBase { __device__ int operator()(const Img& m) const { return m.r_tile_base - m.r_even_base; } };
+
+// Reconstruction tiles of checkerboard colour 0 ((tile row + tile column) even) in an image.
+__host__ __device__ inline int even_tiles(int tiles_x, int tiles_y) {
+  return ((tiles_y + 1) / 2) * ((tiles_x + 1) / 2) + (tiles_y / 2) * (tiles_x / 2);
+}
 
 // Totals of a batch, known on the host (grid sizes).
 struct BatchTotals {
   int n;
   int64_t px;      // total pixels (< 2^31)
   int r_tiles;     // reconstruction tiles
+  int r_even;      // reconstruction tiles of checkerboard colour 0
   int c_tiles;     // labelling tiles
   int blocks;      // rank blocks
   int rows;        // total rows

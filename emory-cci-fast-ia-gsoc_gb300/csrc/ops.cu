@@ -375,12 +375,14 @@ void add_image(Img& m, BatchTotals& t) {
   m.c_tiles_x = (m.W + ccl::kTile - 1) / ccl::kTile;
   const int c_tiles_y = (m.H + ccl::kTile - 1) / ccl::kTile;
   m.r_tile_base = t.r_tiles;
+  m.r_even_base = t.r_even;
   m.c_tile_base = t.c_tiles;
   m.px_base = (int)t.px;
   m.blk_base = t.blocks;
   m.row_base = t.rows;
   const int64_t npx = (int64_t)m.H * m.W;
   t.r_tiles += m.r_tiles_x * m.r_tiles_y;
+  t.r_even += even_tiles(m.r_tiles_x, m.r_tiles_y);
   t.c_tiles += m.c_tiles_x * c_tiles_y;
   t.px += npx;
   t.blocks += (int)((npx + ccl::kBlockPx - 1) / ccl::kBlockPx);
@@ -951,7 +953,7 @@ BatchTotals table_totals(BatchTotals t) {
 
 nsgb_status batch_plan(const nsgb_batch* b, Plan* P, Ws* w) {
   if (!b || !b->ws) return NSGB_ERR_BAD_ARG;
-  BatchTotals t;
+  BatchTotals t{};
   t.n = b->n;
   t.px = b->total_px;
   t.r_tiles = b->recon_tiles;
@@ -975,7 +977,7 @@ nsgb_status batch_plan(const nsgb_batch* b, Plan* P, Ws* w) {
 extern "C" {
 
 size_t nsgb_batch_workspace_size(int dtype, const nsgb_tile* tiles, int n_tiles) {
-  BatchTotals t;
+  BatchTotals t{};
   if (!batch_totals(dtype, tiles, n_tiles, nullptr, &t)) return 0;
   return ws_sizes(table_totals(t)).total;
 }
@@ -984,7 +986,7 @@ nsgb_status nsgb_batch_prepare(int dtype, const nsgb_tile* tiles, int n_tiles, v
                                nsgb_batch* batch) {
   if (!batch) return NSGB_ERR_BAD_ARG;
   std::vector<Img> imgs;
-  BatchTotals t;
+  BatchTotals t{};
   if (!batch_totals(dtype, tiles, n_tiles, &imgs, &t)) return NSGB_ERR_BAD_ARG;
   nsgb_status st = check_ws_bytes(ws, ws_bytes, nsgb_batch_workspace_size(dtype, tiles, n_tiles));
   if (st != NSGB_OK) return st;
@@ -1227,6 +1229,7 @@ __global__ void stack_table_kernel(Img proto, int n, int64_t stride, BatchTotals
   m.plane = (void*)((uintptr_t)proto.plane + (uintptr_t)(i * stride));
   m.aux = (const void*)((uintptr_t)proto.aux + (uintptr_t)(i * stride));
   m.r_tile_base = i * one.r_tiles;
+  m.r_even_base = i * even_tiles(proto.r_tiles_x, proto.r_tiles_y);
   m.c_tile_base = i * one.c_tiles;
   m.px_base = (int)(i * one.px);
   m.blk_base = i * one.blocks;
@@ -1240,6 +1243,7 @@ BatchTotals stacked_totals(const BatchTotals& one, int64_t n) {
   t.n = (int)n;
   t.px = one.px * n;
   t.r_tiles = (int)(one.r_tiles * n);
+  t.r_even = (int)(one.r_even * n);
   t.c_tiles = (int)(one.c_tiles * n);
   t.blocks = (int)(one.blocks * n);
   t.rows = (int)(one.rows * n);

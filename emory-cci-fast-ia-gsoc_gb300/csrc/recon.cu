@@ -786,11 +786,33 @@ __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args a) {
   }
 }
 
+// Initial ring contents: every tile queued once.  A batch in checkerboard order queues the
+// colour-0 tiles of all images before any colour-1 tile, so tiles taken at the same time are
+// not neighbours across the whole batch (per image, the first colour of a small image would
+// otherwise run next to the second one).
 __global__ void recon_init_kernel(Ctl c, Imgs I, int ntiles, int order) {
+  int even_total = 0;
+  if (I.d && order == 1) {
+    const Img& last = I.d[I.n - 1];
+    even_total = last.r_even_base + even_tiles(last.r_tiles_x, last.r_tiles_y);
+  }
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < c.cap; i += gridDim.x * blockDim.x) {
     if ((int)i < ntiles) {
-      const Img im = img_at(I, img_of(I, (int)i, RTileBase()));
-      const int local = (int)i - im.r_tile_base;
+      Img im;
+      int local;
+      if (I.d && order == 1) {
+        if ((int)i < even_total) {
+          im = I.d[img_of(I, (int)i, REvenBase())];
+          local = (int)i - im.r_even_base;
+        } else {
+          const int j = (int)i - even_total;
+          im = I.d[img_of(I, j, ROddBase())];
+          local = even_tiles(im.r_tiles_x, im.r_tiles_y) + j - (im.r_tile_base - im.r_even_base);
+        }
+      } else {
+        im = img_at(I, img_of(I, (int)i, RTileBase()));
+        local = (int)i - im.r_tile_base;
+      }
       c.slots[i].val = im.r_tile_base + initial_tile(local, im.r_tiles_x * im.r_tiles_y, im.r_tiles_x, order);
       c.slots[i].seq = i + 1u;
       c.state[i] = kQueued;
