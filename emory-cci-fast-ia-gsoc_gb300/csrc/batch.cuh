@@ -17,6 +17,7 @@ struct Img {
   int aligned;        // plane / aux aligned for vector tile loads
   int r_tiles_x, r_tiles_y, r_tile_base;  // reconstruction tiles
   int r_even_base;    // first of its checkerboard colour-0 tiles among all images' colour-0 tiles
+  int r_col_base[3];  // the same for the first three colours of the four-colour order
   int c_tiles_x, c_tile_base;             // 32x32 labelling tiles
   int px_base;        // first pixel in the concatenated label planes
   int blk_base;       // first 1024-pixel rank block
@@ -61,12 +62,28 @@ __host__ __device__ inline int even_tiles(int tiles_x, int tiles_y) {
   return ((tiles_y + 1) / 2) * ((tiles_x + 1) / 2) + (tiles_y / 2) * (tiles_x / 2);
 }
 
+// Four-colour order: colour c = 0..3 is (tile row parity, tile column parity) = (0,0), (1,1),
+// (0,1), (1,0); tiles of colour c in an image.
+__host__ __device__ inline int colour_tiles(int tiles_x, int tiles_y, int c) {
+  const int py = (c == 1 || c == 3) ? 1 : 0, px = (c == 1 || c == 2) ? 1 : 0;
+  return ((tiles_y - py + 1) / 2) * ((tiles_x - px + 1) / 2);
+}
+
+// Start of an image's colour-c tiles among all images' colour-c tiles (four-colour order).
+struct RColBase {
+  int c;
+  __device__ int operator()(const Img& m) const {
+    return c < 3 ? m.r_col_base[c] : m.r_tile_base - m.r_col_base[0] - m.r_col_base[1] - m.r_col_base[2];
+  }
+};
+
 // Totals of a batch, known on the host (grid sizes).
 struct BatchTotals {
   int n;
   int64_t px;      // total pixels (< 2^31)
   int r_tiles;     // reconstruction tiles
   int r_even;      // reconstruction tiles of checkerboard colour 0
+  int r_col[3];    // reconstruction tiles of the first three colours of the four-colour order
   int c_tiles;     // labelling tiles
   int blocks;      // rank blocks
   int rows;        // total rows

@@ -376,6 +376,7 @@ void add_image(Img& m, BatchTotals& t) {
   const int c_tiles_y = (m.H + ccl::kTile - 1) / ccl::kTile;
   m.r_tile_base = t.r_tiles;
   m.r_even_base = t.r_even;
+  for (int c = 0; c < 3; ++c) m.r_col_base[c] = t.r_col[c];
   m.c_tile_base = t.c_tiles;
   m.px_base = (int)t.px;
   m.blk_base = t.blocks;
@@ -383,6 +384,7 @@ void add_image(Img& m, BatchTotals& t) {
   const int64_t npx = (int64_t)m.H * m.W;
   t.r_tiles += m.r_tiles_x * m.r_tiles_y;
   t.r_even += even_tiles(m.r_tiles_x, m.r_tiles_y);
+  for (int c = 0; c < 3; ++c) t.r_col[c] += colour_tiles(m.r_tiles_x, m.r_tiles_y, c);
   t.c_tiles += m.c_tiles_x * c_tiles_y;
   t.px += npx;
   t.blocks += (int)((npx + ccl::kBlockPx - 1) / ccl::kBlockPx);
@@ -1230,6 +1232,7 @@ __global__ void stack_table_kernel(Img proto, int n, int64_t stride, BatchTotals
   m.aux = (const void*)((uintptr_t)proto.aux + (uintptr_t)(i * stride));
   m.r_tile_base = i * one.r_tiles;
   m.r_even_base = i * even_tiles(proto.r_tiles_x, proto.r_tiles_y);
+  for (int c = 0; c < 3; ++c) m.r_col_base[c] = i * colour_tiles(proto.r_tiles_x, proto.r_tiles_y, c);
   m.c_tile_base = i * one.c_tiles;
   m.px_base = (int)(i * one.px);
   m.blk_base = i * one.blocks;
@@ -1244,6 +1247,7 @@ BatchTotals stacked_totals(const BatchTotals& one, int64_t n) {
   t.px = one.px * n;
   t.r_tiles = (int)(one.r_tiles * n);
   t.r_even = (int)(one.r_even * n);
+  for (int c = 0; c < 3; ++c) t.r_col[c] = (int)(one.r_col[c] * n);
   t.c_tiles = (int)(one.c_tiles * n);
   t.blocks = (int)(one.blocks * n);
   t.rows = (int)(one.rows * n);

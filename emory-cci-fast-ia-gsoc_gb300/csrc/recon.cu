@@ -786,21 +786,38 @@ __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args a) {
   }
 }
 
-// Initial ring contents: every tile queued once.  A batch in checkerboard order queues the
-// colour-0 tiles of all images before any colour-1 tile, so tiles taken at the same time are
-// not neighbours across the whole batch (per image, the first colour of a small image would
-// otherwise run next to the second one).
+// Initial ring contents: every tile queued once.  A batch queues the tiles of each colour of
+// the image's order (checkerboard: 2 colours, four-colour order: 4) for all images before any
+// tile of the next colour, so tiles taken at the same time are not neighbours across the whole
+// batch (per image, the first colour of a small image would otherwise run next to the second
+// one).
 __global__ void recon_init_kernel(Ctl c, Imgs I, int ntiles, int order) {
   int even_total = 0;
+  int col_end[4] = {0, 0, 0, 0};  // four-colour order: end of each colour's range in the ring
   if (I.d && order == 1) {
     const Img& last = I.d[I.n - 1];
     even_total = last.r_even_base + even_tiles(last.r_tiles_x, last.r_tiles_y);
+  }
+  if (I.d && order == 2) {
+    const Img& last = I.d[I.n - 1];
+    int acc = 0;
+    for (int k = 0; k < 4; ++k) {
+      acc += RColBase{k}(last) + colour_tiles(last.r_tiles_x, last.r_tiles_y, k);
+      col_end[k] = acc;
+    }
   }
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < c.cap; i += gridDim.x * blockDim.x) {
     if ((int)i < ntiles) {
       Img im;
       int local;
-      if (I.d && order == 1) {
+      if (I.d && order == 2) {
+        int k = 0;
+        while (k < 3 && (int)i >= col_end[k]) ++k;
+        const int j = (int)i - (k ? col_end[k - 1] : 0);
+        im = I.d[img_of(I, j, RColBase{k})];
+        local = j - RColBase{k}(im);
+        for (int q = 0; q < k; ++q) local += colour_tiles(im.r_tiles_x, im.r_tiles_y, q);
+      } else if (I.d && order == 1) {
         if ((int)i < even_total) {
           im = I.d[img_of(I, (int)i, REvenBase())];
           local = (int)i - im.r_even_base;
