@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <climits>
 #include <type_traits>
 
 #include "batch.cuh"
@@ -377,15 +378,41 @@ __device__ __forceinline__ void set_root_bit(unsigned* bits, int r) {
   if (!(__ldcg(&bits[r >> 5]) & bit)) atomicOr(&bits[r >> 5], bit);
 }
 
-// Row grid over the rows of all images: x = column (blockIdx.x * blockDim.x + threadIdx.x),
-// blockIdx.y strides the concatenated rows; f(image, y, x) runs for every pixel.
+// Row walk over the rows of all images: g(image, row within the image) for every row this
+// block row owns.  A single image strides its rows by gridDim.y.  A batch gives each block row
+// a contiguous range of the concatenated rows, so the image is looked up once per block row
+// (a binary search over the table) and then followed across image boundaries, instead of
+// searching again for every row.
+template <class G>
+__device__ __forceinline__ void for_batch_rows(const Imgs& I, int total_rows, G&& g) {
+  if (!I.d) {
+    for (int gr = blockIdx.y; gr < total_rows; gr += gridDim.y) g(I.one, gr);
+    return;
+  }
+  const int per = (total_rows + (int)gridDim.y - 1) / (int)gridDim.y;
+  const int r0 = (int)blockIdx.y * per, r1 = min(total_rows, r0 + per);
+  if (r0 >= r1) return;
+  int ii = img_of(I, r0, RowBase());
+  Img m = I.d[ii];
+  int next = ii + 1 < I.n ? I.d[ii + 1].row_base : INT_MAX;
+  for (int gr = r0; gr < r1; ++gr) {
+    while (gr >= next) {
+      ++ii;
+      m = I.d[ii];
+      next = ii + 1 < I.n ? I.d[ii + 1].row_base : INT_MAX;
+    }
+    g(m, gr - m.row_base);
+  }
+}
+
+// Row grid over the rows of all images: x = column (blockIdx.x * blockDim.x + threadIdx.x);
+// f(image, y, x) runs for every pixel.
 template <class F>
 __device__ __forceinline__ void for_batch_pixels(const Imgs& I, int total_rows, F&& f) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  for (int gr = blockIdx.y; gr < total_rows; gr += gridDim.y) {
-    const Img m = img_at(I, img_of(I, gr, RowBase()));
-    if (x < m.W) f(m, gr - m.row_base, x);
-  }
+  for_batch_rows(I, total_rows, [&](const Img& m, int y) {
+    if (x < m.W) f(m, y, x);
+  });
 }
 
 // The same with four consecutive pixels per thread: f(image, y, x, n) for pixels x .. x+n-1
@@ -393,10 +420,9 @@ __device__ __forceinline__ void for_batch_pixels(const Imgs& I, int total_rows, 
 template <class F>
 __device__ __forceinline__ void for_batch_quads(const Imgs& I, int total_rows, F&& f) {
   const int x = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
-  for (int gr = blockIdx.y; gr < total_rows; gr += gridDim.y) {
-    const Img m = img_at(I, img_of(I, gr, RowBase()));
-    if (x < m.W) f(m, gr - m.row_base, x, min(4, m.W - x));
-  }
+  for_batch_rows(I, total_rows, [&](const Img& m, int y) {
+    if (x < m.W) f(m, y, x, min(4, m.W - x));
+  });
 }
 
 // Roots of four consecutive pixels (L read-only): one 16-byte load when aligned.
