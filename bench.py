@@ -36,8 +36,8 @@ sys.path.insert(0, PKG)
 
 METRIC = "imreconstruct+bwlabel MPix/s, uint8 4096², plain vs batched GPU; % of HBM peak"
 # recon init + recon, fill (local, merge, flatten, border seeds, output), label (local, merge,
-# flatten), rank (count, scan, assign), label/area output: see csrc/ops.cu chain_impl
-KERNELS_PER_CHAIN = 14
+# flatten), rank (mark, count, scan, assign), label/area output: see csrc/ops.cu chain_impl
+KERNELS_PER_CHAIN = 15
 RECON_BYTES_PER_PX = 3  # marker read + mask read + result write (u8)
 CHAIN_BYTES_PER_PX = 17  # recon 3 + threshold 2 + fill 2 + bwlabel 5 + bwareaopen 5
 
