@@ -91,21 +91,35 @@ __device__ __forceinline__ void pending_release(const Ctl& c) {
   if (atomicSub(c.pending, 1) == 1) atomicExch(c.done, 1);
 }
 
+// Claims a neighbour whose state the first compare-and-swap found running or running-dirty:
+// a running neighbour is marked dirty (its owner re-runs it).  A neighbour that went idle in
+// between is claimed with a fresh idle -> queued compare-and-swap; it is never pushed while its
+// state still reads idle, which would let a second marker push it again and two warps run the
+// same tile at once.  Returns true when this call queued it.  Rolled and out of line: the
+// retries are rare, and the visit's instruction stream stays short.
+__device__ __noinline__ bool mark_claim_retry(const Ctl& c, int nt, int s) {
+#pragma unroll 1
+  for (int guard = 0; guard < 1024; ++guard) {
+    if (s == kIdle) return true;
+    if (s == kQueued || s == kRunningDirty) return false;  // will load after our stores
+    s = atomicCAS(&c.state[nt], kRunning, kRunningDirty);
+    if (s == kRunning) return false;  // its owner re-runs it
+    s = atomicCAS(&c.state[nt], kIdle, kQueued);
+  }
+  set_status(c.status, kDevTimeout);
+  return false;
+}
+
 // A neighbour's values may have become stale: make sure it (re)reads them.  The common case
 // (an idle neighbour) takes one atomic.
 __device__ __forceinline__ void mark_tile(const Ctl& c, int nt) {
-  int s = atomicCAS(&c.state[nt], kIdle, kQueued);
-  for (int guard = 0; guard < 1024; ++guard) {
-    if (s == kIdle) {  // this call queued it
-      atomicAdd(c.pending, 1);
-      queue_push(c, nt);
-      return;
-    }
-    if (s == kQueued || s == kRunningDirty) return;  // will load after our stores
-    s = atomicCAS(&c.state[nt], kRunning, kRunningDirty);
-    if (s == kRunning) return;  // its owner re-runs it
+  const int s = atomicCAS(&c.state[nt], kIdle, kQueued);
+  bool queued = s == kIdle;
+  if (!queued && s != kQueued && s != kRunningDirty) queued = mark_claim_retry(c, nt, s);
+  if (queued) {
+    atomicAdd(c.pending, 1);
+    queue_push(c, nt);
   }
-  set_status(c.status, kDevTimeout);
 }
 
 // Initial queue order.  order 0: raster.  order 1: checkerboard, even tiles first.  order 2:
