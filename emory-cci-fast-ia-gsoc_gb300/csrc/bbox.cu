@@ -1,0 +1,194 @@
+// Per-label bounding boxes on GB300.
+//
+// Reference semantics: ConnComponents::boundingBox (src/segment/ConnComponents.cpp:241-284)
+// scans the label image in raster order and keeps, per label other than the background, the
+// label and its pixels' min x, max x, min y, max y, in the order of the label's first pixel; a
+// pixel labelled -1 or 0 that is not the background ends the scan (the reference prints a
+// message and stops).  The reference GPU version (cuda/ccl_uf.cu:847-1107, Thrust sort and
+// reduce_by_key) orders entries by label value instead; with raster labels (1..n, from the
+// relabel) both orders are the same.  This file follows the CPU order.
+//
+// Schedule: (1) one pass finds where the scan ends (the first -1 / 0 pixel) and checks that
+// every label indexes the per-label arrays; (2) one pass folds each warp's 32 pixels of a row
+// by label (match_any + warp min/max reductions) and updates, per label, its first pixel index
+// and the four extremes with one atomic each, skipped when a plain read already shows no
+// improvement (the values only move one way, so a stale read can only cost an atomic); (3) the
+// first pixel of each present label is marked in a one-bit-per-pixel map, which is counted and
+// scanned per 1024-pixel block (the rank machinery of the relabel); (4) each present label
+// writes its entry at the rank of its first pixel, i.e. in raster order of first appearance.
+#include <climits>
+
+#include "bbox.cuh"
+#include "ccl.cuh"
+#include "common.cuh"
+
+namespace nsgb {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
+
+struct BWs {
+  int* hdr;  // [0] status, [1] stop (first -1 / 0 pixel, or INT_MAX), [2] labels present
+  int *first, *mnx, *mxx, *mny, *mxy;
+  unsigned* bits;
+  size_t bits_bytes;
+  int *blk, *wpre;
+};
+
+// Per-label planes have px + 1 entries: labels run up to px (an image of isolated pixels).
+BWs carve(void* ws, int64_t px) {
+  BWs w;
+  char* p = (char*)ws;
+  const size_t plane = al(sizeof(int) * (size_t)(px + 1));
+  const int64_t nblocks = (px + ccl::kBlockPx - 1) / ccl::kBlockPx;
+  w.hdr = (int*)p;
+  p += 256;
+  w.first = (int*)p;
+  p += plane;
+  w.mnx = (int*)p;
+  p += plane;
+  w.mxx = (int*)p;
+  p += plane;
+  w.mny = (int*)p;
+  p += plane;
+  w.mxy = (int*)p;
+  p += plane;
+  w.bits = (unsigned*)p;
+  w.bits_bytes = sizeof(unsigned) * (size_t)(px / 32 + 2);
+  p += al(w.bits_bytes);
+  w.blk = (int*)p;
+  p += al(sizeof(int) * (size_t)nblocks);
+  w.wpre = (int*)p;
+  return w;
+}
+
+__device__ __forceinline__ int32_t label_at(const Img& m, int y, int x) {
+  return *(const int32_t*)((const char*)m.plane + (int64_t)y * m.pitch + (int64_t)x * 4);
+}
+
+// Per-label arrays to their neutral values; header.
+__global__ void bbox_init(BWs w, int n) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < n; l += stride) {
+    w.first[l] = INT_MAX;
+    w.mnx[l] = INT_MAX;
+    w.mxx[l] = -1;
+    w.mny[l] = INT_MAX;
+    w.mxy[l] = -1;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    w.hdr[0] = 0;
+    w.hdr[1] = INT_MAX;
+    w.hdr[2] = 0;
+  }
+}
+
+// Where the scan ends, and label range checks.  Every lane of a warp runs the loop (lanes past
+// the row end take no part), so the warp reductions see full warps.
+__global__ void __launch_bounds__(kThreads) bbox_scan(Imgs I, int32_t bgval, BWs w) {
+  const Img& m = I.one;
+  const int n = m.H * m.W;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int y = blockIdx.y; y < m.H; y += gridDim.y) {
+    int cand = INT_MAX;
+    if (x < m.W) {
+      const int32_t l = label_at(m, y, x);
+      if (l != bgval) {
+        if (l == -1 || l == 0) cand = y * m.W + x;
+        else if (l < 1 || l > n) set_status(w.hdr, NSGB_ERR_BAD_ARG);
+      }
+    }
+    const int s = __reduce_min_sync(NSGB_FULL, cand);
+    if (s != INT_MAX && (threadIdx.x & 31) == 0) atomicMin(w.hdr + 1, s);
+  }
+}
+
+// Folds each warp's row segment by label, then one update per label and field.
+__global__ void __launch_bounds__(kThreads) bbox_accum(Imgs I, int32_t bgval, BWs w) {
+  const Img& m = I.one;
+  const int n = m.H * m.W;
+  const int stop = __ldcg(w.hdr + 1);
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  for (int y = blockIdx.y; y < m.H; y += gridDim.y) {
+    int key = -1;
+    if (x < m.W && y * m.W + x < stop) {
+      const int32_t l = label_at(m, y, x);
+      if (l != bgval && l >= 1 && l <= n) key = l;
+    }
+    const unsigned peers = __match_any_sync(NSGB_FULL, key);
+    if (key < 0) continue;
+    const int xmin = __reduce_min_sync(peers, x);
+    const int xmax = __reduce_max_sync(peers, x);
+    if (lane != __ffs(peers) - 1) continue;
+    const int fi = y * m.W + xmin;
+    if (fi < w.first[key]) atomicMin(w.first + key, fi);
+    if (xmin < w.mnx[key]) atomicMin(w.mnx + key, xmin);
+    if (xmax > w.mxx[key]) atomicMax(w.mxx + key, xmax);
+    if (y < w.mny[key]) atomicMin(w.mny + key, y);
+    if (y > w.mxy[key]) atomicMax(w.mxy + key, y);
+  }
+}
+
+// The first pixel of every present label into the bitmap; labels counted.
+__global__ void __launch_bounds__(kThreads) bbox_mark(BWs w, int n) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int l = base + threadIdx.x;
+    const bool present = l < n && __ldcg(w.mxx + l) >= 0;
+    if (present) {
+      const int f = __ldcg(w.first + l);
+      atomicOr(w.bits + (f >> 5), 1u << (f & 31));
+    }
+    const unsigned b = __ballot_sync(NSGB_FULL, present);
+    if (b && (threadIdx.x & 31) == 0) atomicAdd(w.hdr + 2, __popc(b));
+  }
+}
+
+// Entry of each present label at the rank of its first pixel.
+__global__ void __launch_bounds__(kThreads) bbox_out(BWs w, int n, int32_t* boxes, int64_t cap) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < n; l += stride) {
+    if (__ldcg(w.mxx + l) < 0) continue;
+    const int r = ccl::bit_rank(w.bits, w.blk, w.wpre, __ldcg(w.first + l));
+    if (r >= cap) continue;
+    boxes[r] = l;
+    boxes[cap + r] = __ldcg(w.mnx + l);
+    boxes[2 * cap + r] = __ldcg(w.mxx + l);
+    boxes[3 * cap + r] = __ldcg(w.mny + l);
+    boxes[4 * cap + r] = __ldcg(w.mxy + l);
+  }
+}
+
+}  // namespace
+
+size_t bbox_workspace_bytes(int64_t px) {
+  const int64_t nblocks = (px + ccl::kBlockPx - 1) / ccl::kBlockPx;
+  return 256 + 5 * al(sizeof(int) * (size_t)(px + 1)) + al(sizeof(unsigned) * (size_t)(px / 32 + 2)) +
+         al(sizeof(int) * (size_t)nblocks) + al(sizeof(int) * 32 * (size_t)nblocks);
+}
+
+cudaError_t bbox_launch(const Imgs& I, const BatchTotals& t, int32_t bgval, void* ws, int32_t* boxes, int64_t cap,
+                        int32_t* count_dev, cudaStream_t s) {
+  const int n = (int)t.px + 1;  // label values 0 .. px
+  BWs w = carve(ws, t.px);
+  cudaError_t e = cudaMemsetAsync(w.bits, 0, w.bits_bytes, s);
+  if (e != cudaSuccess) return e;
+  const int g = ccl::flat_grid(n);
+  const dim3 rows = ccl::rowcol_grid(t.rows, t.max_w);
+  bbox_init<<<g, kThreads, 0, s>>>(w, n);
+  bbox_scan<<<rows, kThreads, 0, s>>>(I, bgval, w);
+  bbox_accum<<<rows, kThreads, 0, s>>>(I, bgval, w);
+  bbox_mark<<<g, kThreads, 0, s>>>(w, n);
+  e = ccl::rank_bits(I, t, w.bits, w.blk, w.wpre, s);
+  if (e != cudaSuccess) return e;
+  bbox_out<<<g, kThreads, 0, s>>>(w, n, boxes, cap);
+  e = cudaGetLastError();
+  if (e == cudaSuccess && count_dev) e = cudaMemcpyAsync(count_dev, w.hdr + 2, sizeof(int32_t), cudaMemcpyDeviceToDevice, s);
+  return e;
+}
+
+}  // namespace nsgb

@@ -14,13 +14,6 @@ namespace {
 
 constexpr int kRankThreads = 256;
 
-// Bits of pixels p .. p+31 (the bitmap has a spare word at the end).
-__device__ __forceinline__ unsigned bits_at(const unsigned* bits, int p) {
-  const int w = p >> 5, sh = p & 31;
-  const unsigned lo = __ldcg(bits + w);
-  return sh ? __funnelshift_r(lo, __ldcg(bits + w + 1), sh) : lo;
-}
-
 // Global roots among the local roots: set their bit, count them (and the kept ones) per image.
 __global__ void __launch_bounds__(kRankThreads) mark_roots(Imgs I, Forest f, int max_roots, int lo, int hi,
                                                            unsigned* __restrict__ bits, int* __restrict__ counts) {
@@ -169,6 +162,14 @@ int flat_grid(int64_t n) {
   if (b > 152 * 32) b = 152 * 32;
   if (b < 1) b = 1;
   return (int)b;
+}
+
+cudaError_t rank_bits(const Imgs& I, const BatchTotals& t, const unsigned* bits, int* block_tmp, int* wpre,
+                      cudaStream_t s) {
+  count_blocks<<<(t.blocks + kRankThreads / 32 - 1) / (kRankThreads / 32), kRankThreads, 0, s>>>(I, t.blocks, bits,
+                                                                                                  block_tmp, wpre);
+  scan_blocks<<<t.n, 1024, 0, s>>>(I, block_tmp);
+  return cudaGetLastError();
 }
 
 cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, int* rank,

@@ -531,5 +531,27 @@ cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int
                        unsigned* bits, size_t bits_bytes, int* block_tmp, int* wpre, int* counts, cudaStream_t s);
 constexpr int kBlockPx = 1024;
 
+// The counting half of rank_roots for any bitmap of the images' pixels: per 1024-px block the
+// set bits before it in its image (block_tmp, exclusive scan) and per 32-px word the set bits
+// before it in its block (wpre).  A set bit's rank is then bit_rank().
+cudaError_t rank_bits(const Imgs& I, const BatchTotals& t, const unsigned* bits, int* block_tmp, int* wpre,
+                      cudaStream_t s);
+
+// Bits of pixels p .. p+31 (the bitmap has a spare word at the end).
+__device__ __forceinline__ unsigned bits_at(const unsigned* bits, int p) {
+  const int w = p >> 5, sh = p & 31;
+  const unsigned lo = __ldcg(bits + w);
+  return sh ? __funnelshift_r(lo, __ldcg(bits + w + 1), sh) : lo;
+}
+
+// Rank of pixel p (a set bit) among the set bits of a single image, after rank_bits.
+__device__ __forceinline__ int bit_rank(const unsigned* bits, const int* block_tmp, const int* wpre, int p) {
+  const int b = p / kBlockPx, j = (p % kBlockPx) >> 5;
+  const int w0 = b * kBlockPx + 32 * j;
+  int c = __ldcg(block_tmp + b) + __ldcg(wpre + 32 * b + j);
+  if (p > w0) c += __popc(bits_at(bits, w0) & ((1u << (p - w0)) - 1u));
+  return c;
+}
+
 }  // namespace ccl
 }  // namespace nsgb

@@ -15,6 +15,7 @@
 
 #include "../../include/nsgb.h"
 #include "batch.cuh"
+#include "bbox.cuh"
 #include "ccl.cuh"
 #include "common.cuh"
 #include "recon.cuh"
@@ -602,6 +603,7 @@ size_t nsgb_workspace_size(int op, int dtype, int64_t rows, int64_t cols) {
   if (op == NSGB_OP_BWLABEL || op == NSGB_OP_BWAREAOPEN) dtype = NSGB_U8;
   if (dtype < 0 || dtype > 3) return 0;
   if (op == NSGB_OP_IMRECONSTRUCT || op == NSGB_OP_HMIN) return align256(recon_workspace_bytes(dtype, rows, cols));
+  if (op == NSGB_OP_BOUNDING_BOX) return align256(bbox_workspace_bytes(rows * cols));
   const Plan P = single_plan(dtype, nullptr, nullptr, rows, cols, cols * elem_size(dtype));
   return ws_sizes(P.t).total;
 }
@@ -852,6 +854,23 @@ nsgb_status nsgb_bwareaopen(const void* in, int labeled, int32_t* labels_out, ui
   }
   if (e == cudaSuccess && count) {
     e = cudaMemcpyAsync(count, w.counts + 1, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  return finish(e, ws, s, opts);
+}
+
+nsgb_status nsgb_bounding_boxes(const int32_t* labels, int64_t rows, int64_t cols, int64_t pitch, int32_t bgval,
+                                int32_t* boxes, int64_t capacity, int32_t* count, int32_t* count_dev, void* ws,
+                                size_t ws_bytes, nsgb_stream_t stream, const nsgb_opts* opts) {
+  if (!labels || !valid_dims(rows, cols) || !valid_pitch(pitch, cols, 4) || capacity < 0 || (capacity > 0 && !boxes))
+    return NSGB_ERR_BAD_ARG;
+  nsgb_status st = check_ws(ws, ws_bytes, NSGB_OP_BOUNDING_BOX, NSGB_I32, rows, cols);
+  if (st != NSGB_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const Plan P = single_plan(NSGB_I32, (void*)labels, nullptr, rows, cols, pitch);
+  cudaError_t e = bbox_launch(P.I, P.t, bgval, ws, boxes, capacity, count_dev, s);
+  if (e == cudaSuccess && count) {
+    e = cudaMemcpyAsync(count, (const int*)ws + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   }
   return finish(e, ws, s, opts);

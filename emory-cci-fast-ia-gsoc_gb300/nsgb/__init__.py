@@ -23,7 +23,7 @@ from ._ffi import NsgbError, lib
 
 __all__ = [
     "imreconstruct", "imreconstructBinary", "imfillHoles", "imhmin", "bwselect", "bwlabel", "bwlabel2",
-    "bwareaopen2", "threshold", "invert", "chain", "imreconstructQueueThroughput", "chain_batch", "BatchPlan",
+    "bwareaopen2", "bounding_boxes", "threshold", "invert", "chain", "imreconstructQueueThroughput", "chain_batch", "BatchPlan",
     "recon_f32", "recon_f32_backward", "NsgbError", "workspace",
 ]
 
@@ -234,6 +234,25 @@ def bwareaopen2(image: torch.Tensor, labeled: bool, flatten: bool, minSize: int,
                                  _stream(), None)
     _ffi.check(st, "bwareaopen2")
     return out, int(cnt.value)
+
+
+def bounding_boxes(labels: torch.Tensor, bgval: int = 0) -> torch.Tensor:
+    """ConnComponents::boundingBox (ConnComponents.cpp:241-284) of an int32 label image on the
+    device: int32 tensor (5, count) of label, min x, max x, min y, max y per label other than
+    `bgval`, in the order of each label's first pixel in raster order."""
+    _check_image(labels, "labels")
+    if labels.dtype != torch.int32:
+        raise NsgbError(2, "labels must be int32")
+    lab = _contig(labels)
+    rows, cols = lab.shape
+    ws, nb = _ws(_ffi.OP_BOUNDING_BOX, _ffi.I32, rows, cols, lab.device)
+    cap = rows * cols
+    boxes = torch.empty((5, cap), dtype=torch.int32, device=lab.device)
+    cnt = C.c_int32(0)
+    st = lib.nsgb_bounding_boxes(lab.data_ptr(), rows, cols, _pitch(lab), int(bgval), boxes.data_ptr(), cap,
+                                 C.byref(cnt), None, ws, nb, _stream(), None)
+    _ffi.check(st, "bounding_boxes")
+    return boxes[:, :int(cnt.value)].contiguous()
 
 
 def threshold(image: torch.Tensor, thr: float) -> torch.Tensor:

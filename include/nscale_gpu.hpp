@@ -376,6 +376,41 @@ inline GpuMat bwareaopen(const GpuMat& binaryImage, bool labeled, bool flatten, 
   return bwareaopen2(binaryImage, labeled, flatten, minSize, maxSize, connectivity, count, stream);
 }
 
+// nscale::gpu::boundingBox2 (cuda/ccl_uf.cuh:16, used at HistologicalEntitiesGPU.cpp:825):
+// per-label boxes of a device int32 label image (w x h, dense rows), returned as a device array
+// of 5 * compcount ints (labels, then min x, max x, min y, max y, each compcount long) that the
+// caller frees with cudaFree, as with the reference.  Entries follow the raster order of each
+// label's first pixel (ConnComponents::boundingBox, ConnComponents.cpp:241-284).
+inline int* boundingBox2(const int w, const int h, int* d_label, int bgval, int& compcount, cudaStream_t stream) {
+  const size_t nb = nsgb_workspace_size(NSGB_OP_BOUNDING_BOX, NSGB_I32, h, w);
+  const int64_t cap = (int64_t)w * h;
+  int32_t* tmp = nullptr;
+  if (cudaMalloc(&tmp, sizeof(int32_t) * 5 * (size_t)(cap > 0 ? cap : 1)) != cudaSuccess)
+    throw cv::Exception(-217, "boundingBox2: cudaMalloc failed");
+  int32_t c = 0;
+  const nsgb_status st = nsgb_bounding_boxes(d_label, h, w, (int64_t)w * 4, bgval, tmp, cap, &c, nullptr,
+                                             detail::workspace(nb), nb, (nsgb_stream_t)stream, nullptr);
+  if (st != NSGB_OK) {
+    cudaFree(tmp);
+    detail::check(st, "boundingBox2");
+  }
+  int* out = nullptr;
+  if (cudaMalloc(&out, sizeof(int) * 5 * (size_t)(c > 0 ? c : 1)) != cudaSuccess) {
+    cudaFree(tmp);
+    throw cv::Exception(-217, "boundingBox2: cudaMalloc failed");
+  }
+  if (c > 0 && (cudaMemcpy2DAsync(out, sizeof(int) * (size_t)c, tmp, sizeof(int) * (size_t)cap,
+                                  sizeof(int) * (size_t)c, 5, cudaMemcpyDeviceToDevice, stream) != cudaSuccess ||
+                cudaStreamSynchronize(stream) != cudaSuccess)) {
+    cudaFree(tmp);
+    cudaFree(out);
+    throw cv::Exception(-217, "boundingBox2: copy failed");
+  }
+  cudaFree(tmp);
+  compcount = c;
+  return out;
+}
+
 // nscale::gpu::imhmin<T> (MorphologicOperations.h:172).
 template <typename T>
 GpuMat imhmin(const GpuMat& image, T h, int connectivity, Stream& stream) {

@@ -48,7 +48,8 @@ typedef enum {
   NSGB_OP_BWSELECT = 4,
   NSGB_OP_BWLABEL = 5,
   NSGB_OP_BWAREAOPEN = 6,
-  NSGB_OP_CHAIN = 7
+  NSGB_OP_CHAIN = 7,
+  NSGB_OP_BOUNDING_BOX = 8
 } nsgb_op;
 
 typedef struct {
@@ -150,6 +151,23 @@ nsgb_status nsgb_bwareaopen(const void* in, int labeled, int32_t* labels_out, ui
                             int64_t pitch_flat, int32_t min_size, int32_t max_size, int conn,
                             int32_t* count, void* ws, size_t ws_bytes, nsgb_stream_t stream,
                             const nsgb_opts* opts);
+
+/* Per-label bounding boxes: ConnComponents::boundingBox (src/segment/ConnComponents.cpp:241-284),
+ * GPU counterpart nscale::gpu::boundingBox2 (src/segment/cuda/ccl_uf.cuh:16, ccl_uf.cu:847-1107).
+ * `labels`: int32 device image (rows x cols, pitch in bytes).  Each pixel holds `bgval` or a label
+ * in [1, rows*cols]: the raster labels of nsgb_bwlabel (1..n, background 0) or its root indices
+ * (background -1).  As in the reference, a pixel labelled -1 or 0 that is not bgval ends the scan:
+ * only the pixels before it in raster order count.  Any other value outside [-1, rows*cols]
+ * gives NSGB_ERR_BAD_ARG.
+ * `boxes`: device int32, 5 * capacity: entry k is label boxes[k], min x boxes[capacity + k],
+ * max x [2 * capacity + k], min y [3 * capacity + k], max y [4 * capacity + k], entries in the
+ * order of each label's first pixel in raster order (the reference CPU order; for raster labels
+ * that is label order).  Entries past `capacity` are dropped.  The number of labels goes to
+ * `count` (host, optional: forces a synchronisation) and / or `count_dev` (device, optional).
+ * Workspace: nsgb_workspace_size(NSGB_OP_BOUNDING_BOX, NSGB_I32, rows, cols). */
+nsgb_status nsgb_bounding_boxes(const int32_t* labels, int64_t rows, int64_t cols, int64_t pitch, int32_t bgval,
+                                int32_t* boxes, int64_t capacity, int32_t* count, int32_t* count_dev, void* ws,
+                                size_t ws_bytes, nsgb_stream_t stream, const nsgb_opts* opts);
 
 /* Elementwise helpers of the path: `in > thr` -> 255 / 0 (u8 out; OpenCV `Mat > k` as used at
  * HistologicalEntities.cpp:214; GPU thresholdCaller pixel-ops.cu:349-381), and invert

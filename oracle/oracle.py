@@ -40,6 +40,8 @@ def _load() -> C.CDLL:
     lib.orc_bwlabel2.restype = i32
     lib.orc_bwareaopen2.argtypes = [vp, C.c_int, C.c_int, i32, i32, C.c_int, i64, i64, vp, vp]
     lib.orc_bwareaopen2.restype = i32
+    lib.orc_bounding_box.argtypes = [vp, i64, i64, i32, vp, i64]
+    lib.orc_bounding_box.restype = i32
     lib.orc_chain.argtypes = [C.c_int, vp, vp, i64, i64, C.c_int, C.c_double, C.c_int, C.c_int, i32, i32,
                               vp, vp, vp, vp, C.POINTER(i32), vp]
     lib.orc_chain.restype = i32
@@ -125,6 +127,18 @@ def bwareaopen2(image: np.ndarray, labeled: bool, flatten: bool, lo: int, hi: in
     return (flat if flatten else labels), int(cnt)
 
 
+def bounding_box(labels: np.ndarray, bgval: int = 0) -> np.ndarray:
+    """ConnComponents::boundingBox (ConnComponents.cpp:241-284): int32 array (5, count) of
+    label, min x, max x, min y, max y per label other than bgval, in order of first appearance
+    in raster order."""
+    labels = _c(labels).astype(np.int32)
+    H, W = labels.shape
+    cap = H * W
+    out = np.zeros((5, max(cap, 1)), np.int32)
+    n = lib.orc_bounding_box(_p(labels), H, W, bgval, _p(out), max(cap, 1))
+    return np.ascontiguousarray(out[:, :n])
+
+
 def chain(marker: np.ndarray, mask: np.ndarray, recon_conn=8, thr=128.0, fill_conn=4, label_conn=8, lo=11,
           hi=1000):
     marker, mask = _c(marker), _c(mask)
@@ -158,6 +172,8 @@ def _ref() -> C.CDLL:
     r.ref_cc_relabel.restype = C.c_int
     r.ref_cc_area_threshold_labeled.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int]
     r.ref_cc_area_threshold_labeled.restype = C.c_int
+    r.ref_cc_bounding_box.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int]
+    r.ref_cc_bounding_box.restype = C.c_int
     return r
 
 
@@ -178,6 +194,16 @@ def ref_area_threshold_labeled(labels: np.ndarray, lo: int, hi: int):
     out = np.empty((H, W), np.int32)
     n = r.ref_cc_area_threshold_labeled(_p(labels), W, H, _p(out), -1, lo, hi)
     return out, int(n)
+
+
+def ref_bounding_box(labels: np.ndarray, bgval: int = 0) -> np.ndarray:
+    r = _ref()
+    labels = _c(labels).astype(np.int32)
+    H, W = labels.shape
+    cap = max(H * W, 1)
+    out = np.zeros((5, cap), np.int32)
+    n = r.ref_cc_bounding_box(_p(labels), W, H, bgval, _p(out), cap)
+    return np.ascontiguousarray(out[:, :n])
 
 
 # -- differentiable float32 reconstruction ------------------------------------------------

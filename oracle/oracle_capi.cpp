@@ -97,6 +97,10 @@ int32_t orc_bwlabel2(const uint8_t* bin, int64_t H, int64_t W, int conn, int rel
   return orc::bwlabel2(bin, H, W, conn, relab != 0, out);
 }
 
+int32_t orc_bounding_box(const int32_t* labels, int64_t H, int64_t W, int32_t bgval, int32_t* out, int64_t cap) {
+  return orc::cc_bounding_box(labels, W, H, bgval, out, cap);
+}
+
 int32_t orc_bwareaopen2(const void* image, int labeled, int flatten, int32_t minSize, int32_t maxSize,
                         int conn, int64_t H, int64_t W, int32_t* labels_out, uint8_t* flat_out) {
   return orc::bwareaopen2(image, labeled != 0, flatten != 0, minSize, maxSize, conn, H, W,

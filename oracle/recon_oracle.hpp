@@ -26,6 +26,7 @@
 #include <deque>
 #include <limits>
 #include <type_traits>
+#include <unordered_map>
 #include <vector>
 
 namespace orc {
@@ -391,6 +392,48 @@ inline int32_t cc_area_threshold_labeled(const int32_t* L, int64_t W, int64_t H,
     if (it->second >= lower && it->second < upper) out[i] = L[i];
   }
   return kept;
+}
+
+// ConnComponents::boundingBox (ConnComponents.cpp:241-284): one entry per label other than
+// bgval, in the order of the label's first pixel in raster order, holding the label and its
+// pixels' min x, max x, min y, max y.  A pixel labelled -1 or 0 that is not bgval ends the scan
+// there (the reference prints a message and stops).  Writes min(count, cap) entries as five
+// arrays of stride `cap` (label, minx, maxx, miny, maxy) and returns the count.
+inline int32_t cc_bounding_box(const int32_t* L, int64_t W, int64_t H, int32_t bgval, int32_t* out,
+                               int64_t cap) {
+  std::unordered_map<int32_t, size_t> at;
+  std::vector<int32_t> lab, mnx, mxx, mny, mxy;
+  const int64_t n = W * H;
+  for (int64_t i = 0; i < n; ++i) {
+    const int32_t l = L[i];
+    if (l == bgval) continue;
+    if (l == -1 || l == 0) break;
+    const int32_t x = (int32_t)(i % W), y = (int32_t)(i / W);
+    auto it = at.find(l);
+    if (it == at.end()) {
+      at.emplace(l, lab.size());
+      lab.push_back(l);
+      mnx.push_back(x);
+      mxx.push_back(x);
+      mny.push_back(y);
+      mxy.push_back(y);
+    } else {
+      const size_t k = it->second;
+      mnx[k] = std::min(mnx[k], x);
+      mxx[k] = std::max(mxx[k], x);
+      mny[k] = std::min(mny[k], y);
+      mxy[k] = std::max(mxy[k], y);
+    }
+  }
+  const int64_t m = std::min<int64_t>((int64_t)lab.size(), cap);
+  for (int64_t k = 0; k < m; ++k) {
+    out[k] = lab[k];
+    out[cap + k] = mnx[k];
+    out[2 * cap + k] = mxx[k];
+    out[3 * cap + k] = mny[k];
+    out[4 * cap + k] = mxy[k];
+  }
+  return (int32_t)lab.size();
 }
 
 // src/segment/MorphologicOperations.cpp:2012-2035 (bwlabel2).

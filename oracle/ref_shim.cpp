@@ -3,6 +3,7 @@
 // TEST INFRASTRUCTURE ONLY: it pins the oracle's labelling restatement; nothing in the
 // product links it.
 #include <cstdint>
+#include <cstdlib>
 
 #include "ConnComponents.h"
 
@@ -30,6 +31,19 @@ int ref_cc_area_threshold_labeled(const int* label, int w, int h, int* out, int 
 int ref_cc_area_threshold(unsigned char* img, int w, int h, int* label, int bgval, int lo, int hi, int conn) {
   nscale::ConnComponents cc;
   return cc.areaThreshold(img, w, h, label, bgval, lo, hi, conn);
+}
+
+// ConnComponents::boundingBox (ConnComponents.cpp:241-284): copies min(count, cap) entries into
+// five arrays of stride `cap` (label, minx, maxx, miny, maxy); returns the count.
+int ref_cc_bounding_box(const int* label, int w, int h, int bgval, int* out, int cap) {
+  nscale::ConnComponents cc;
+  int count = 0;
+  int* box = cc.boundingBox(w, h, label, bgval, count);
+  const int m = count < cap ? count : cap;
+  for (int f = 0; f < 5; ++f)
+    for (int k = 0; k < m; ++k) out[f * cap + k] = box[f * count + k];
+  free(box);
+  return count;
 }
 
 }  // extern "C"

@@ -57,6 +57,24 @@ int main(int argc, char** argv) {
   save(dir, "batch0.u8", b0);
   save(dir, "batch1.u8", b1);
 
+  // per-label bounding boxes of the raster labels (cuda/ccl_uf.cuh:16), device in / device out
+  int* d_lab = nullptr;
+  if (cudaMalloc(&d_lab, sizeof(int) * (size_t)H * W) != cudaSuccess) return 5;
+  for (int y = 0; y < H; ++y)
+    cudaMemcpy(d_lab + (size_t)y * W, labels.ptr<int>(y), sizeof(int) * W, cudaMemcpyHostToDevice);
+  int compcount = -1;
+  int* d_box = nscale::gpu::boundingBox2(W, H, d_lab, 0, compcount, (cudaStream_t)stream.raw());
+  std::vector<int> box(5 * (size_t)(compcount > 0 ? compcount : 1));
+  cudaMemcpy(box.data(), d_box, sizeof(int) * 5 * (size_t)compcount, cudaMemcpyDeviceToHost);
+  cudaFree(d_box);
+  cudaFree(d_lab);
+  {
+    FILE* f = std::fopen((dir + "/bbox.i32").c_str(), "wb");
+    if (!f) return 2;
+    std::fwrite(box.data(), sizeof(int), 5 * (size_t)compcount, f);
+    std::fclose(f);
+  }
+
   // error convention: a type mismatch raises cv::Exception, as CV_Assert does
   bool threw = false;
   try {
@@ -65,6 +83,6 @@ int main(int argc, char** argv) {
   } catch (const cv::Exception&) {
     threw = true;
   }
-  std::printf("count %d iter %u threw %d\n", count, iter, threw ? 1 : 0);
+  std::printf("count %d iter %u threw %d boxes %d\n", count, iter, threw ? 1 : 0, compcount);
   return threw ? 0 : 4;
 }

@@ -8,9 +8,12 @@ Sources of truth, both independent of the oracle restatement:
     (scipy.ndimage.label): mask pixels connected to a seed take the seed value.
   * ref_ccl_cases.npz -- seeded u8 images labelled by the reference's own ConnComponents.cpp
     (label, relabel, areaThresholdLabeled), compiled from its sources into oracle/_ref/.
+  * ref_bbox_cases.npz -- label images (raw root labels with background -1, raster labels with
+    background 0, and raster labels with stray -1 pixels that end the reference's scan) and the
+    reference's own ConnComponents::boundingBox output for them.
   * synth_digest.json -- SHA-256 of generator outputs, pinning the synthetic inputs across
     machines (x86-64 here, aarch64 on the GPU hosts).
-Usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [--bbox-only]
 """
 from __future__ import annotations
 
@@ -83,9 +86,44 @@ def ccl_cases(rng):
     return cases
 
 
+def bbox_cases(oracle):
+    """Label images for ConnComponents::boundingBox, each with the background value it uses."""
+    rng = np.random.default_rng(20261204)
+    cases = []
+    for k, img in enumerate(ccl_cases(np.random.default_rng(20261203))):
+        for conn in (4, 8):
+            lab, _ = oracle.ref_label(img, conn, relab=False)
+            rel, _ = oracle.ref_label(img, conn, relab=True)
+            cases.append((lab, -1))
+            cases.append((rel, 0))
+            if rel.size >= 16 and (rel > 0).any():
+                stray = rel.copy()
+                fg = np.flatnonzero(stray > 0)
+                stray.flat[fg[rng.integers(0, fg.size)]] = -1  # ends the reference's scan there
+                cases.append((stray, 0))
+    return cases
+
+
+def write_bbox(oracle):
+    arrays = {}
+    for k, (lab, bg) in enumerate(bbox_cases(oracle)):
+        arrays[f"lab{k}"] = lab
+        arrays[f"bg{k}"] = np.array(bg)
+        arrays[f"box{k}"] = oracle.ref_bounding_box(lab, bg)
+    np.savez_compressed(os.path.join(HERE, "ref_bbox_cases.npz"), **arrays)
+
+
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/fastIA-master"
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    ref_root = args[0] if args else "/root/reference/fastIA-master"
     import oracle  # noqa: E402
+
+    if "--bbox-only" in sys.argv:
+        if not oracle.ref_available():
+            raise SystemExit("oracle/_ref not built: run oracle/build_ref.sh first")
+        write_bbox(oracle)
+        print("wrote ref_bbox_cases.npz")
+        return
 
     # 1. reference inline fixture
     image, seeds, seed_list = parse_queue_fixture(ref_root)
@@ -109,6 +147,7 @@ def main():
             arrays[f"kept{k}_{conn}"] = kept
             arrays[f"nk{k}_{conn}"] = np.array(nk)
     np.savez_compressed(os.path.join(HERE, "ref_ccl_cases.npz"), **arrays)
+    write_bbox(oracle)
 
     # 3. generator digests
     from nsgb import synth

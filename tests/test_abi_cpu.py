@@ -40,9 +40,11 @@ def test_status_strings_and_workspace_sizes():
     lib = ffi.lib
     assert lib.nsgb_status_string(0) == b"ok"
     assert b"workspace" in lib.nsgb_status_string(3)
-    for op in range(8):
+    for op in range(9):
         for dt in range(4):
             assert lib.nsgb_workspace_size(op, dt, 64, 64) > 0
+    # bounding boxes: five per-label planes plus the bitmap and rank scratch
+    assert lib.nsgb_workspace_size(ffi.OP_BOUNDING_BOX, ffi.I32, 4096, 4096) >= 5 * 4 * 4096 * 4096
     assert lib.nsgb_workspace_size(0, 0, 0, 10) == 0
     big = lib.nsgb_workspace_size(7, 0, 4096, 4096)
     assert big > 3 * 4 * 4096 * 4096
@@ -60,3 +62,7 @@ def test_argument_errors_need_no_gpu():
     assert lib.nsgb_imreconstruct(0, 1, 1, 4, 4, 4, 8, 0, None, 0, None, None) == 3
     assert lib.nsgb_bwlabel(None, 1, 4, 4, 4, 16, 8, 1, None, 1, 1 << 20, None, None) == 1
     assert lib.nsgb_imhmin(2, 1, 2, 4, 4, 16, 1.0, 8, 1, 1 << 20, None, None) == 2
+    # bounding boxes: null labels, pitch below the row, capacity without an output buffer
+    assert lib.nsgb_bounding_boxes(None, 4, 4, 16, 0, 1, 4, None, None, 1, 1 << 20, None, None) == 1
+    assert lib.nsgb_bounding_boxes(1, 4, 4, 8, 0, 1, 4, None, None, 1, 1 << 20, None, None) == 1
+    assert lib.nsgb_bounding_boxes(1, 4, 4, 16, 0, None, 4, None, None, 1, 1 << 20, None, None) == 1

@@ -238,6 +238,59 @@ def test_bwlabel_bwareaopen_random(nsgb, oracle, conn):
                 assert c == ce and np.array_equal(to_np(got), exp), (h, w, p, flatten)
 
 
+def test_bounding_boxes_reference_fixtures(nsgb, golden_dir):
+    """ConnComponents::boundingBox of the reference itself (raw root labels, raster labels, and
+    raster labels with a stray -1 that ends the reference's scan)."""
+    d = np.load(os.path.join(golden_dir, "ref_bbox_cases.npz"))
+    k = 0
+    while f"lab{k}" in d:
+        got = to_np(nsgb.bounding_boxes(to_dev(d[f"lab{k}"]), int(d[f"bg{k}"])))
+        assert np.array_equal(got, d[f"box{k}"]), k
+        k += 1
+    assert k >= 150
+
+
+def test_bounding_boxes_random(nsgb, oracle):
+    rng = np.random.default_rng(3)
+    for (h, w) in SHAPES + [(513, 1000), (1024, 1024)]:
+        for p in (0.2, 0.55, 0.9):
+            img = ((rng.random((h, w)) < p) * 255).astype(np.uint8)
+            rel, _ = oracle.bwlabel2(img, 8, True)
+            assert np.array_equal(to_np(nsgb.bounding_boxes(to_dev(rel), 0)), oracle.bounding_box(rel, 0)), (h, w, p)
+            raw, _ = oracle.bwlabel2(img, 4, False)
+            assert np.array_equal(to_np(nsgb.bounding_boxes(to_dev(raw), -1)), oracle.bounding_box(raw, -1)), (h, w)
+    # arbitrary label values in [1, n), repeated in separate places, and a background of 7
+    lab = rng.integers(1, 60, (300, 200)).astype(np.int32)
+    lab[rng.random(lab.shape) < 0.4] = 7
+    assert np.array_equal(to_np(nsgb.bounding_boxes(to_dev(lab), 7)), oracle.bounding_box(lab, 7))
+
+
+def test_bounding_boxes_chain_labels(nsgb, oracle):
+    """The boxes of the chain's labelled output (HistologicalEntities.cpp:573 takes them after
+    bwlabel2), on the inverted workload with thousands of components."""
+    from nsgb import synth
+
+    mask, marker = synth.tile_u8(2048, 2048, 1500, 4)
+    inv_mask = (255 - mask).astype(np.uint8)
+    inv_marker = np.maximum(inv_mask.astype(int) - 10, 0).astype(np.uint8)
+    got = nsgb.chain(to_dev(inv_marker), to_dev(inv_mask), thr=128)
+    labels = got["labels"]
+    box = to_np(nsgb.bounding_boxes(labels, 0))
+    exp = oracle.bounding_box(to_np(labels), 0)
+    assert box.shape[1] == got["n_labels"] > 100
+    assert np.array_equal(box, exp)
+
+
+def test_bounding_boxes_bad_labels(nsgb):
+    lab = np.zeros((16, 16), np.int32)
+    lab[3, 4] = 16 * 16 + 1  # outside [-1, rows*cols]
+    with pytest.raises(nsgb.NsgbError):
+        nsgb.bounding_boxes(to_dev(lab), 0)
+    lab[3, 4] = -5
+    with pytest.raises(nsgb.NsgbError):
+        nsgb.bounding_boxes(to_dev(lab), 0)
+
+
 def test_threshold_invert(nsgb, oracle):
     rng = np.random.default_rng(0)
     for dtype in DTYPES:

@@ -2,6 +2,8 @@
 
 * union-find labelling: exact match with the reference's own ConnComponents.cpp, through the
   committed fixtures (tests/golden/ref_ccl_cases.npz) and, where oracle/_ref was built, live;
+* bounding boxes: the same for ConnComponents::boundingBox (tests/golden/ref_bbox_cases.npz),
+  plus an independent numpy formulation;
 * reconstruction: the reference's inline 32x32 queue fixture, and an independent numpy
   fixed-point definition (Jacobi iteration to convergence) on random small images, including
   the 0-valued padding ring and odd / non-square sizes;
@@ -114,6 +116,49 @@ def test_labels_match_reference_live(oracle):
             a, n = oracle.bwlabel2(img, conn, True)
             b, m = oracle.ref_label(img, conn, True)
             assert n == m and np.array_equal(a, b)
+
+
+def _bbox_numpy(labels, bg):
+    """Independent formulation: the scan ends at the first -1 / 0 pixel that is not bg;
+    entries in order of first appearance."""
+    flat = labels.ravel()
+    bad = np.flatnonzero(((flat == -1) | (flat == 0)) & (flat != bg))
+    end = bad[0] if bad.size else flat.size
+    idx = np.flatnonzero(flat[:end] != bg)
+    if idx.size == 0:
+        return np.zeros((5, 0), np.int32)
+    labs, first = np.unique(flat[idx], return_index=True)
+    order = np.argsort(idx[first])
+    W = labels.shape[1]
+    out = []
+    for l in labs[order]:
+        p = idx[flat[idx] == l]
+        x, y = p % W, p // W
+        out.append([l, x.min(), x.max(), y.min(), y.max()])
+    return np.array(out, np.int32).T
+
+
+def test_bbox_matches_reference_fixtures(oracle, golden_dir):
+    d = np.load(os.path.join(golden_dir, "ref_bbox_cases.npz"))
+    k = 0
+    while f"lab{k}" in d:
+        lab, bg = d[f"lab{k}"], int(d[f"bg{k}"])
+        got = oracle.bounding_box(lab, bg)
+        assert np.array_equal(got, d[f"box{k}"]), k
+        assert np.array_equal(got, _bbox_numpy(lab, bg)), k
+        k += 1
+    assert k >= 150
+
+
+def test_bbox_matches_reference_live(oracle):
+    if not oracle.ref_available():
+        pytest.skip("reference ConnComponents not built here (oracle/_ref)")
+    rng = np.random.default_rng(11)
+    for trial in range(60):
+        h, w = rng.integers(1, 60, 2)
+        lab = rng.integers(-1, 9, (h, w)).astype(np.int32)
+        bg = int(rng.choice([-1, 0, 4]))
+        assert np.array_equal(oracle.bounding_box(lab, bg), oracle.ref_bounding_box(lab, bg))
 
 
 def test_recon_reference_queue_fixture(oracle, golden_dir):
