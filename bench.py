@@ -61,6 +61,7 @@ def parse_args():
                         "prints the batched section alone")
     p.add_argument("--no-grad", action="store_true")
     p.add_argument("--no-large", action="store_true")
+    p.add_argument("--no-bbox", action="store_true")
     p.add_argument("--large-size", type=int, default=16384)
     return p.parse_args()
 
@@ -424,6 +425,8 @@ def run_nsgb(args):
         line["differentiable"] = grad_section(dev)
     if not args.no_large:
         line["large"] = large_section(args, dev)
+    if not args.no_bbox:
+        line["bbox"] = bbox_section(args, dev)
     if rank == 0:
         print(json.dumps(line))
     if dist:
@@ -689,6 +692,52 @@ def grad_section(dev, steps=5):
             "forward_algorithmic_GBps": 16 * px / (t_fwd / 1e3) / 1e9,
             "backward_algorithmic_GBps": 16 * px / (t_bwd / 1e3) / 1e9,
             "bytes_per_px": "16 each way (fwd: marker, mask, out, prov; bwd: g, prov, dmarker, dmask)"}
+
+
+# -- per-label bounding boxes ---------------------------------------------------------------------
+def bbox_section(args, dev, steps=20):
+    """ConnComponents::boundingBox after bwlabel (HistologicalEntities.cpp:573) on the dark objects
+    of the headline tile (thousands of components): raster labels in, boxes in raster order of
+    first appearance out."""
+    import torch
+
+    from nsgb import _ffi, synth
+
+    lib = _ffi.lib
+    H = W = args.size
+    mask_h, _ = synth.tile_u8(H, W, args.ellipses, 0)
+    binary = ((torch.from_numpy(mask_h).to(dev) < 128).to(torch.uint8) * 255).contiguous()
+    labels = torch.empty((H, W), dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    lws_n = lib.nsgb_workspace_size(_ffi.OP_BWLABEL, _ffi.U8, H, W)
+    lws_t = torch.empty(lws_n + 256, dtype=torch.uint8, device=dev)
+    lws = (lws_t.data_ptr() + 255) & ~255
+    n_lab = C.c_int32(0)
+    _ffi.check(lib.nsgb_bwlabel(binary.data_ptr(), labels.data_ptr(), H, W, W, W * 4, 8, 1, C.byref(n_lab), lws,
+                                lws_n, sp, None), "bwlabel")
+    bws_n = lib.nsgb_workspace_size(_ffi.OP_BOUNDING_BOX, _ffi.I32, H, W)
+    bws_t = torch.empty(bws_n + 256, dtype=torch.uint8, device=dev)
+    bws = (bws_t.data_ptr() + 255) & ~255
+    cap = max(int(n_lab.value), 1)
+    boxes = torch.empty((5, cap), dtype=torch.int32, device=dev)
+    count_dev = torch.zeros(1, dtype=torch.int32, device=dev)
+    opts = _ffi.Opts(0, 0, 0)
+
+    def f_box():
+        _ffi.check(lib.nsgb_bounding_boxes(labels.data_ptr(), H, W, W * 4, 0, boxes.data_ptr(), cap, None,
+                                           count_dev.data_ptr(), bws, bws_n, sp, C.byref(opts)), "bounding_boxes")
+
+    t = event_ms(f_box, steps, 3, stream)
+    st = lib.nsgb_device_status(C.c_void_p(bws), sp)
+    if st != 0:
+        raise RuntimeError(f"bounding boxes: device status {_ffi.STATUS.get(st, st)}")
+    n_box = int(count_dev.item())
+    if n_box != int(n_lab.value):
+        raise RuntimeError(f"bounding boxes: {n_box} boxes for {n_lab.value} labels")
+    return {"workload": f"{H}x{W} raster labels of the dark objects of the headline tile (mask < 128, "
+                        f"bwlabel 8-conn relabel), background 0",
+            "components": n_box, "ms": t, "mpix_s": H * W / 1e3 / t}
 
 
 # -- large single image -------------------------------------------------------------------------

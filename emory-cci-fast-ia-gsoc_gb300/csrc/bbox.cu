@@ -8,8 +8,9 @@
 // reduce_by_key) orders entries by label value instead; with raster labels (1..n, from the
 // relabel) both orders are the same.  This file follows the CPU order.
 //
-// Schedule: (1) one pass finds where the scan ends (the first -1 / 0 pixel) and checks that
-// every label indexes the per-label arrays; (2) one pass folds each warp's 32 pixels of a row
+// Schedule: (1) one pass finds where the scan ends (the first -1 / 0 pixel) and the largest
+// label, and checks that every label indexes the per-label arrays (which are then initialised
+// up to that label only); (2) one pass folds each warp's 32 pixels of a row
 // by label (match_any + warp min/max reductions) and updates, per label, its first pixel index
 // and the four extremes with one atomic each, skipped when a plain read already shows no
 // improvement (the values only move one way, so a stale read can only cost an atomic); (3) the
@@ -31,7 +32,8 @@ constexpr int kThreads = 256;
 size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
 
 struct BWs {
-  int* hdr;  // [0] status, [1] stop (first -1 / 0 pixel, or INT_MAX), [2] labels present
+  int* hdr;  // [0] status, [1] stop (first -1 / 0 pixel, or INT_MAX), [2] labels present,
+             // [3] largest label seen
   int *first, *mnx, *mxx, *mny, *mxy;
   unsigned* bits;
   size_t bits_bytes;
@@ -69,8 +71,21 @@ __device__ __forceinline__ int32_t label_at(const Img& m, int y, int x) {
   return *(const int32_t*)((const char*)m.plane + (int64_t)y * m.pitch + (int64_t)x * 4);
 }
 
-// Per-label arrays to their neutral values; header.
-__global__ void bbox_init(BWs w, int n) {
+__global__ void bbox_header(BWs w) {
+  w.hdr[0] = 0;
+  w.hdr[1] = INT_MAX;
+  w.hdr[2] = 0;
+  w.hdr[3] = 0;
+}
+
+// Label slots in use: 0 .. the largest label seen (raster labels use few of the px + 1 slots).
+// A plain load: written by an earlier launch, read by every thread, served from L1 after the
+// first warp of each SM.
+__device__ __forceinline__ int slots_used(const BWs& w, int n) { return min(n, w.hdr[3] + 1); }
+
+// Per-label arrays to their neutral values, for the slots in use.
+__global__ void bbox_init(BWs w, int n_slots) {
+  const int n = slots_used(w, n_slots);
   const int stride = gridDim.x * blockDim.x;
   for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < n; l += stride) {
     w.first[l] = INT_MAX;
@@ -79,30 +94,41 @@ __global__ void bbox_init(BWs w, int n) {
     w.mny[l] = INT_MAX;
     w.mxy[l] = -1;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    w.hdr[0] = 0;
-    w.hdr[1] = INT_MAX;
-    w.hdr[2] = 0;
-  }
 }
 
-// Where the scan ends, and label range checks.  Every lane of a warp runs the loop (lanes past
-// the row end take no part), so the warp reductions see full warps.
+// Where the scan ends, the largest label, and label range checks.  Every lane of a warp runs the
+// loop (lanes past the row end take no part), so the warp reductions see full warps; each block
+// folds its rows first and updates the two header words once.
 __global__ void __launch_bounds__(kThreads) bbox_scan(Imgs I, int32_t bgval, BWs w) {
+  __shared__ int s_stop[kThreads / 32], s_top[kThreads / 32];
   const Img& m = I.one;
   const int n = m.H * m.W;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  int stop = INT_MAX, top = 0;
   for (int y = blockIdx.y; y < m.H; y += gridDim.y) {
-    int cand = INT_MAX;
     if (x < m.W) {
       const int32_t l = label_at(m, y, x);
       if (l != bgval) {
-        if (l == -1 || l == 0) cand = y * m.W + x;
+        if (l == -1 || l == 0) stop = min(stop, y * m.W + x);
         else if (l < 1 || l > n) set_status(w.hdr, NSGB_ERR_BAD_ARG);
+        else top = max(top, (int)l);
       }
     }
-    const int s = __reduce_min_sync(NSGB_FULL, cand);
-    if (s != INT_MAX && (threadIdx.x & 31) == 0) atomicMin(w.hdr + 1, s);
+  }
+  stop = __reduce_min_sync(NSGB_FULL, stop);
+  top = __reduce_max_sync(NSGB_FULL, top);
+  if ((threadIdx.x & 31) == 0) {
+    s_stop[threadIdx.x >> 5] = stop;
+    s_top[threadIdx.x >> 5] = top;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < kThreads / 32; ++k) {
+      stop = min(stop, s_stop[k]);
+      top = max(top, s_top[k]);
+    }
+    if (stop != INT_MAX) atomicMin(w.hdr + 1, stop);
+    if (top > 0) atomicMax(w.hdr + 3, top);
   }
 }
 
@@ -134,7 +160,8 @@ __global__ void __launch_bounds__(kThreads) bbox_accum(Imgs I, int32_t bgval, BW
 }
 
 // The first pixel of every present label into the bitmap; labels counted.
-__global__ void __launch_bounds__(kThreads) bbox_mark(BWs w, int n) {
+__global__ void __launch_bounds__(kThreads) bbox_mark(BWs w, int n_slots) {
+  const int n = slots_used(w, n_slots);
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
     const int l = base + threadIdx.x;
@@ -149,7 +176,8 @@ __global__ void __launch_bounds__(kThreads) bbox_mark(BWs w, int n) {
 }
 
 // Entry of each present label at the rank of its first pixel.
-__global__ void __launch_bounds__(kThreads) bbox_out(BWs w, int n, int32_t* boxes, int64_t cap) {
+__global__ void __launch_bounds__(kThreads) bbox_out(BWs w, int n_slots, int32_t* boxes, int64_t cap) {
+  const int n = slots_used(w, n_slots);
   const int stride = gridDim.x * blockDim.x;
   for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < n; l += stride) {
     if (__ldcg(w.mxx + l) < 0) continue;
@@ -179,8 +207,9 @@ cudaError_t bbox_launch(const Imgs& I, const BatchTotals& t, int32_t bgval, void
   if (e != cudaSuccess) return e;
   const int g = ccl::flat_grid(n);
   const dim3 rows = ccl::rowcol_grid(t.rows, t.max_w);
+  bbox_header<<<1, 1, 0, s>>>(w);
+  bbox_scan<<<dim3(rows.x, rows.y < 512 ? rows.y : 512), kThreads, 0, s>>>(I, bgval, w);
   bbox_init<<<g, kThreads, 0, s>>>(w, n);
-  bbox_scan<<<rows, kThreads, 0, s>>>(I, bgval, w);
   bbox_accum<<<rows, kThreads, 0, s>>>(I, bgval, w);
   bbox_mark<<<g, kThreads, 0, s>>>(w, n);
   e = ccl::rank_bits(I, t, w.bits, w.blk, w.wpre, s);
