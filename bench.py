@@ -62,6 +62,9 @@ def parse_args():
     p.add_argument("--no-grad", action="store_true")
     p.add_argument("--no-large", action="store_true")
     p.add_argument("--no-bbox", action="store_true")
+    p.add_argument("--no-candidates", action="store_true")
+    p.add_argument("--candidates-only", action="store_true",
+                   help="profiling aid: only the nucleus-candidate section")
     p.add_argument("--large-size", type=int, default=16384)
     return p.parse_args()
 
@@ -212,6 +215,9 @@ def run_nsgb(args):
     torch.cuda.set_device(local)
     if args.batch_only:
         print(json.dumps({"batched": batched_section(args, torch.device("cuda", local))}))
+        return 0
+    if args.candidates_only:
+        print(json.dumps({"candidates": candidates_section(args, torch.device("cuda", local))}))
         return 0
     dist = None
     if world > 1:
@@ -427,6 +433,8 @@ def run_nsgb(args):
         line["large"] = large_section(args, dev)
     if not args.no_bbox:
         line["bbox"] = bbox_section(args, dev)
+    if not args.no_candidates:
+        line["candidates"] = candidates_section(args, dev)
     if rank == 0:
         print(json.dumps(line))
     if dist:
@@ -738,6 +746,82 @@ def bbox_section(args, dev, steps=20):
     return {"workload": f"{H}x{W} raster labels of the dark objects of the headline tile (mask < 128, "
                         f"bwlabel 8-conn relabel), background 0",
             "components": n_box, "ms": t, "mpix_s": H * W / 1e3 / t}
+
+
+# -- nucleus-candidate stage ----------------------------------------------------------------------
+# recon init + recon, fill (local, merge, flatten, border seeds, output), bw1 label (local, merge,
+# flatten) + kept count, bw2 label (local, merge, flatten), seeds, output: csrc/ops.cu candidates_impl
+CANDIDATE_KERNELS = 16
+
+
+def candidates_section(args, dev, steps=20):
+    """The stage after the 19x19 opening in plFindNucleusCandidates (HistologicalEntities.cpp:
+    195-275) on the headline tile: rc = inverted tile, rc_open = rc - 90 (saturating; an
+    opening's stand-in, <= rc), rbc = dark objects of a second tile.  One nsgb_nucleus_candidates
+    call per step; L2 flushed between steps; rc_open restored (untimed) before each."""
+    import numpy as np
+    import torch
+
+    from nsgb import _ffi, synth
+
+    lib = _ffi.lib
+    H = W = args.size
+    mask_h, _ = synth.tile_u8(H, W, args.ellipses, 0)
+    rc_h = (255 - mask_h).astype(np.uint8)
+    open_h = np.where(rc_h > 90, rc_h - 90, 0).astype(np.uint8)
+    other_h, _ = synth.tile_u8(H, W, args.ellipses // 4, 1)
+    rbc_h = np.where(other_h < 128, 255, 0).astype(np.uint8)
+    rc, open_src, rbc = (torch.from_numpy(a).to(dev) for a in (rc_h, open_h, rbc_h))
+    work = torch.empty_like(open_src)
+    seg = torch.empty_like(open_src)
+    nb = lib.nsgb_workspace_size(_ffi.OP_NUCLEUS_CANDIDATES, _ffi.U8, H, W)
+    ws_t = torch.empty(nb + 256, dtype=torch.uint8, device=dev)
+    ws = (ws_t.data_ptr() + 255) & ~255
+    n_dev = torch.zeros(1, dtype=torch.int32, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    opts = _ffi.Opts(0, 0, 0)
+
+    def call():
+        _ffi.check(lib.nsgb_nucleus_candidates(work.data_ptr(), rc.data_ptr(), rbc.data_ptr(), seg.data_ptr(), H, W, W,
+                                               80.0, 45.0, 11, 1000, None, n_dev.data_ptr(), ws, nb, sp,
+                                               C.byref(opts)), "nucleus_candidates")
+
+    for _ in range(3):
+        work.copy_(open_src)
+        call()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in evs:
+        work.copy_(open_src)
+        flush.fill_(1)
+        a.record(stream)
+        call()
+        b.record(stream)
+    torch.cuda.synchronize()
+    ms = sorted(a.elapsed_time(b) for a, b in evs)
+    t = sum(ms) / len(ms)
+    st = lib.nsgb_device_status(C.c_void_p(ws), sp)
+    if st != 0:
+        raise RuntimeError(f"nucleus candidates: device status {_ffi.STATUS.get(st, st)}")
+    res = {"workload": f"{H}x{W} u8: rc = 255 - headline tile, rc_open = rc - 90 (saturating), rbc = mask < 128 of a "
+                       f"second tile ({args.ellipses // 4} ellipses); G1 80, G2 45, areas [11, 1000)",
+           "kept_components": int(n_dev.item()), "candidate_px": int((seg != 0).sum().item()),
+           "ms": t, "ms_median": ms[len(ms) // 2], "mpix_s": H * W / 1e3 / t, "gpu_launches_per_call": CANDIDATE_KERNELS,
+           "l2": "flushed between steps (512 MB write)"}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        t0 = time.perf_counter()
+        exp, n_exp = oracle.nucleus_candidates(rc_h, open_h, rbc_h)
+        cpu_s = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": H * W / 1e6 / cpu_s, "unit": "MPix/s", "cores": 1, "kind": "port",
+                               "sample": f"one serial run of the stage on the full {H}x{W} tile, {cpu_s:.2f} s "
+                                         f"(oracle restatement, composed step by step)",
+                               "same_kept_count": n_exp == res["kept_components"]}
+    return res
 
 
 # -- large single image -------------------------------------------------------------------------

@@ -186,5 +186,13 @@ cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int
   return cudaGetLastError();
 }
 
+cudaError_t count_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, unsigned* bits,
+                        int* counts, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * 2 * (size_t)t.n, s);
+  if (e != cudaSuccess) return e;
+  mark_roots<<<list_grid(t.px), kRankThreads, 0, s>>>(I, f, (int)t.px, lo, hi, bits, counts);
+  return cudaGetLastError();
+}
+
 }  // namespace ccl
 }  // namespace nsgb

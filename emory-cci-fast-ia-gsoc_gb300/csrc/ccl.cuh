@@ -529,6 +529,10 @@ cudaError_t label(const Cls& cls, const Imgs& I, const BatchTotals& t, int conn,
 // block) are scratch.
 cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, int* rank,
                        unsigned* bits, size_t bits_bytes, int* block_tmp, int* wpre, int* counts, cudaStream_t s);
+// The counts of rank_roots alone (no ranks).  `bits` receives the global roots' bits (scratch,
+// not cleared first).
+cudaError_t count_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, unsigned* bits,
+                        int* counts, cudaStream_t s);
 constexpr int kBlockPx = 1024;
 
 // The counting half of rank_roots for any bitmap of the images' pixels: per 1024-px block the

@@ -99,6 +99,22 @@ struct ClsNotAbove {  // hole filling of (R > thr): the complement class !(R > t
   }
 };
 
+// The red-channel valleys of the nucleus-candidate stage, D = rc - R (OpenCV's saturating u8
+// Mat subtraction, HistologicalEntities.cpp:199), from the reconstruction R (plane, written by
+// an earlier launch) and the image rc it was taken under (aux).
+__device__ __forceinline__ uint8_t valley(const Img& m, int y, int x) {
+  const int d = (int)px<uint8_t>(m.aux, m.pitch, y, x) - (int)pxcg<uint8_t>(m.plane, m.pitch, y, x);
+  return (uint8_t)(d > 0 ? d : 0);
+}
+struct ClsValleyNotAbove {  // hole filling of (D > g1): the complement class !(D > g1)
+  GtThr<uint8_t> gt;
+  __device__ uint32_t operator()(const Img& m, int y, int x) const { return gt(valley(m, y, x)) ? 0u : 1u; }
+};
+struct ClsValleyAbove {  // bwselect's image D > g2
+  GtThr<uint8_t> gt;
+  __device__ uint32_t operator()(const Img& m, int y, int x) const { return gt(valley(m, y, x)) ? 1u : 0u; }
+};
+
 // Seeds (pixels that flag their component's root).
 template <class Cls>
 struct SeedBorder {
@@ -112,6 +128,22 @@ struct SeedBoth {  // a != 0 and b != 0, with a = plane or aux as selected
     const void* a = a_is_plane ? m.plane : m.aux;
     const void* b = a_is_plane ? m.aux : m.plane;
     return pxcg<T>(a, m.pitch, y, x) != (T)0 && px<T>(b, m.pitch, y, x) != (T)0;
+  }
+};
+
+// bwselect's seeds in the nucleus-candidate stage: D > g2 on a pixel of a filled component
+// (forest LF, areas A) whose area lies in [lo, hi) -- bw2 & bw1_t without writing bw1_t.
+struct SeedCandidate {
+  GtThr<uint8_t> gt;
+  const int* LF;
+  const int* A;
+  int lo, hi;
+  __device__ bool operator()(const Img& m, int y, int x) const {
+    if (!gt(valley(m, y, x))) return false;
+    const int r = ccl::root_of_ro(LF, (int64_t)m.px_base + (int64_t)y * m.W + x);
+    if (r < 0) return false;
+    const int a = __ldg(A + r);
+    return a >= lo && a < hi;
   }
 };
 
@@ -180,6 +212,27 @@ __global__ void bwselect_out_kernel(Imgs I, int total_rows, void* out, const int
     const T v = px<T>(m.plane, m.pitch, y, x);
     const int r = ccl::root_of_ro(L, (int64_t)m.px_base + (int64_t)y * m.W + x);
     *pxp<T>(out, m.pitch, y, x) = (v != (T)0 && r >= 0 && ccl::test_bit(bits, r)) ? v : (T)0;
+  });
+}
+
+// Nucleus candidates: 255 on a component of (D > g2) that holds a seed, where rbc is 0
+// (bwselect(bw2, bw1_t, 8) & (rbc == 0), HistologicalEntities.cpp:268-271).  L2 is the forest
+// of D > g2 (root -1 off it), `bits` its seeded roots.
+__global__ void candidates_out_kernel(Imgs I, int total_rows, const int* __restrict__ L2,
+                                      const unsigned* __restrict__ bits, const uint8_t* __restrict__ rbc,
+                                      uint8_t* out) {
+  ccl::for_batch_quads(I, total_rows, [&](const Img& m, int y, int x, int n) {
+    int r[4];
+    ccl::roots4_ro(L2, (int64_t)m.px_base + (int64_t)y * m.W + x, n, r);
+    const uint8_t* q = rbc + (int64_t)y * m.pitch + x;
+    bool sel[4];
+    uint8_t o[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      sel[k] = (k > 0 && r[k] == r[k - 1]) ? sel[k - 1] : (r[k] >= 0 && ccl::test_bit(bits, r[k]));
+      o[k] = (k < n && sel[k] && __ldg(q + k) == 0) ? 255 : 0;
+    }
+    store4_u8(pxp<uint8_t>(out, m.pitch, y, x), n, o);
   });
 }
 
@@ -551,6 +604,41 @@ cudaError_t chain_impl(int dtype, const Plan& P, const Ws& w, int recon_conn, do
   return e;
 }
 
+// The nucleus-candidate stage on one image (plane = rc_open, reconstructed in place; aux = rc):
+// (a) R = recon(rc_open, rc, 8); (b) bw1 = imfillHoles(D > g1, 4) into F, the threshold fused
+// into the labelling's classifier; (c) bw1's 8-connected components and their areas, the kept
+// ones counted (w.counts[1]); (d) bwselect(D > g2, bw1_t, 8): D > g2 labelled into a second
+// forest (the rank array R, unused here), its roots seeded straight from bw1's forest and
+// areas, so bw1_t is never written; (e) the output with rbc == 0 folded in.
+cudaError_t candidates_impl(const Plan& P, const Ws& w, double g1, double g2, int lo, int hi, const uint8_t* rbc,
+                            uint8_t* out, const nsgb_opts* opts, cudaStream_t s) {
+  const BatchTotals& t = P.t;
+  const ClsValleyNotAbove holes{GtThr<uint8_t>::make(g1)};
+  const GtThr<uint8_t> gt2 = GtThr<uint8_t>::make(g2);
+  cudaError_t e = recon_timed(opts, NSGB_U8, P, 8, false, false, w.recon, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.bits, 0, w.bits_bytes, s);
+  if (e == cudaSuccess) e = ccl::label(holes, P.I, t, 4, w.forest(false), s);
+  if (e == cudaSuccess) {
+    const int gx = grid1d(t.perimeter_max) > 64 ? 64 : grid1d(t.perimeter_max);
+    ccl::ccl_seed_border<SeedBorder<ClsValleyNotAbove>><<<dim3(gx, t.n), 256, 0, s>>>(
+        P.I, w.L, SeedBorder<ClsValleyNotAbove>{holes}, w.bits);
+    fill_out_kernel<uint8_t><<<qrb(t), 256, 0, s>>>(P.I, t.rows, w.L, w.bits, w.F, nullptr, 0, (uint8_t)255);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = ccl::label(ClsDenseU8{w.F}, P.I, t, 8, w.forest(true), s);
+  if (e == cudaSuccess) e = ccl::count_roots(P.I, t, w.forest(true), lo, hi, w.bits, w.counts, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.bits, 0, w.bits_bytes, s);
+  const ccl::Forest sel{w.R, nullptr, w.roots, w.nroots};
+  if (e == cudaSuccess) e = ccl::label(ClsValleyAbove{gt2}, P.I, t, 8, sel, s);
+  if (e == cudaSuccess) {
+    ccl::ccl_seed_pixels<SeedCandidate><<<rcb(t), 256, 0, s>>>(P.I, t.rows, w.R, SeedCandidate{gt2, w.L, w.A, lo, hi},
+                                                               w.bits);
+    candidates_out_kernel<<<qrb(t), 256, 0, s>>>(P.I, t.rows, w.R, w.bits, rbc, out);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
 }  // namespace
 }  // namespace nsgb
 
@@ -599,8 +687,8 @@ nsgb_status check_ws(void* ws, size_t ws_bytes, int op, int dtype, int64_t rows,
 extern "C" {
 
 size_t nsgb_workspace_size(int op, int dtype, int64_t rows, int64_t cols) {
-  if (rows <= 0 || cols <= 0) return 0;
-  if (op == NSGB_OP_BWLABEL || op == NSGB_OP_BWAREAOPEN) dtype = NSGB_U8;
+  if (rows <= 0 || cols <= 0 || op < 0 || op > NSGB_OP_NUCLEUS_CANDIDATES) return 0;
+  if (op == NSGB_OP_BWLABEL || op == NSGB_OP_BWAREAOPEN || op == NSGB_OP_NUCLEUS_CANDIDATES) dtype = NSGB_U8;
   if (dtype < 0 || dtype > 3) return 0;
   if (op == NSGB_OP_IMRECONSTRUCT || op == NSGB_OP_HMIN) return align256(recon_workspace_bytes(dtype, rows, cols));
   if (op == NSGB_OP_BOUNDING_BOX) return align256(bbox_workspace_bytes(rows * cols));
@@ -871,6 +959,27 @@ nsgb_status nsgb_bounding_boxes(const int32_t* labels, int64_t rows, int64_t col
   cudaError_t e = bbox_launch(P.I, P.t, bgval, ws, boxes, capacity, count_dev, s);
   if (e == cudaSuccess && count) {
     e = cudaMemcpyAsync(count, (const int*)ws + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  return finish(e, ws, s, opts);
+}
+
+nsgb_status nsgb_nucleus_candidates(uint8_t* rc_open, const uint8_t* rc, const uint8_t* rbc, uint8_t* seg_out,
+                                    int64_t rows, int64_t cols, int64_t pitch, double g1, double g2,
+                                    int32_t area_min, int32_t area_max, int32_t* n_kept, int32_t* n_kept_dev,
+                                    void* ws, size_t ws_bytes, nsgb_stream_t stream, const nsgb_opts* opts) {
+  if (!rc_open || !rc || !rbc || !seg_out || !valid_dims(rows, cols) || !valid_pitch(pitch, cols, 1))
+    return NSGB_ERR_BAD_ARG;
+  nsgb_status st = check_ws(ws, ws_bytes, NSGB_OP_NUCLEUS_CANDIDATES, NSGB_U8, rows, cols);
+  if (st != NSGB_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const Plan P = single_plan(NSGB_U8, rc_open, rc, rows, cols, pitch);
+  Ws w = carve(ws, P.t);
+  cudaError_t e = candidates_impl(P, w, g1, g2, area_min, area_max, rbc, seg_out, opts, s);
+  if (e == cudaSuccess && n_kept_dev)
+    e = cudaMemcpyAsync(n_kept_dev, w.counts + 1, sizeof(int32_t), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess && n_kept) {
+    e = cudaMemcpyAsync(n_kept, w.counts + 1, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   }
   return finish(e, ws, s, opts);

@@ -305,6 +305,32 @@ def chain(marker: torch.Tensor, mask: torch.Tensor, recon_conn: int = 8, thr: fl
             "n_kept": int(nk.value)}
 
 
+def nucleus_candidates(rc: torch.Tensor, rc_open: torch.Tensor, rbc: torch.Tensor, g1: float = 80, g2: float = 45,
+                       area_min: int = 11, area_max: int = 1000) -> Tuple[torch.Tensor, int]:
+    """The nucleus-candidate stage after the opening (HistologicalEntities.cpp:195-275) on the
+    device, uint8 images of one shape: reconstruction of `rc_open` under `rc`, valleys
+    D = rc - recon, bw1 = imfillHoles(D > g1), bw1_t = bwareaopen2(bw1, [area_min, area_max)),
+    seg = bwselect(D > g2, bw1_t, 8) & (rbc == 0).  Returns (seg as 255 / 0, number of
+    components kept in bw1_t); the reference stops with NO_CANDIDATES_LEFT when that is 0."""
+    for t, n in ((rc, "rc"), (rc_open, "rc_open"), (rbc, "rbc")):
+        _check_image(t, n)
+        if t.dtype != torch.uint8:
+            raise NsgbError(2, f"{n} must be uint8")
+    _same_shape(rc, rc_open, "nucleus_candidates")
+    _same_shape(rc, rbc, "nucleus_candidates")
+    rec = _contig(rc_open).clone()
+    img, red = _contig(rc), _contig(rbc)
+    rows, cols = rec.shape
+    seg = torch.empty((rows, cols), dtype=torch.uint8, device=rec.device)
+    ws, nb = _ws(_ffi.OP_NUCLEUS_CANDIDATES, _ffi.U8, rows, cols, rec.device)
+    nk = C.c_int32(0)
+    st = lib.nsgb_nucleus_candidates(rec.data_ptr(), img.data_ptr(), red.data_ptr(), seg.data_ptr(), rows, cols,
+                                     _pitch(rec), float(g1), float(g2), int(area_min), int(area_max), C.byref(nk),
+                                     None, ws, nb, _stream(), None)
+    _ffi.check(st, "nucleus_candidates")
+    return seg, int(nk.value)
+
+
 class BatchPlan:
     """A prepared batch of tiles (nsgb_batch_prepare): the image table lives in a workspace
     owned by this object; `chain()` / `reconstruct()` then launch kernels only."""

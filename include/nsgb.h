@@ -49,7 +49,8 @@ typedef enum {
   NSGB_OP_BWLABEL = 5,
   NSGB_OP_BWAREAOPEN = 6,
   NSGB_OP_CHAIN = 7,
-  NSGB_OP_BOUNDING_BOX = 8
+  NSGB_OP_BOUNDING_BOX = 8,
+  NSGB_OP_NUCLEUS_CANDIDATES = 9
 } nsgb_op;
 
 typedef struct {
@@ -189,6 +190,24 @@ nsgb_status nsgb_chain(int dtype, void* marker, const void* mask, int64_t rows, 
                        int32_t area_min, int32_t area_max, uint8_t* fill_out, int32_t* labels_out,
                        uint8_t* area_out, int32_t* n_labels, int32_t* n_kept, void* ws,
                        size_t ws_bytes, nsgb_stream_t stream, const nsgb_opts* opts);
+
+/* The nucleus-candidate stage after the opening, kept on the device: the tail of
+ * HistologicalEntities::plFindNucleusCandidates (src/segment/HistologicalEntities.cpp:195-275;
+ * GPU twin HistologicalEntitiesGPU.cpp:307-432):
+ *   R    = imreconstruct(rc_open, rc, 8)             in place on `rc_open`
+ *   D    = rc - R                                    (u8, saturating)
+ *   bw1  = imfillHoles(D > g1, binary, 4)
+ *   bw1t = bwareaopen2(bw1, unlabeled, flatten, area_min, area_max, 8)   -> n_kept
+ *   seg  = bwselect(D > g2, bw1t, 8) & (rbc == 0)    -> 255 / 0 in `seg_out`
+ * The reference uses g1 = 80, g2 = 45 and [11, 1000), and returns NO_CANDIDATES_LEFT when
+ * n_kept is 0 without writing its output; here `seg_out` is then all 0 and n_kept tells the
+ * caller.  rc_open, rc, rbc and seg_out are u8 device images sharing `pitch` (bytes); seg_out
+ * may be rc_open.  n_kept: host (optional; synchronizes) and / or n_kept_dev (device, optional).
+ * Workspace: nsgb_workspace_size(NSGB_OP_NUCLEUS_CANDIDATES, NSGB_U8, rows, cols). */
+nsgb_status nsgb_nucleus_candidates(uint8_t* rc_open, const uint8_t* rc, const uint8_t* rbc, uint8_t* seg_out,
+                                    int64_t rows, int64_t cols, int64_t pitch, double g1, double g2,
+                                    int32_t area_min, int32_t area_max, int32_t* n_kept, int32_t* n_kept_dev,
+                                    void* ws, size_t ws_bytes, nsgb_stream_t stream, const nsgb_opts* opts);
 
 /* ---- Batches: many images of uneven sizes in one persistent reconstruction launch and one
  * launch per labelling stage (the reference's imreconstructQueueThroughput<T>,

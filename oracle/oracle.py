@@ -155,6 +155,21 @@ def chain(marker: np.ndarray, mask: np.ndarray, recon_conn=8, thr=128.0, fill_co
             "n_kept": int(kept)}
 
 
+def nucleus_candidates(rc: np.ndarray, rc_open: np.ndarray, rbc: np.ndarray, g1=80.0, g2=45.0, lo=11, hi=1000):
+    """The candidate stage of HistologicalEntities::plFindNucleusCandidates after the opening
+    (src/segment/HistologicalEntities.cpp:195-275), composed from the restated steps:
+    recon 8-conn (195), diffIm = rc - recon saturating (199), imfillHoles(diffIm > G1, binary, 4)
+    (214-219), bwareaopen2(.., false, true, lo, hi, 8) (247), bwselect(diffIm > G2, bw1_t, 8)
+    (268) and `& (rbc == 0)` (271).  Returns (seg_norbc, compcount2)."""
+    rc, rc_open, rbc = _c(rc), _c(rc_open), _c(rbc)
+    rec = imreconstruct(rc_open, rc, 8)
+    diff = np.where(rc > rec, rc.astype(np.int16) - rec, 0).astype(np.uint8)
+    bw1 = imfill_holes(threshold_gt(diff, g1), True, 4)
+    bw1_t, n = bwareaopen2(bw1, False, True, lo, hi, 8)
+    seg = bwselect(threshold_gt(diff, g2), bw1_t, 8)
+    return np.where(rbc == 0, seg, 0).astype(np.uint8), n
+
+
 def chain_replicas_seconds(marker: np.ndarray, mask: np.ndarray, threads: int, reps: int) -> float:
     marker, mask = _c(marker), _c(mask)
     return float(lib.orc_chain_replicas_seconds(_p(marker), _p(mask), mask.shape[0], mask.shape[1], threads, reps))

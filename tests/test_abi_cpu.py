@@ -40,9 +40,15 @@ def test_status_strings_and_workspace_sizes():
     lib = ffi.lib
     assert lib.nsgb_status_string(0) == b"ok"
     assert b"workspace" in lib.nsgb_status_string(3)
-    for op in range(9):
+    for op in range(10):
         for dt in range(4):
             assert lib.nsgb_workspace_size(op, dt, 64, 64) > 0
+    assert lib.nsgb_workspace_size(10, 0, 64, 64) == 0
+    assert lib.nsgb_workspace_size(-1, 0, 64, 64) == 0
+    # nucleus candidates: the chain's u8 workspace whatever dtype is asked for
+    for dt in range(4):
+        assert lib.nsgb_workspace_size(ffi.OP_NUCLEUS_CANDIDATES, dt, 300, 400) == \
+            lib.nsgb_workspace_size(ffi.OP_CHAIN, ffi.U8, 300, 400)
     # bounding boxes: five per-label planes plus the bitmap and rank scratch
     assert lib.nsgb_workspace_size(ffi.OP_BOUNDING_BOX, ffi.I32, 4096, 4096) >= 5 * 4 * 4096 * 4096
     assert lib.nsgb_workspace_size(0, 0, 0, 10) == 0
@@ -66,3 +72,10 @@ def test_argument_errors_need_no_gpu():
     assert lib.nsgb_bounding_boxes(None, 4, 4, 16, 0, 1, 4, None, None, 1, 1 << 20, None, None) == 1
     assert lib.nsgb_bounding_boxes(1, 4, 4, 8, 0, 1, 4, None, None, 1, 1 << 20, None, None) == 1
     assert lib.nsgb_bounding_boxes(1, 4, 4, 16, 0, None, 4, None, None, 1, 1 << 20, None, None) == 1
+    # nucleus candidates: null image, pitch below the row, missing workspace
+    assert lib.nsgb_nucleus_candidates(None, 1, 1, 1, 4, 4, 4, 80.0, 45.0, 11, 1000, None, None, 1, 1 << 20,
+                                       None, None) == 1
+    assert lib.nsgb_nucleus_candidates(1, 1, 1, 1, 4, 4, 3, 80.0, 45.0, 11, 1000, None, None, 1, 1 << 20,
+                                       None, None) == 1
+    assert lib.nsgb_nucleus_candidates(1, 1, 1, 1, 4, 4, 4, 80.0, 45.0, 11, 1000, None, None, None, 0,
+                                       None, None) == 3

@@ -264,3 +264,58 @@ def test_chain_small(oracle):
     assert np.array_equal(r["labels"], lab) and n == r["n_labels"]
     a, k = oracle.bwareaopen2(r["fill"], False, True, 11, 1000, 8)
     assert np.array_equal(r["area"], a) and k == r["n_kept"]
+
+
+def np_candidates(rc, rc_open, rbc, g1=80, g2=45, lo=11, hi=1000):
+    """Independent statement of HistologicalEntities.cpp:195-275: numpy reconstruction, scipy
+    hole filling (4-connected background), 8-connected areas and component selection."""
+    rec = np_recon(rc_open, rc, 8)
+    diff = np.where(rc > rec, rc.astype(np.int16) - rec, 0)
+    bw1 = np_fill_binary(np.where(diff > g1, 255, 0).astype(np.uint8), 4) != 0
+    lab, _ = ndi.label(bw1, structure=struct(8))
+    areas = np.bincount(lab.ravel())
+    keep = (areas >= lo) & (areas < hi)
+    keep[0] = False
+    bw1_t = keep[lab]
+    bw2 = diff > g2
+    lab2, _ = ndi.label(bw2, structure=struct(8))
+    sel = np.unique(lab2[bw1_t & bw2])
+    sel = sel[sel > 0]
+    seg = np.isin(lab2, sel) & bw2 & (rbc == 0)
+    return np.where(seg, 255, 0).astype(np.uint8), int(keep.sum())
+
+
+@pytest.mark.parametrize("case", ["tile", "noise", "small", "row", "col"])
+def test_nucleus_candidates_composition(oracle, case):
+    import candidates_inputs as ci
+
+    rng = np.random.default_rng(11)
+    if case == "tile":
+        rc, rc_open, rbc = ci.tile(128, 96, 14, 3)
+    elif case == "noise":
+        rc, rc_open, rbc = ci.noise(rng, 40, 52)
+    elif case == "small":
+        rc, rc_open, rbc = ci.tile(9, 13, 2, 5, drop=120)
+    elif case == "row":
+        rc, rc_open, rbc = ci.noise(rng, 1, 90)
+    else:
+        rc, rc_open, rbc = ci.noise(rng, 90, 1)
+    seg, n = oracle.nucleus_candidates(rc, rc_open, rbc)
+    exp, n_exp = np_candidates(rc, rc_open, rbc)
+    assert n == n_exp
+    assert np.array_equal(seg, exp)
+    if case == "tile":
+        assert n > 0 and seg.any()
+
+
+def test_nucleus_candidates_thresholds(oracle):
+    import candidates_inputs as ci
+
+    rc, rc_open, rbc = ci.tile(120, 120, 20, 7)
+    for g1, g2, lo, hi in [(80, 45, 11, 1000), (40, 60, 1, 10 ** 6), (255, 45, 11, 1000), (80.5, 44.9, 30, 200)]:
+        seg, n = oracle.nucleus_candidates(rc, rc_open, rbc, g1, g2, lo, hi)
+        exp, n_exp = np_candidates(rc, rc_open, rbc, g1, g2, lo, hi)
+        assert n == n_exp and np.array_equal(seg, exp), (g1, g2, lo, hi)
+    # nothing above g1 = 255: no component survives, nothing is selected
+    seg, n = oracle.nucleus_candidates(rc, rc_open, rbc, 255, 45)
+    assert n == 0 and not seg.any()
