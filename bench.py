@@ -748,78 +748,114 @@ def bbox_section(args, dev, steps=20):
             "components": n_box, "ms": t, "mpix_s": H * W / 1e3 / t}
 
 
-# -- nucleus-candidate stage ----------------------------------------------------------------------
+# -- S1 after the colour steps: opening and nucleus-candidate stage ------------------------------
 # recon init + recon, fill (local, merge, flatten, border seeds, output), bw1 label (local, merge,
 # flatten) + kept count, bw2 label (local, merge, flatten), seeds, output: csrc/ops.cu candidates_impl
 CANDIDATE_KERNELS = 16
+OPEN_KERNELS = 2  # erosion, dilation (csrc/morph.cu)
+
+
+def timed_steps(stream, steps, before, call):
+    """Mean / median ms of `call` over `steps` runs, each after an untimed `before`."""
+    import torch
+
+    for _ in range(3):
+        before()
+        call()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in evs:
+        before()
+        a.record(stream)
+        call()
+        b.record(stream)
+    torch.cuda.synchronize()
+    ms = sorted(a.elapsed_time(b) for a, b in evs)
+    return sum(ms) / len(ms), ms[len(ms) // 2]
 
 
 def candidates_section(args, dev, steps=20):
-    """The stage after the 19x19 opening in plFindNucleusCandidates (HistologicalEntities.cpp:
-    195-275) on the headline tile: rc = inverted tile, rc_open = rc - 90 (saturating; an
-    opening's stand-in, <= rc), rbc = dark objects of a second tile.  One nsgb_nucleus_candidates
-    call per step; L2 flushed between steps; rc_open restored (untimed) before each."""
+    """S1 of plFindNucleusCandidates after the colour steps (HistologicalEntities.cpp:184-275) on
+    the headline tile: rc = the inverted tile (nuclei bright), rc_open = morphOpen(rc, 19 x 19
+    disk), then the candidate stage with rbc = dark objects of a second tile.  Timed: the opening
+    alone, the candidate stage alone (rc_open restored untimed), and both back to back from rc.
+    L2 flushed before every step."""
     import numpy as np
     import torch
 
-    from nsgb import _ffi, synth
+    from nsgb import _ffi, disk19, synth
 
     lib = _ffi.lib
     H = W = args.size
     mask_h, _ = synth.tile_u8(H, W, args.ellipses, 0)
     rc_h = (255 - mask_h).astype(np.uint8)
-    open_h = np.where(rc_h > 90, rc_h - 90, 0).astype(np.uint8)
     other_h, _ = synth.tile_u8(H, W, args.ellipses // 4, 1)
     rbc_h = np.where(other_h < 128, 255, 0).astype(np.uint8)
-    rc, open_src, rbc = (torch.from_numpy(a).to(dev) for a in (rc_h, open_h, rbc_h))
-    work = torch.empty_like(open_src)
-    seg = torch.empty_like(open_src)
-    nb = lib.nsgb_workspace_size(_ffi.OP_NUCLEUS_CANDIDATES, _ffi.U8, H, W)
-    ws_t = torch.empty(nb + 256, dtype=torch.uint8, device=dev)
-    ws = (ws_t.data_ptr() + 255) & ~255
+    rc, rbc = (torch.from_numpy(a).to(dev) for a in (rc_h, rbc_h))
+    open_src = torch.empty_like(rc)
+    work = torch.empty_like(rc)
+    seg = torch.empty_like(rc)
+    kern = np.ascontiguousarray(disk19())
+    kp = kern.ctypes.data_as(C.c_void_p)
+    nb_c = lib.nsgb_workspace_size(_ffi.OP_NUCLEUS_CANDIDATES, _ffi.U8, H, W)
+    nb_o = lib.nsgb_workspace_size(_ffi.OP_MORPH_OPEN, _ffi.U8, H, W)
+    ws_t = [torch.empty(n + 256, dtype=torch.uint8, device=dev) for n in (nb_c, nb_o)]
+    ws_c, ws_o = [(t.data_ptr() + 255) & ~255 for t in ws_t]
     n_dev = torch.zeros(1, dtype=torch.int32, device=dev)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
     sp = C.c_void_p(stream.cuda_stream)
     opts = _ffi.Opts(0, 0, 0)
 
-    def call():
+    def open_into(dst):
+        _ffi.check(lib.nsgb_morph_open(rc.data_ptr(), dst.data_ptr(), H, W, W, W, kp, 19, ws_o, nb_o, sp,
+                                       C.byref(opts)), "morph_open")
+
+    def candidates():
         _ffi.check(lib.nsgb_nucleus_candidates(work.data_ptr(), rc.data_ptr(), rbc.data_ptr(), seg.data_ptr(), H, W, W,
-                                               80.0, 45.0, 11, 1000, None, n_dev.data_ptr(), ws, nb, sp,
+                                               80.0, 45.0, 11, 1000, None, n_dev.data_ptr(), ws_c, nb_c, sp,
                                                C.byref(opts)), "nucleus_candidates")
 
-    for _ in range(3):
-        work.copy_(open_src)
-        call()
-    torch.cuda.synchronize()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    for a, b in evs:
+    def restore():
         work.copy_(open_src)
         flush.fill_(1)
-        a.record(stream)
-        call()
-        b.record(stream)
-    torch.cuda.synchronize()
-    ms = sorted(a.elapsed_time(b) for a, b in evs)
-    t = sum(ms) / len(ms)
-    st = lib.nsgb_device_status(C.c_void_p(ws), sp)
-    if st != 0:
-        raise RuntimeError(f"nucleus candidates: device status {_ffi.STATUS.get(st, st)}")
-    res = {"workload": f"{H}x{W} u8: rc = 255 - headline tile, rc_open = rc - 90 (saturating), rbc = mask < 128 of a "
-                       f"second tile ({args.ellipses // 4} ellipses); G1 80, G2 45, areas [11, 1000)",
+
+    open_into(open_src)
+    t_open, t_open_med = timed_steps(stream, steps, lambda: flush.fill_(1), lambda: open_into(work))
+    t_cand, t_cand_med = timed_steps(stream, steps, restore, candidates)
+    t_s1, t_s1_med = timed_steps(stream, steps, lambda: flush.fill_(1), lambda: (open_into(work), candidates()))
+    for w in (ws_c, ws_o):
+        st = lib.nsgb_device_status(C.c_void_p(w), sp)
+        if st != 0:
+            raise RuntimeError(f"S1: device status {_ffi.STATUS.get(st, st)}")
+    px = H * W
+    res = {"workload": f"{H}x{W} u8: rc = 255 - headline tile, rc_open = morphOpen(rc, 19x19 disk), rbc = mask < 128 "
+                       f"of a second tile ({args.ellipses // 4} ellipses); G1 80, G2 45, areas [11, 1000)",
            "kept_components": int(n_dev.item()), "candidate_px": int((seg != 0).sum().item()),
-           "ms": t, "ms_median": ms[len(ms) // 2], "mpix_s": H * W / 1e3 / t, "gpu_launches_per_call": CANDIDATE_KERNELS,
-           "l2": "flushed between steps (512 MB write)"}
+           "open_ms": t_open, "open_mpix_s": px / 1e3 / t_open,
+           "open_algorithmic_GBps": 4 * px / (t_open / 1e3) / 1e9,
+           "open_bytes_per_px": "4 (erosion: read, write; dilation: read, write)",
+           "candidates_ms": t_cand, "candidates_mpix_s": px / 1e3 / t_cand,
+           "s1_ms": t_s1, "s1_mpix_s": px / 1e3 / t_s1,
+           "medians_ms": {"open": t_open_med, "candidates": t_cand_med, "s1": t_s1_med},
+           "gpu_launches_per_s1": OPEN_KERNELS + CANDIDATE_KERNELS,
+           "l2": "flushed before every step (512 MB write)"}
     if not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle
 
+        strip = 512
         t0 = time.perf_counter()
-        exp, n_exp = oracle.nucleus_candidates(rc_h, open_h, rbc_h)
-        cpu_s = time.perf_counter() - t0
-        res["cpu_baseline"] = {"value": H * W / 1e6 / cpu_s, "unit": "MPix/s", "cores": 1, "kind": "port",
-                               "sample": f"one serial run of the stage on the full {H}x{W} tile, {cpu_s:.2f} s "
-                                         f"(oracle restatement, composed step by step)",
+        oracle.morph_open(rc_h[:strip], kern)
+        t_o = time.perf_counter() - t0
+        open_h = open_src.cpu().numpy()
+        t0 = time.perf_counter()
+        _, n_exp = oracle.nucleus_candidates(rc_h, open_h, rbc_h)
+        t_c = time.perf_counter() - t0
+        s1_s = t_o * H / strip + t_c
+        res["cpu_baseline"] = {"value": px / 1e6 / s1_s, "unit": "MPix/s", "cores": 1, "kind": "port",
+                               "sample": f"oracle opening of a {strip}x{W} strip ({t_o:.2f} s, scaled to {H} rows) "
+                                         f"plus the candidate stage on the full tile ({t_c:.2f} s), one host core",
                                "same_kept_count": n_exp == res["kept_components"]}
     return res
 

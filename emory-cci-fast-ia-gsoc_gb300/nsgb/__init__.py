@@ -305,6 +305,48 @@ def chain(marker: torch.Tensor, mask: torch.Tensor, recon_conn: int = 8, thr: fl
             "n_kept": int(nk.value)}
 
 
+def disk19() -> "np.ndarray":
+    """The 19 x 19 disk the reference opens the red channel with (HistologicalEntities.cpp:
+    162-185, MATLAB's strel('disk', 10) written out): centred rows of widths 11, 13, 15, 17,
+    eleven of 19, then 17, 15, 13, 11."""
+    import numpy as np
+
+    widths = [11, 13, 15, 17] + [19] * 11 + [17, 15, 13, 11]
+    k = np.zeros((19, 19), np.uint8)
+    for i, w in enumerate(widths):
+        k[i, 9 - w // 2:9 + w // 2 + 1] = 1
+    return k
+
+
+def ellipse3() -> "np.ndarray":
+    """getStructuringElement(MORPH_ELLIPSE, Size(3, 3)) (HistologicalEntities.cpp:309): the cross."""
+    import numpy as np
+
+    return np.array([[0, 1, 0], [1, 1, 1], [0, 1, 0]], np.uint8)
+
+
+def morphOpen(image: torch.Tensor, kernel) -> torch.Tensor:
+    """nscale::morphOpen<unsigned char> (MorphologicOperations.cpp:2459-2493): erosion with the
+    image surrounded by 255, then dilation surrounded by 0, by the flat element `kernel` (a k x k
+    host array, k odd in [3, 63], non-zero = in the element)."""
+    import numpy as np
+
+    _check_image(image, "image")
+    if image.dtype != torch.uint8:
+        raise NsgbError(2, "morphOpen: image must be uint8 (the reference's one instantiation)")
+    k = np.ascontiguousarray(np.asarray(kernel).astype(np.uint8))
+    if k.ndim != 2 or k.shape[0] != k.shape[1]:
+        raise NsgbError(1, "morphOpen: kernel must be square")
+    img = _contig(image)
+    rows, cols = img.shape
+    out = torch.empty((rows, cols), dtype=torch.uint8, device=img.device)
+    ws, nb = _ws(_ffi.OP_MORPH_OPEN, _ffi.U8, rows, cols, img.device)
+    st = lib.nsgb_morph_open(img.data_ptr(), out.data_ptr(), rows, cols, _pitch(img), _pitch(out),
+                             k.ctypes.data_as(C.c_void_p), int(k.shape[0]), ws, nb, _stream(), None)
+    _ffi.check(st, "morphOpen")
+    return out
+
+
 def nucleus_candidates(rc: torch.Tensor, rc_open: torch.Tensor, rbc: torch.Tensor, g1: float = 80, g2: float = 45,
                        area_min: int = 11, area_max: int = 1000) -> Tuple[torch.Tensor, int]:
     """The nucleus-candidate stage after the opening (HistologicalEntities.cpp:195-275) on the

@@ -423,6 +423,26 @@ GpuMat imhmin(const GpuMat& image, T h, int connectivity, Stream& stream) {
   return out;
 }
 
+// nscale::gpu::morphOpen<T> (MorphologicOperations.h:182, MorphologicOperationsGPU.cpp:1308),
+// with the CPU version's borders (255 around the erosion, 0 around the dilation).  `kernel`: a
+// host CV_8UC1 k x k element, k odd; the reference instantiates unsigned char only.
+template <typename T>
+GpuMat morphOpen(const GpuMat& image, const cv::Mat& kernel, Stream& stream) {
+  static_assert(sizeof(T) == 1, "morphOpen: the reference instantiates unsigned char only");
+  NSGB_CV_ASSERT(image.channels() == 1 && image.type() == CV_8UC1);
+  NSGB_CV_ASSERT(kernel.rows == kernel.cols && kernel.rows > 1 && kernel.rows % 2 == 1 && kernel.type() == CV_8UC1);
+  std::vector<unsigned char> k((size_t)kernel.rows * kernel.cols);
+  for (int i = 0; i < kernel.rows; ++i)
+    std::memcpy(&k[(size_t)i * kernel.cols], kernel.ptr<unsigned char>(i), (size_t)kernel.cols);
+  GpuMat out(image.rows, image.cols, image.type());
+  const size_t nb = nsgb_workspace_size(NSGB_OP_MORPH_OPEN, NSGB_U8, image.rows, image.cols);
+  detail::check(nsgb_morph_open(image.data, out.data, image.rows, image.cols, (int64_t)image.step,
+                                (int64_t)out.step, k.data(), kernel.rows, detail::workspace(nb), nb,
+                                detail::raw(stream), nullptr),
+                "morphOpen");
+  return out;
+}
+
 }  // namespace gpu
 
 // ---- nscale:: (host cv::Mat signatures, MorphologicOperations.h:21-94), run on the GPU ----
@@ -479,6 +499,14 @@ template <typename T>
 cv::Mat imhmin(const cv::Mat& image, T h, int connectivity) {
   return detail::via_gpu(image, [&](cv::gpu::GpuMat& g) {
     return gpu::imhmin<T>(g, h, connectivity, cv::gpu::Stream::Null());
+  });
+}
+
+// nscale::morphOpen<T> (MorphologicOperations.h:89).
+template <typename T>
+cv::Mat morphOpen(const cv::Mat& image, const cv::Mat& kernel) {
+  return detail::via_gpu(image, [&](cv::gpu::GpuMat& g) {
+    return gpu::morphOpen<T>(g, kernel, cv::gpu::Stream::Null());
   });
 }
 

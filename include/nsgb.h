@@ -50,7 +50,8 @@ typedef enum {
   NSGB_OP_BWAREAOPEN = 6,
   NSGB_OP_CHAIN = 7,
   NSGB_OP_BOUNDING_BOX = 8,
-  NSGB_OP_NUCLEUS_CANDIDATES = 9
+  NSGB_OP_NUCLEUS_CANDIDATES = 9,
+  NSGB_OP_MORPH_OPEN = 10
 } nsgb_op;
 
 typedef struct {
@@ -190,6 +191,19 @@ nsgb_status nsgb_chain(int dtype, void* marker, const void* mask, int64_t rows, 
                        int32_t area_min, int32_t area_max, uint8_t* fill_out, int32_t* labels_out,
                        uint8_t* area_out, int32_t* n_labels, int32_t* n_kept, void* ws,
                        size_t ws_bytes, nsgb_stream_t stream, const nsgb_opts* opts);
+
+/* Opening of a u8 image by a flat k x k structuring element: nscale::morphOpen<unsigned char>
+ * (src/segment/MorphologicOperations.cpp:2459-2493; GPU twin MorphologicOperationsGPU.cpp:1308).
+ * Erosion with the image surrounded by 255, then dilation of the result surrounded by 0, each
+ * in OpenCV's convention: at (y, x) the min / max of src(y + i - c, x + j - c) over the
+ * element's non-zero (i, j), c = (k - 1) / 2.  `kernel`: HOST array of k x k bytes, row-major,
+ * non-zero = in the element; k odd, 3 <= k <= 63, at least one non-zero entry (else
+ * NSGB_ERR_BAD_ARG).  The reference applies it with its 19 x 19 disk
+ * (HistologicalEntities.cpp:162-185) and a 3 x 3 disk (:481).  out must not overlap in.
+ * Workspace: nsgb_workspace_size(NSGB_OP_MORPH_OPEN, NSGB_U8, rows, cols) (the eroded image). */
+nsgb_status nsgb_morph_open(const uint8_t* in, uint8_t* out, int64_t rows, int64_t cols, int64_t pitch_in,
+                            int64_t pitch_out, const uint8_t* kernel, int k, void* ws, size_t ws_bytes,
+                            nsgb_stream_t stream, const nsgb_opts* opts);
 
 /* The nucleus-candidate stage after the opening, kept on the device: the tail of
  * HistologicalEntities::plFindNucleusCandidates (src/segment/HistologicalEntities.cpp:195-275;

@@ -36,6 +36,7 @@ def _load() -> C.CDLL:
     lib.orc_imhmin.argtypes = [C.c_int, vp, i64, i64, C.c_double, C.c_int, vp]
     lib.orc_bwselect.argtypes = [C.c_int, vp, vp, i64, i64, C.c_int, vp]
     lib.orc_threshold_gt.argtypes = [C.c_int, vp, i64, C.c_double, vp]
+    lib.orc_morph_open_u8.argtypes = [vp, i64, i64, vp, C.c_int, vp]
     lib.orc_bwlabel2.argtypes = [vp, i64, i64, C.c_int, C.c_int, vp]
     lib.orc_bwlabel2.restype = i32
     lib.orc_bwareaopen2.argtypes = [vp, C.c_int, C.c_int, i32, i32, C.c_int, i64, i64, vp, vp]
@@ -101,6 +102,16 @@ def bwselect(image: np.ndarray, seeds: np.ndarray, conn: int) -> np.ndarray:
     out = np.empty_like(image)
     assert lib.orc_bwselect(DT[image.dtype], _p(image), _p(seeds), image.shape[0], image.shape[1], conn,
                             _p(out)) == 0
+    return out
+
+
+def morph_open(image: np.ndarray, kernel: np.ndarray) -> np.ndarray:
+    """morphOpen<unsigned char> (MorphologicOperations.cpp:2459-2493), u8 image, k x k element."""
+    image = _c(image).astype(np.uint8, copy=False)
+    kernel = _c((np.asarray(kernel) != 0).astype(np.uint8))
+    out = np.empty_like(image)
+    assert lib.orc_morph_open_u8(_p(image), image.shape[0], image.shape[1], _p(kernel), kernel.shape[0],
+                                 _p(out)) == 0
     return out
 
 

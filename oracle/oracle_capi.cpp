@@ -93,6 +93,12 @@ int orc_threshold_gt(int dtype, const void* in, int64_t n, double k, uint8_t* ou
   });
 }
 
+int orc_morph_open_u8(const uint8_t* in, int64_t H, int64_t W, const uint8_t* kern, int k, uint8_t* out) {
+  if (k < 1 || k % 2 == 0) return -1;
+  orc::morph_open_u8(in, H, W, kern, k, out);
+  return 0;
+}
+
 int32_t orc_bwlabel2(const uint8_t* bin, int64_t H, int64_t W, int conn, int relab, int32_t* out) {
   return orc::bwlabel2(bin, H, W, conn, relab != 0, out);
 }

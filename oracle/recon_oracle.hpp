@@ -551,4 +551,35 @@ inline void recon_grad_fixed(const float* g, const int32_t* prov, int64_t n, flo
   }
 }
 
+// Flat erosion (MAX = false) / dilation (MAX = true) of a u8 image by a k x k element, as
+// cv::erode / cv::dilate compute them on the bordered image that morphOpen builds: at (y, x)
+// the min / max over the element's non-zero (i, j) of src(y + i - c, x + j - c), c = (k-1)/2,
+// pixels outside the image reading `pad`.
+inline void morph_u8(const uint8_t* src, int64_t H, int64_t W, const uint8_t* kern, int k, bool max_op,
+                     uint8_t pad, uint8_t* dst) {
+  const int c = (k - 1) / 2;
+  for (int64_t y = 0; y < H; ++y)
+    for (int64_t x = 0; x < W; ++x) {
+      int v = max_op ? 0 : 255;
+      for (int i = 0; i < k; ++i)
+        for (int j = 0; j < k; ++j) {
+          if (!kern[i * k + j]) continue;
+          const int64_t yy = y + i - c, xx = x + j - c;
+          const int p = (yy < 0 || yy >= H || xx < 0 || xx >= W) ? pad : src[yy * W + xx];
+          v = max_op ? (p > v ? p : v) : (p < v ? p : v);
+        }
+      dst[y * W + x] = (uint8_t)v;
+    }
+}
+
+// src/segment/MorphologicOperations.cpp:2459-2493 (morphOpen<unsigned char>): copyMakeBorder by
+// c with 255, erode, crop; copyMakeBorder by c with 0, dilate, crop.  The crops keep only pixels
+// whose element reach stays inside the bordered image, so OpenCV's own border mode never
+// enters.
+inline void morph_open_u8(const uint8_t* src, int64_t H, int64_t W, const uint8_t* kern, int k, uint8_t* dst) {
+  std::vector<uint8_t> eroded((size_t)(H * W));
+  morph_u8(src, H, W, kern, k, false, 255, eroded.data());
+  morph_u8(eroded.data(), H, W, kern, k, true, 0, dst);
+}
+
 }  // namespace orc

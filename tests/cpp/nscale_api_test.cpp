@@ -40,6 +40,10 @@ int main(int argc, char** argv) {
   save(dir, "area.u8", kept);
   cv::Mat hmin = nscale::imhmin<unsigned char>(mask, (unsigned char)10, 8);
   save(dir, "hmin8.u8", hmin);
+  cv::Mat cross(3, 3, CV_8UC1);  // getStructuringElement(MORPH_ELLIPSE, Size(3, 3))
+  for (int i = 0; i < 9; ++i) cross.data[i] = (i % 2) ? 1 : (i == 4 ? 1 : 0);
+  cv::Mat opened = nscale::morphOpen<unsigned char>(mask, cross);
+  save(dir, "open3.u8", opened);
 
   // device signatures (MorphologicOperations.h:96-190)
   cv::gpu::Stream stream;

@@ -40,10 +40,12 @@ def test_status_strings_and_workspace_sizes():
     lib = ffi.lib
     assert lib.nsgb_status_string(0) == b"ok"
     assert b"workspace" in lib.nsgb_status_string(3)
-    for op in range(10):
+    for op in range(11):
         for dt in range(4):
             assert lib.nsgb_workspace_size(op, dt, 64, 64) > 0
-    assert lib.nsgb_workspace_size(10, 0, 64, 64) == 0
+    assert lib.nsgb_workspace_size(11, 0, 64, 64) == 0
+    # opening: the status word and the eroded image with rows padded to 128 bytes
+    assert lib.nsgb_workspace_size(ffi.OP_MORPH_OPEN, ffi.U8, 100, 130) >= 256 + 100 * 256
     assert lib.nsgb_workspace_size(-1, 0, 64, 64) == 0
     # nucleus candidates: the chain's u8 workspace whatever dtype is asked for
     for dt in range(4):
@@ -72,6 +74,17 @@ def test_argument_errors_need_no_gpu():
     assert lib.nsgb_bounding_boxes(None, 4, 4, 16, 0, 1, 4, None, None, 1, 1 << 20, None, None) == 1
     assert lib.nsgb_bounding_boxes(1, 4, 4, 8, 0, 1, 4, None, None, 1, 1 << 20, None, None) == 1
     assert lib.nsgb_bounding_boxes(1, 4, 4, 16, 0, None, 4, None, None, 1, 1 << 20, None, None) == 1
+    # opening: even / too large / empty element, overlapping output, missing workspace
+    k3 = (ctypes.c_uint8 * 9)(0, 1, 0, 1, 1, 1, 0, 1, 0)
+    k0 = (ctypes.c_uint8 * 9)()
+    k4 = (ctypes.c_uint8 * 16)(*([1] * 16))
+    ka = ctypes.addressof
+    assert lib.nsgb_morph_open(1, 4096, 4, 4, 4, 4, ka(k4), 4, 1, 1 << 20, None, None) == 1
+    assert lib.nsgb_morph_open(1, 4096, 4, 4, 4, 4, ka(k0), 3, 1, 1 << 20, None, None) == 1
+    assert lib.nsgb_morph_open(1, 4096, 4, 4, 4, 4, ka(k3), 65, 1, 1 << 20, None, None) == 1
+    assert lib.nsgb_morph_open(1, 4096, 4, 4, 4, 4, None, 3, 1, 1 << 20, None, None) == 1
+    assert lib.nsgb_morph_open(4096, 4100, 4, 4, 4, 4, ka(k3), 3, 1, 1 << 20, None, None) == 1
+    assert lib.nsgb_morph_open(4096, 8192, 4, 4, 4, 4, ka(k3), 3, None, 0, None, None) == 3
     # nucleus candidates: null image, pitch below the row, missing workspace
     assert lib.nsgb_nucleus_candidates(None, 1, 1, 1, 4, 4, 4, 80.0, 45.0, 11, 1000, None, None, 1, 1 << 20,
                                        None, None) == 1

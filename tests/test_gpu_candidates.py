@@ -87,3 +87,18 @@ def test_candidates_c_abi_pitched_async(nsgb, oracle):
     assert np.array_equal(t_open[:, :W].cpu().numpy(), exp)
     # the padding between rows is left alone
     assert not t_open[:, W:].any()
+
+
+def test_candidates_after_device_opening(nsgb, oracle):
+    """S1 from rc: the device opening with the 19 x 19 disk as the marker, as the reference
+    builds it (HistologicalEntities.cpp:184-199), then the candidate stage."""
+    from nsgb import disk19
+
+    rc, _, rbc = ci.tile(1024, 1280, 450, 8)
+    rc_open = nsgb.morphOpen(to_dev(rc), disk19())
+    exp_open = oracle.morph_open(rc, disk19())
+    assert np.array_equal(rc_open.cpu().numpy(), exp_open)
+    seg, n = nsgb.nucleus_candidates(to_dev(rc), rc_open, to_dev(rbc))
+    exp, n_exp = oracle.nucleus_candidates(rc, exp_open, rbc)
+    assert n == n_exp and n > 0
+    assert np.array_equal(seg.cpu().numpy(), exp)

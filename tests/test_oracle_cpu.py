@@ -319,3 +319,49 @@ def test_nucleus_candidates_thresholds(oracle):
     # nothing above g1 = 255: no component survives, nothing is selected
     seg, n = oracle.nucleus_candidates(rc, rc_open, rbc, 255, 45)
     assert n == 0 and not seg.any()
+
+
+def np_morph_open(img, kern):
+    """OpenCV's erode / dilate convention written out in numpy: min / max of
+    src(y + i - c, x + j - c) over the element, outside the image 255 for the erosion and 0 for
+    the dilation (morphOpen's borders, MorphologicOperations.cpp:2472-2481)."""
+    k = kern.shape[0]
+    c = (k - 1) // 2
+    H, W = img.shape
+
+    def pass_(src, pad, op):
+        P = np.full((H + 2 * c, W + 2 * c), pad, np.uint8)
+        P[c:c + H, c:c + W] = src
+        acc = np.full((H, W), pad, np.uint8)  # the identity of the fold
+        for i in range(k):
+            for j in range(k):
+                if kern[i, j]:
+                    acc = op(acc, P[i:i + H, j:j + W])
+        return acc
+
+    return pass_(pass_(img, 255, np.minimum), 0, np.maximum)
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (1, 40), (40, 1), (23, 37), (70, 90)])
+def test_morph_open(oracle, shape):
+    from nsgb import disk19, ellipse3
+
+    rng = np.random.default_rng(shape[0] * 100 + shape[1])
+    img = rng.integers(0, 256, shape).astype(np.uint8)
+    asym = (rng.random((5, 5)) < 0.4).astype(np.uint8)
+    asym[0, 4] = 1
+    for kern in (disk19(), ellipse3(), np.ones((3, 3), np.uint8), asym):
+        got = oracle.morph_open(img, kern)
+        assert np.array_equal(got, np_morph_open(img, kern))
+        if np.array_equal(kern, kern[::-1, ::-1]):  # symmetric: scipy's footprint convention agrees
+            e = ndi.grey_erosion(img, footprint=kern != 0, mode="constant", cval=255)
+            assert np.array_equal(got, ndi.grey_dilation(e, footprint=kern != 0, mode="constant", cval=0))
+
+
+def test_disk19_matches_reference_shape():
+    from nsgb import disk19
+
+    d = disk19()
+    assert d.shape == (19, 19) and int(d.sum()) == 321
+    assert np.array_equal(d, d[::-1]) and np.array_equal(d, d[:, ::-1]) and np.array_equal(d, d.T)
+    assert [int(r.sum()) for r in d[:5]] == [11, 13, 15, 17, 19]
