@@ -63,8 +63,9 @@ def parse_args():
     p.add_argument("--no-large", action="store_true")
     p.add_argument("--no-bbox", action="store_true")
     p.add_argument("--no-candidates", action="store_true")
+    p.add_argument("--no-distance", action="store_true")
     p.add_argument("--candidates-only", action="store_true",
-                   help="profiling aid: only the nucleus-candidate section")
+                   help="profiling aid: only the segmentation-stage sections (opening + candidates, distance)")
     p.add_argument("--large-size", type=int, default=16384)
     return p.parse_args()
 
@@ -217,7 +218,8 @@ def run_nsgb(args):
         print(json.dumps({"batched": batched_section(args, torch.device("cuda", local))}))
         return 0
     if args.candidates_only:
-        print(json.dumps({"candidates": candidates_section(args, torch.device("cuda", local))}))
+        dev = torch.device("cuda", local)
+        print(json.dumps({"candidates": candidates_section(args, dev), "distance": distance_section(args, dev)}))
         return 0
     dist = None
     if world > 1:
@@ -435,6 +437,8 @@ def run_nsgb(args):
         line["bbox"] = bbox_section(args, dev)
     if not args.no_candidates:
         line["candidates"] = candidates_section(args, dev)
+    if not args.no_distance:
+        line["distance"] = distance_section(args, dev)
     if rank == 0:
         print(json.dumps(line))
     if dist:
@@ -857,6 +861,54 @@ def candidates_section(args, dev, steps=20):
                                "sample": f"oracle opening of a {strip}x{W} strip ({t_o:.2f} s, scaled to {H} rows) "
                                          f"plus the candidate stage on the full tile ({t_c:.2f} s), one host core",
                                "same_kept_count": n_exp == res["kept_components"]}
+    return res
+
+
+def distance_section(args, dev, steps=20):
+    """The distance map and watershed basins of S2 (HistologicalEntities.cpp:341-356) for the dark
+    objects of the headline tile (mask < 128): exact Euclidean distance to the nearest zero pixel,
+    -distance on the objects, -FLT_MAX elsewhere.  L2 flushed before every step."""
+    import numpy as np
+    import torch
+
+    from nsgb import _ffi, synth
+
+    lib = _ffi.lib
+    H = W = args.size
+    mask_h, _ = synth.tile_u8(H, W, args.ellipses, 0)
+    m_h = np.where(mask_h < 128, 255, 0).astype(np.uint8)
+    m = torch.from_numpy(m_h).to(dev)
+    out = torch.empty((H, W), dtype=torch.float32, device=dev)
+    nb = lib.nsgb_workspace_size(_ffi.OP_DISTANCE, _ffi.U8, H, W)
+    ws_t = torch.empty(nb + 256, dtype=torch.uint8, device=dev)
+    ws = (ws_t.data_ptr() + 255) & ~255
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    opts = _ffi.Opts(0, 0, 0)
+
+    def call():
+        _ffi.check(lib.nsgb_distance_transform(m.data_ptr(), out.data_ptr(), H, W, W, W * 4, 1, ws, nb, sp,
+                                               C.byref(opts)), "distance_transform")
+
+    t, t_med = timed_steps(stream, steps, lambda: flush.fill_(1), call)
+    st = lib.nsgb_device_status(C.c_void_p(ws), sp)
+    if st != 0:
+        raise RuntimeError(f"distance: device status {_ffi.STATUS.get(st, st)}")
+    px = H * W
+    res = {"workload": f"{H}x{W} u8 mask (dark objects of the headline tile, mask < 128), basins output",
+           "object_px": int(m_h.astype(bool).sum()), "ms": t, "ms_median": t_med, "mpix_s": px / 1e3 / t,
+           "gpu_launches_per_call": 3, "l2": "flushed before every step (512 MB write)"}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        t0 = time.perf_counter()
+        oracle.distance_queue(m_h)
+        t_q = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": px / 1e6 / t_q, "unit": "MPix/s", "cores": 1, "kind": "port",
+                               "sample": f"the reference's queue-based distanceTransform restated, full tile, "
+                                         f"{t_q:.2f} s, one host core"}
     return res
 
 

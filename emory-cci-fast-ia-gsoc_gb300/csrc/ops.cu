@@ -18,6 +18,7 @@
 #include "bbox.cuh"
 #include "ccl.cuh"
 #include "common.cuh"
+#include "edt.cuh"
 #include "morph.cuh"
 #include "recon.cuh"
 
@@ -688,14 +689,15 @@ nsgb_status check_ws(void* ws, size_t ws_bytes, int op, int dtype, int64_t rows,
 extern "C" {
 
 size_t nsgb_workspace_size(int op, int dtype, int64_t rows, int64_t cols) {
-  if (rows <= 0 || cols <= 0 || op < 0 || op > NSGB_OP_MORPH_OPEN) return 0;
+  if (rows <= 0 || cols <= 0 || op < 0 || op > NSGB_OP_DISTANCE) return 0;
   if (op == NSGB_OP_BWLABEL || op == NSGB_OP_BWAREAOPEN || op == NSGB_OP_NUCLEUS_CANDIDATES ||
-      op == NSGB_OP_MORPH_OPEN)
+      op == NSGB_OP_MORPH_OPEN || op == NSGB_OP_DISTANCE)
     dtype = NSGB_U8;
   if (dtype < 0 || dtype > 3) return 0;
   if (op == NSGB_OP_IMRECONSTRUCT || op == NSGB_OP_HMIN) return align256(recon_workspace_bytes(dtype, rows, cols));
   if (op == NSGB_OP_BOUNDING_BOX) return align256(bbox_workspace_bytes(rows * cols));
   if (op == NSGB_OP_MORPH_OPEN) return align256(morph_open_workspace_bytes(rows, cols));
+  if (op == NSGB_OP_DISTANCE) return align256(edt_workspace_bytes(rows, cols));
   const Plan P = single_plan(dtype, nullptr, nullptr, rows, cols, cols * elem_size(dtype));
   return ws_sizes(P.t).total;
 }
@@ -985,6 +987,20 @@ nsgb_status nsgb_morph_open(const uint8_t* in, uint8_t* out, int64_t rows, int64
   if (e2 == cudaSuccess)
     e2 = morph_open_launch(in, pitch_in, out, pitch_out, (int)rows, (int)cols, e, (uint8_t*)ws + 256, s);
   return finish(e2, ws, s, opts);
+}
+
+nsgb_status nsgb_distance_transform(const uint8_t* mask, float* out, int64_t rows, int64_t cols, int64_t pitch_in,
+                                    int64_t pitch_out, int basins, void* ws, size_t ws_bytes, nsgb_stream_t stream,
+                                    const nsgb_opts* opts) {
+  if (!mask || !out || !valid_dims(rows, cols) || !valid_pitch(pitch_in, cols, 1) || !valid_pitch(pitch_out, cols, 4) ||
+      rows > 65535LL * 128)
+    return NSGB_ERR_BAD_ARG;
+  nsgb_status st = check_ws(ws, ws_bytes, NSGB_OP_DISTANCE, NSGB_U8, rows, cols);
+  if (st != NSGB_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(ws, 0, sizeof(int), s);
+  if (e == cudaSuccess) e = edt_launch(mask, pitch_in, out, pitch_out, (int)rows, (int)cols, basins != 0, ws, s);
+  return finish(e, ws, s, opts);
 }
 
 nsgb_status nsgb_nucleus_candidates(uint8_t* rc_open, const uint8_t* rc, const uint8_t* rbc, uint8_t* seg_out,

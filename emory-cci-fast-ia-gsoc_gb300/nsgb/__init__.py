@@ -347,6 +347,24 @@ def morphOpen(image: torch.Tensor, kernel) -> torch.Tensor:
     return out
 
 
+def distanceTransform(mask: torch.Tensor, basins: bool = False) -> torch.Tensor:
+    """Distance from every pixel of a uint8 mask to its nearest zero pixel, float32, exact (the
+    map of HistologicalEntities.cpp:341; nscale::gpu::distanceTransform's role).  basins=True
+    gives the watershed basins of HistologicalEntities.cpp:347-356 instead: -distance on
+    non-zero pixels, -FLT_MAX on zero pixels."""
+    _check_image(mask, "mask")
+    if mask.dtype != torch.uint8:
+        raise NsgbError(2, "distanceTransform: mask must be uint8")
+    m = _contig(mask)
+    rows, cols = m.shape
+    out = torch.empty((rows, cols), dtype=torch.float32, device=m.device)
+    ws, nb = _ws(_ffi.OP_DISTANCE, _ffi.U8, rows, cols, m.device)
+    st = lib.nsgb_distance_transform(m.data_ptr(), out.data_ptr(), rows, cols, _pitch(m), _pitch(out),
+                                     1 if basins else 0, ws, nb, _stream(), None)
+    _ffi.check(st, "distanceTransform")
+    return out
+
+
 def nucleus_candidates(rc: torch.Tensor, rc_open: torch.Tensor, rbc: torch.Tensor, g1: float = 80, g2: float = 45,
                        area_min: int = 11, area_max: int = 1000) -> Tuple[torch.Tensor, int]:
     """The nucleus-candidate stage after the opening (HistologicalEntities.cpp:195-275) on the

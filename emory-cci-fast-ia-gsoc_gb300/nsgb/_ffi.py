@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libnsgb.so")
 U8, U16, I32, F32 = 0, 1, 2, 3
 OP_IMRECONSTRUCT, OP_IMRECONSTRUCT_BINARY, OP_FILL_HOLES, OP_HMIN = 0, 1, 2, 3
 OP_BWSELECT, OP_BWLABEL, OP_BWAREAOPEN, OP_CHAIN = 4, 5, 6, 7
-OP_BOUNDING_BOX, OP_NUCLEUS_CANDIDATES, OP_MORPH_OPEN = 8, 9, 10
+OP_BOUNDING_BOX, OP_NUCLEUS_CANDIDATES, OP_MORPH_OPEN, OP_DISTANCE = 8, 9, 10, 11
 NOALLOC_SCRATCH_BYTES = 1 << 20  # NSGB_NOALLOC_SCRATCH_BYTES
 
 STATUS = {
@@ -76,6 +76,7 @@ _SIGS = {
     "nsgb_bwareaopen": (_int, [_vp, _int, _vp, _vp, _i64, _i64, _i64, _i64, _i64, C.c_int32, C.c_int32, _int,
                                _i32p, _vp, _sz, _vp, _optp]),
     "nsgb_bounding_boxes": (_int, [_vp, _i64, _i64, _i64, C.c_int32, _vp, _i64, _i32p, _vp, _vp, _sz, _vp, _optp]),
+    "nsgb_distance_transform": (_int, [_vp, _vp, _i64, _i64, _i64, _i64, _int, _vp, _sz, _vp, _optp]),
     "nsgb_morph_open": (_int, [_vp, _vp, _i64, _i64, _i64, _i64, _vp, _int, _vp, _sz, _vp, _optp]),
     "nsgb_nucleus_candidates": (_int, [_vp, _vp, _vp, _vp, _i64, _i64, _i64, _dbl, _dbl, C.c_int32, C.c_int32, _i32p,
                                        _vp, _vp, _sz, _vp, _optp]),

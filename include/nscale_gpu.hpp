@@ -443,6 +443,22 @@ GpuMat morphOpen(const GpuMat& image, const cv::Mat& kernel, Stream& stream) {
   return out;
 }
 
+// nscale::gpu::distanceTransform (MorphologicOperations.h:188): CV_32FC1 distance to the nearest
+// zero pixel of a CV_8UC1 mask, exact (the reference's queue propagation can overshoot; see
+// nsgb.h).  Only the distance map (calcDist = true) is provided; the tiling arguments are
+// accepted and ignored.
+inline GpuMat distanceTransform(const GpuMat& mask, Stream& stream, bool calcDist = true, int /*tIdX*/ = 0,
+                                int /*tIdY*/ = 0, int /*tileSize*/ = 0, int /*imgCols*/ = 0) {
+  NSGB_CV_ASSERT(mask.channels() == 1 && mask.type() == CV_8UC1);
+  NSGB_CV_ASSERT(calcDist);
+  GpuMat out(mask.rows, mask.cols, CV_32FC1);
+  const size_t nb = nsgb_workspace_size(NSGB_OP_DISTANCE, NSGB_U8, mask.rows, mask.cols);
+  detail::check(nsgb_distance_transform(mask.data, (float*)out.data, mask.rows, mask.cols, (int64_t)mask.step,
+                                        (int64_t)out.step, 0, detail::workspace(nb), nb, detail::raw(stream), nullptr),
+                "distanceTransform");
+  return out;
+}
+
 }  // namespace gpu
 
 // ---- nscale:: (host cv::Mat signatures, MorphologicOperations.h:21-94), run on the GPU ----
@@ -499,6 +515,13 @@ template <typename T>
 cv::Mat imhmin(const cv::Mat& image, T h, int connectivity) {
   return detail::via_gpu(image, [&](cv::gpu::GpuMat& g) {
     return gpu::imhmin<T>(g, h, connectivity, cv::gpu::Stream::Null());
+  });
+}
+
+// nscale::distanceTransform (MorphologicOperations.h:92), distance map only.
+inline cv::Mat distanceTransform(const cv::Mat& mask, bool calcDist = true) {
+  return detail::via_gpu(mask, [&](cv::gpu::GpuMat& g) {
+    return gpu::distanceTransform(g, cv::gpu::Stream::Null(), calcDist);
   });
 }
 

@@ -51,7 +51,8 @@ typedef enum {
   NSGB_OP_CHAIN = 7,
   NSGB_OP_BOUNDING_BOX = 8,
   NSGB_OP_NUCLEUS_CANDIDATES = 9,
-  NSGB_OP_MORPH_OPEN = 10
+  NSGB_OP_MORPH_OPEN = 10,
+  NSGB_OP_DISTANCE = 11
 } nsgb_op;
 
 typedef struct {
@@ -204,6 +205,21 @@ nsgb_status nsgb_chain(int dtype, void* marker, const void* mask, int64_t rows, 
 nsgb_status nsgb_morph_open(const uint8_t* in, uint8_t* out, int64_t rows, int64_t cols, int64_t pitch_in,
                             int64_t pitch_out, const uint8_t* kernel, int k, void* ws, size_t ws_bytes,
                             nsgb_stream_t stream, const nsgb_opts* opts);
+
+/* Euclidean distance transform of a u8 mask: out(y, x) = distance from (y, x) to the nearest
+ * zero pixel (0 on zero pixels), as float: the correctly rounded square root of the exact
+ * integer squared distance.  This is the map the segmentation takes before its watershed
+ * (HistologicalEntities.cpp:341, OpenCV's CV_DIST_L2 with CV_DIST_MASK_PRECISE); the reference's
+ * own nscale::distanceTransform (MorphologicOperations.cpp:197-275; GPU
+ * nscale::gpu::distanceTransform, MorphologicOperationsGPU.cpp:112) propagates nearest zero
+ * pixels between 8-neighbours and can return a larger distance where that propagation misses
+ * the nearest one.  basins != 0 writes the watershed basins of HistologicalEntities.cpp:347-356
+ * instead: -distance on non-zero pixels, -FLT_MAX on zero pixels.  A mask without any zero
+ * pixel gives +inf distances.  out: float, pitch_out in bytes.  rows <= 65535 * 128.
+ * Workspace: nsgb_workspace_size(NSGB_OP_DISTANCE, NSGB_U8, rows, cols). */
+nsgb_status nsgb_distance_transform(const uint8_t* mask, float* out, int64_t rows, int64_t cols, int64_t pitch_in,
+                                    int64_t pitch_out, int basins, void* ws, size_t ws_bytes, nsgb_stream_t stream,
+                                    const nsgb_opts* opts);
 
 /* The nucleus-candidate stage after the opening, kept on the device: the tail of
  * HistologicalEntities::plFindNucleusCandidates (src/segment/HistologicalEntities.cpp:195-275;

@@ -37,6 +37,8 @@ def _load() -> C.CDLL:
     lib.orc_bwselect.argtypes = [C.c_int, vp, vp, i64, i64, C.c_int, vp]
     lib.orc_threshold_gt.argtypes = [C.c_int, vp, i64, C.c_double, vp]
     lib.orc_morph_open_u8.argtypes = [vp, i64, i64, vp, C.c_int, vp]
+    lib.orc_edt_exact_u8.argtypes = [vp, i64, i64, C.c_int, vp]
+    lib.orc_dist_queue_u8.argtypes = [vp, i64, i64, vp]
     lib.orc_bwlabel2.argtypes = [vp, i64, i64, C.c_int, C.c_int, vp]
     lib.orc_bwlabel2.restype = i32
     lib.orc_bwareaopen2.argtypes = [vp, C.c_int, C.c_int, i32, i32, C.c_int, i64, i64, vp, vp]
@@ -112,6 +114,23 @@ def morph_open(image: np.ndarray, kernel: np.ndarray) -> np.ndarray:
     out = np.empty_like(image)
     assert lib.orc_morph_open_u8(_p(image), image.shape[0], image.shape[1], _p(kernel), kernel.shape[0],
                                  _p(out)) == 0
+    return out
+
+
+def distance_transform(mask: np.ndarray, basins: bool = False) -> np.ndarray:
+    """Exact distance to the nearest zero pixel, float32 (HistologicalEntities.cpp:341's map);
+    basins: -distance on non-zero pixels, -FLT_MAX on zero pixels (347-356)."""
+    mask = _c(mask).astype(np.uint8, copy=False)
+    out = np.empty(mask.shape, np.float32)
+    assert lib.orc_edt_exact_u8(_p(mask), mask.shape[0], mask.shape[1], int(basins), _p(out)) == 0
+    return out
+
+
+def distance_queue(mask: np.ndarray) -> np.ndarray:
+    """The reference's queue-based nscale::distanceTransform (MorphologicOperations.cpp:197-275)."""
+    mask = _c(mask).astype(np.uint8, copy=False)
+    out = np.empty(mask.shape, np.float32)
+    assert lib.orc_dist_queue_u8(_p(mask), mask.shape[0], mask.shape[1], _p(out)) == 0
     return out
 
 

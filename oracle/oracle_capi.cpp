@@ -99,6 +99,16 @@ int orc_morph_open_u8(const uint8_t* in, int64_t H, int64_t W, const uint8_t* ke
   return 0;
 }
 
+int orc_edt_exact_u8(const uint8_t* m, int64_t H, int64_t W, int basins, float* out) {
+  orc::edt_exact_u8(m, H, W, basins != 0, out);
+  return 0;
+}
+
+int orc_dist_queue_u8(const uint8_t* m, int64_t H, int64_t W, float* out) {
+  orc::dist_queue_u8(m, H, W, out);
+  return 0;
+}
+
 int32_t orc_bwlabel2(const uint8_t* bin, int64_t H, int64_t W, int conn, int relab, int32_t* out) {
   return orc::bwlabel2(bin, H, W, conn, relab != 0, out);
 }

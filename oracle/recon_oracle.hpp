@@ -582,4 +582,87 @@ inline void morph_open_u8(const uint8_t* src, int64_t H, int64_t W, const uint8_
   morph_u8(eroded.data(), H, W, kern, k, true, 0, dst);
 }
 
+// Exact Euclidean distance to the nearest zero pixel of a u8 mask: the definition behind
+// OpenCV's distanceTransform(CV_DIST_L2, CV_DIST_MASK_PRECISE) at HistologicalEntities.cpp:341,
+// as float = the correctly rounded square root of the integer squared distance.  Column
+// distances first, then per pixel an outward search along the row that stops once the column
+// offset alone exceeds the best distance found.  No zero pixel: +inf.  basins: -distance on
+// non-zero pixels, -FLT_MAX on zero ones (HistologicalEntities.cpp:347-356).
+inline void edt_exact_u8(const uint8_t* m, int64_t H, int64_t W, bool basins, float* out) {
+  const int64_t inf = H + W;
+  std::vector<int64_t> g((size_t)(H * W));
+  for (int64_t x = 0; x < W; ++x) {
+    int64_t d = inf;
+    for (int64_t y = 0; y < H; ++y) {
+      d = m[y * W + x] == 0 ? 0 : std::min(d + 1, inf);
+      g[y * W + x] = d;
+    }
+    d = inf;
+    for (int64_t y = H - 1; y >= 0; --y) {
+      d = m[y * W + x] == 0 ? 0 : std::min(d + 1, inf);
+      g[y * W + x] = std::min(g[y * W + x], d);
+    }
+  }
+  for (int64_t y = 0; y < H; ++y)
+    for (int64_t x = 0; x < W; ++x) {
+      const int64_t* gr = &g[y * W];
+      int64_t best = gr[x] * gr[x];
+      for (int64_t k = 1; k < W && k * k < best; ++k) {
+        if (x - k >= 0) best = std::min(best, k * k + gr[x - k] * gr[x - k]);
+        if (x + k < W) best = std::min(best, k * k + gr[x + k] * gr[x + k]);
+      }
+      const float d = best >= inf * inf ? std::numeric_limits<float>::infinity() : (float)std::sqrt((double)best);
+      out[y * W + x] = basins ? (m[y * W + x] != 0 ? -d : -std::numeric_limits<float>::max()) : d;
+    }
+}
+
+// The reference's own queue-based transform: src/segment/MorphologicOperations.cpp:197-275
+// (nscale::distanceTransform) with checkDistNeighbors8 (31-89), propagateDist (91-121) and
+// propagateDist8 (123-195).  Zero pixels with a non-zero 8-neighbour seed a FIFO queue in raster
+// order; a popped pixel offers its nearest zero pixel to its neighbours (upper left, upper
+// right, upper, lower left, lower right, lower, left, right), which take it when it is strictly
+// closer (float distances) and are queued again.  Non-zero pixels start at the index
+// rows*cols*3.  The result is the distance to the nearest zero pixel found.
+inline void dist_queue_u8(const uint8_t* m, int64_t H, int64_t W, float* out) {
+  std::vector<int> nn((size_t)(H * W));
+  std::deque<std::pair<int, int>> q;
+  const int far = (int)(H * W * 3);
+  auto fdist = [&](int64_t px, int64_t py, int idx) {
+    const double dx = (double)(px - idx % W), dy = (double)(py - idx / W);
+    return (float)std::sqrt(dx * dx + dy * dy);
+  };
+  for (int64_t y = 0; y < H; ++y)
+    for (int64_t x = 0; x < W; ++x) {
+      nn[y * W + x] = far;
+      if (m[y * W + x] != 0) continue;
+      nn[y * W + x] = (int)(y * W + x);
+      bool edge = false;
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int64_t yy = y + dy, xx = x + dx;
+          if ((dx || dy) && yy >= 0 && yy < H && xx >= 0 && xx < W && m[yy * W + xx] != 0) edge = true;
+        }
+      if (edge) q.emplace_back((int)x, (int)y);
+    }
+  const int order[8][2] = {{-1, -1}, {1, -1}, {0, -1}, {-1, 1}, {1, 1}, {0, 1}, {-1, 0}, {1, 0}};
+  while (!q.empty()) {
+    const int x = q.front().first, y = q.front().second;
+    q.pop_front();
+    for (const auto& o : order) {
+      const int64_t tx = x + o[0], ty = y + o[1];
+      if (tx < 0 || tx >= W || ty < 0 || ty >= H) continue;
+      const int cur = nn[y * W + x];
+      if (fdist(tx, ty, cur) < fdist(tx, ty, nn[ty * W + tx])) {
+        nn[ty * W + tx] = cur;
+        q.emplace_back((int)tx, (int)ty);
+      }
+    }
+  }
+  for (int64_t y = 0; y < H; ++y)
+    for (int64_t x = 0; x < W; ++x) {
+      const int64_t c = nn[y * W + x], dx = x - c % W, dy = y - c / W;
+      out[y * W + x] = (float)std::sqrt((double)(dx * dx + dy * dy));
+    }
+}
+
 }  // namespace orc

@@ -44,6 +44,11 @@ int main(int argc, char** argv) {
   for (int i = 0; i < 9; ++i) cross.data[i] = (i % 2) ? 1 : (i == 4 ? 1 : 0);
   cv::Mat opened = nscale::morphOpen<unsigned char>(mask, cross);
   save(dir, "open3.u8", opened);
+  cv::Mat bin_mask(H, W, CV_8UC1);
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) bin_mask.ptr<unsigned char>(y)[x] = mask.ptr<unsigned char>(y)[x] < 128 ? 255 : 0;
+  cv::Mat dist = nscale::distanceTransform(bin_mask);
+  save(dir, "dist.f32", dist);
 
   // device signatures (MorphologicOperations.h:96-190)
   cv::gpu::Stream stream;

@@ -40,10 +40,12 @@ def test_status_strings_and_workspace_sizes():
     lib = ffi.lib
     assert lib.nsgb_status_string(0) == b"ok"
     assert b"workspace" in lib.nsgb_status_string(3)
-    for op in range(11):
+    for op in range(12):
         for dt in range(4):
             assert lib.nsgb_workspace_size(op, dt, 64, 64) > 0
-    assert lib.nsgb_workspace_size(11, 0, 64, 64) == 0
+    assert lib.nsgb_workspace_size(12, 0, 64, 64) == 0
+    # distance transform: column distances and the row pass's two stacks, 4 B/px each
+    assert lib.nsgb_workspace_size(ffi.OP_DISTANCE, ffi.U8, 100, 130) >= 3 * 4 * 100 * 130
     # opening: the status word and the eroded image with rows padded to 128 bytes
     assert lib.nsgb_workspace_size(ffi.OP_MORPH_OPEN, ffi.U8, 100, 130) >= 256 + 100 * 256
     assert lib.nsgb_workspace_size(-1, 0, 64, 64) == 0
@@ -85,6 +87,11 @@ def test_argument_errors_need_no_gpu():
     assert lib.nsgb_morph_open(1, 4096, 4, 4, 4, 4, None, 3, 1, 1 << 20, None, None) == 1
     assert lib.nsgb_morph_open(4096, 4100, 4, 4, 4, 4, ka(k3), 3, 1, 1 << 20, None, None) == 1
     assert lib.nsgb_morph_open(4096, 8192, 4, 4, 4, 4, ka(k3), 3, None, 0, None, None) == 3
+    # distance transform: null mask, float pitch not a multiple of 4, too many rows, no workspace
+    assert lib.nsgb_distance_transform(None, 1, 4, 4, 4, 16, 0, 1, 1 << 20, None, None) == 1
+    assert lib.nsgb_distance_transform(1, 1, 4, 4, 4, 18, 0, 1, 1 << 20, None, None) == 1
+    assert lib.nsgb_distance_transform(1, 1, 65535 * 128 + 1, 1, 1, 4, 0, 1, 1 << 30, None, None) == 1
+    assert lib.nsgb_distance_transform(1, 1, 4, 4, 4, 16, 0, None, 0, None, None) == 3
     # nucleus candidates: null image, pitch below the row, missing workspace
     assert lib.nsgb_nucleus_candidates(None, 1, 1, 1, 4, 4, 4, 80.0, 45.0, 11, 1000, None, None, 1, 1 << 20,
                                        None, None) == 1

@@ -1,6 +1,7 @@
 """The C++ API mirror run on the GPU: nscale::imreconstruct / imfillHoles / bwlabel2 /
 bwareaopen2 / imhmin and nscale::gpu::imreconstruct / imreconstructQueueThroughput /
-boundingBox2 and nscale::morphOpen give the oracle's results; a type mismatch raises cv::Exception."""
+boundingBox2, nscale::morphOpen and nscale::distanceTransform give the oracle's
+results; a type mismatch raises cv::Exception."""
 import subprocess
 
 import numpy as np
@@ -37,6 +38,8 @@ def test_cpp_api_matches_oracle(nsgb, oracle, tmp_path):
     assert np.array_equal(load("hmin8.u8", np.uint8), oracle.imhmin(mask, 10, 8))
     cross = np.array([[0, 1, 0], [1, 1, 1], [0, 1, 0]], np.uint8)
     assert np.array_equal(load("open3.u8", np.uint8), oracle.morph_open(mask, cross))
+    bin_mask = np.where(mask < 128, 255, 0).astype(np.uint8)
+    assert np.array_equal(load("dist.f32", np.float32), oracle.distance_transform(bin_mask))
     box = oracle.bounding_box(lab, 0)
     assert f"boxes {box.shape[1]}" in r.stdout
     assert np.array_equal(np.fromfile(tmp_path / "bbox.i32", dtype=np.int32).reshape(5, -1), box)

@@ -365,3 +365,55 @@ def test_disk19_matches_reference_shape():
     assert d.shape == (19, 19) and int(d.sum()) == 321
     assert np.array_equal(d, d[::-1]) and np.array_equal(d, d[:, ::-1]) and np.array_equal(d, d.T)
     assert [int(r.sum()) for r in d[:5]] == [11, 13, 15, 17, 19]
+
+
+def _blob_mask(rng, h, w, n):
+    m = np.zeros((h, w), np.uint8)
+    yy, xx = np.mgrid[0:h, 0:w]
+    for _ in range(n):
+        cy, cx, r = rng.integers(0, h), rng.integers(0, w), rng.integers(2, 15)
+        m[(yy - cy) ** 2 + (xx - cx) ** 2 <= r * r] = 255
+    return m
+
+
+@pytest.mark.parametrize("case", ["blobs", "noise", "one_zero", "row", "col", "dense"])
+def test_distance_transform_exact(oracle, case):
+    """The oracle's distance map equals scipy's exact EDT (float64 sqrt of the integer squared
+    distance, rounded to float32), and the basins follow HistologicalEntities.cpp:347-356."""
+    rng = np.random.default_rng(len(case))
+    if case == "blobs":
+        m = _blob_mask(rng, 120, 150, 25)
+    elif case == "noise":
+        m = np.where(rng.random((60, 70)) < 0.8, 255, 0).astype(np.uint8)
+    elif case == "one_zero":
+        m = np.full((50, 90), 255, np.uint8)
+        m[49, 0] = 0
+    elif case == "row":
+        m = np.where(rng.random((1, 200)) < 0.9, 7, 0).astype(np.uint8)
+    elif case == "col":
+        m = np.where(rng.random((200, 1)) < 0.9, 7, 0).astype(np.uint8)
+    else:
+        m = np.where(rng.random((80, 80)) < 0.995, 1, 0).astype(np.uint8)
+        m[0, 0] = 0
+    d = oracle.distance_transform(m)
+    exp = ndi.distance_transform_edt(m != 0).astype(np.float32)
+    assert np.array_equal(d, exp)
+    b = oracle.distance_transform(m, basins=True)
+    assert np.array_equal(b, np.where(m != 0, -exp, -np.finfo(np.float32).max).astype(np.float32))
+
+
+def test_distance_transform_without_zero(oracle):
+    d = oracle.distance_transform(np.full((5, 7), 3, np.uint8))
+    assert np.isinf(d).all() and (d > 0).all()
+
+
+def test_distance_queue_never_below_exact(oracle):
+    """The reference's queue propagation settles on a real zero pixel, so it is never closer than
+    the exact distance; on blob masks it agrees almost everywhere."""
+    rng = np.random.default_rng(3)
+    m = _blob_mask(rng, 200, 260, 60)
+    exact = oracle.distance_transform(m)
+    queue = oracle.distance_queue(m)
+    assert (queue >= exact).all()
+    assert (queue == exact).mean() > 0.99
+    assert (queue[m == 0] == 0).all()
