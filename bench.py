@@ -628,18 +628,51 @@ def cpu_tile_parallel(tiles_u8, budget_tiles):
             "sample": f"first {len(sample)} of the u8 tiles, one tile per thread, {dt:.1f} s"}
 
 
+def combine_batched(r, px):
+    """One dtype's batched figures over the ranks: the slowest rank's times, all ranks' pixels."""
+    from nsgb.shard import combine
+
+    out = dict(r)
+    total = px
+    for arm in ("plain", "plain_async", "batched"):
+        key = "batched_ms" if arm == "batched" else f"{arm}_ms"
+        if key in r:
+            out[key], total = combine(r[key], px)
+    mp = total / 1e6
+    if "plain_ms" in out:
+        out["plain_mpix_s"] = mp / (out["plain_ms"] / 1e3)
+        out["plain_async_mpix_s"] = mp / (out["plain_async_ms"] / 1e3)
+        out["speedup_vs_plain"] = out["plain_ms"] / out["batched_ms"]
+        out["speedup_vs_plain_async"] = out["plain_async_ms"] / out["batched_ms"]
+    out["batched_graph_mpix_s"] = mp / (out["batched_ms"] / 1e3)
+    if "batch_equals_single_tile" in r:
+        ok, _ = combine(0.0 if r["batch_equals_single_tile"] else 1.0, 0)  # any rank that differs -> 1
+        out["batch_equals_single_tile"] = ok == 0.0
+    return out
+
+
 def batched_section(args, dev):
+    rank, world, _ = dist_info()
     tiles = batch_tiles_host(args.batch_tiles)
+    all_px = int(sum(m.size for m, _ in tiles))
+    if world > 1:
+        from nsgb.shard import rank_tiles
+
+        tiles = [tiles[i] for i in rank_tiles([m.size for m, _ in tiles], world, rank)]
     res = {"workload": f"{args.batch_tiles} tiles, H and W i.i.d. uniform in [256,4096], 1 ellipse per 2800 px^2, "
                        "chain (a)-(e) per tile; u16 = u8 x 257, i32 = u8 x 1000 (threshold scaled the same way)",
-           "total_px": int(sum(m.size for m, _ in tiles)),
+           "total_px": all_px,
+           "sharding": (f"tiles split over {world} ranks by pixel count (largest first onto the least-loaded "
+                        f"rank), no exchange; times are the slowest rank's") if world > 1 else "one GPU",
            "plain": "nsgb_chain per tile on one stream, counts read per tile (the reference API returns them)",
            "plain_async": "nsgb_chain per tile on one stream, no count reads",
            "batched": "nsgb_chain_batch + nsgb_batch_counts_async recorded once in a CUDA graph, replayed",
            "l2": "inputs larger than L2; marker restore outside the timed events"}
+    my_px = int(sum(m.size for m, _ in tiles))
     for d in [x for x in args.batch_dtypes.split(",") if x]:
-        res[d] = run_batched(args, dev, tiles, d)
-    if not args.no_cpu_baseline:
+        r = run_batched(args, dev, tiles, d)
+        res[d] = combine_batched(r, my_px) if world > 1 else r
+    if not args.no_cpu_baseline and world == 1:
         res["cpu_tile_parallel"] = cpu_tile_parallel(tiles, 2 * (os.cpu_count() or 1))
     return res
 
