@@ -334,7 +334,7 @@ def morphOpen(image: torch.Tensor, kernel) -> torch.Tensor:
     _check_image(image, "image")
     if image.dtype != torch.uint8:
         raise NsgbError(2, "morphOpen: image must be uint8 (the reference's one instantiation)")
-    k = np.ascontiguousarray(np.asarray(kernel).astype(np.uint8))
+    k = np.ascontiguousarray((np.asarray(kernel) != 0).astype(np.uint8))
     if k.ndim != 2 or k.shape[0] != k.shape[1]:
         raise NsgbError(1, "morphOpen: kernel must be square")
     img = _contig(image)
