@@ -350,7 +350,10 @@ def test_morph_open(oracle, shape):
     img = rng.integers(0, 256, shape).astype(np.uint8)
     asym = (rng.random((5, 5)) < 0.4).astype(np.uint8)
     asym[0, 4] = 1
-    for kern in (disk19(), ellipse3(), np.ones((3, 3), np.uint8), asym):
+    y, x = np.mgrid[-31:32, -31:32]
+    disk63 = (x * x + y * y <= 31 * 31).astype(np.uint8)
+    kerns = (disk19(), ellipse3(), np.ones((3, 3), np.uint8), asym) + ((disk63,) if shape[0] * shape[1] < 1000 else ())
+    for kern in kerns:
         got = oracle.morph_open(img, kern)
         assert np.array_equal(got, np_morph_open(img, kern))
         if np.array_equal(kern, kern[::-1, ::-1]):  # symmetric: scipy's footprint convention agrees
@@ -376,7 +379,7 @@ def _blob_mask(rng, h, w, n):
     return m
 
 
-@pytest.mark.parametrize("case", ["blobs", "noise", "one_zero", "row", "col", "dense"])
+@pytest.mark.parametrize("case", ["blobs", "noise", "one_zero", "row", "col", "dense", "band", "far"])
 def test_distance_transform_exact(oracle, case):
     """The oracle's distance map equals scipy's exact EDT (float64 sqrt of the integer squared
     distance, rounded to float32), and the basins follow HistologicalEntities.cpp:347-356."""
@@ -392,9 +395,16 @@ def test_distance_transform_exact(oracle, case):
         m = np.where(rng.random((1, 200)) < 0.9, 7, 0).astype(np.uint8)
     elif case == "col":
         m = np.where(rng.random((200, 1)) < 0.9, 7, 0).astype(np.uint8)
-    else:
+    elif case == "dense":
         m = np.where(rng.random((80, 80)) < 0.995, 1, 0).astype(np.uint8)
         m[0, 0] = 0
+    elif case == "band":  # zeros in a few rows and columns only: columns without any zero
+        m = np.full((300, 200), 9, np.uint8)
+        m[130:140:3, ::37] = 0
+    else:  # one zero row with a gap: distances grow down the image
+        m = np.full((400, 150), 255, np.uint8)
+        m[0, :] = 0
+        m[0, 75] = 255
     d = oracle.distance_transform(m)
     exp = ndi.distance_transform_edt(m != 0).astype(np.float32)
     assert np.array_equal(d, exp)
