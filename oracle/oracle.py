@@ -54,6 +54,7 @@ def _load() -> C.CDLL:
     lib.orc_recon_f32_prov.restype = C.c_int
     lib.orc_recon_f32_grad.argtypes = [vp, vp, i64, i64, i64, vp, vp, C.c_int]
     lib.orc_recon_fd.argtypes = [vp, vp, vp, i64, i64, C.c_int, vp, i64, C.c_double, vp, vp, C.c_int]
+    lib.nsgb_synth_tile_u8.argtypes = [vp, vp, i64, i64, i64, i64, C.c_uint64]
     return lib
 
 
@@ -66,6 +67,16 @@ def _p(a):
 
 def _c(a: np.ndarray) -> np.ndarray:
     return np.ascontiguousarray(a)
+
+
+def synth_tile_u8(H: int, W: int, n_ellipses: int, seed: int = 0):
+    """(mask, marker) of the seeded generator (csrc/synth.cpp, built into liboracle.so), the
+    same bytes as nsgb.synth.tile_u8, for CPU-only processes."""
+    mask = np.empty((H, W), np.uint8)
+    marker = np.empty((H, W), np.uint8)
+    if lib.nsgb_synth_tile_u8(_p(mask), _p(marker), H, W, W, n_ellipses, seed) != 0:
+        raise ValueError("bad synth arguments")
+    return mask, marker
 
 
 def imreconstruct(seeds: np.ndarray, image: np.ndarray, conn: int) -> np.ndarray:
@@ -208,6 +219,135 @@ def chain_replicas_seconds(marker: np.ndarray, mask: np.ndarray, threads: int, r
 # -- the reference's own ConnComponents (only where it was built) ---------------------------
 def ref_available() -> bool:
     return os.path.exists(REF_LIB)
+
+
+# -- the reference's own serial reconstruction functions (only where they were built) ------
+# libmorph_ref.so follows OpenCV's CV_32S arithmetic (wrap-around); libmorph_ref_sat.so is the
+# same code with saturating CV_32S arithmetic (the reading the oracle takes for
+# invert<int>(INT_MIN)).  See oracle/ref_morph.cpp and oracle/cv_shim.hpp.
+REF_MORPH_LIB = os.path.join(HERE, "_ref", "libmorph_ref.so")
+REF_MORPH_SAT_LIB = os.path.join(HERE, "_ref", "libmorph_ref_sat.so")
+
+
+def ref_morph_available() -> bool:
+    return os.path.exists(REF_MORPH_LIB) and os.path.exists(REF_MORPH_SAT_LIB)
+
+
+_ref_morph_libs = {}
+
+
+def _ref_morph(saturate_32s: bool = False) -> C.CDLL:
+    key = bool(saturate_32s)
+    if key not in _ref_morph_libs:
+        r = C.CDLL(REF_MORPH_SAT_LIB if key else REF_MORPH_LIB)
+        vp, i64, i32 = C.c_void_p, C.c_int64, C.c_int32
+        r.ref_imreconstruct.argtypes = [C.c_int, vp, vp, i64, i64, C.c_int, vp]
+        r.ref_imreconstruct_binary.argtypes = [C.c_int, vp, vp, i64, i64, C.c_int, vp]
+        r.ref_imfill_holes.argtypes = [C.c_int, vp, i64, i64, C.c_int, C.c_int, vp]
+        r.ref_imhmin.argtypes = [C.c_int, vp, i64, i64, C.c_double, C.c_int, vp]
+        r.ref_bwselect.argtypes = [C.c_int, vp, vp, i64, i64, C.c_int, vp]
+        r.ref_threshold_gt.argtypes = [C.c_int, vp, i64, i64, C.c_double, vp]
+        r.ref_bwlabel2.argtypes = [vp, i64, i64, C.c_int, C.c_int, vp]
+        r.ref_bwlabel2.restype = C.c_int
+        r.ref_bwareaopen2.argtypes = [vp, C.c_int, C.c_int, i32, i32, C.c_int, i64, i64, vp]
+        r.ref_bwareaopen2.restype = C.c_int
+        r.ref_chain.argtypes = [C.c_int, vp, vp, i64, i64, C.c_int, C.c_double, C.c_int, C.c_int, i32, i32,
+                                vp, vp, vp, vp, C.POINTER(i32), vp]
+        r.ref_chain.restype = i32
+        r.ref_chain_replicas_seconds.argtypes = [vp, vp, i64, i64, C.c_int, C.c_int]
+        r.ref_chain_replicas_seconds.restype = C.c_double
+        _ref_morph_libs[key] = r
+    return _ref_morph_libs[key]
+
+
+def ref_imreconstruct(seeds, image, conn, saturate_32s=False):
+    seeds, image = _c(seeds), _c(image)
+    out = np.empty_like(image)
+    rc = _ref_morph(saturate_32s).ref_imreconstruct(DT[image.dtype], _p(seeds), _p(image), *image.shape, conn,
+                                                    _p(out))
+    assert rc == 0, rc
+    return out
+
+
+def ref_imreconstruct_binary(seeds, image, conn, saturate_32s=False):
+    seeds, image = _c(seeds), _c(image)
+    out = np.empty_like(image)
+    rc = _ref_morph(saturate_32s).ref_imreconstruct_binary(DT[image.dtype], _p(seeds), _p(image), *image.shape,
+                                                           conn, _p(out))
+    assert rc == 0, rc
+    return out
+
+
+def ref_imfill_holes(image, binary, conn, saturate_32s=False):
+    image = _c(image)
+    out = np.empty_like(image)
+    rc = _ref_morph(saturate_32s).ref_imfill_holes(DT[image.dtype], _p(image), *image.shape, int(binary), conn,
+                                                   _p(out))
+    assert rc == 0, rc
+    return out
+
+
+def ref_imhmin(image, h, conn, saturate_32s=False):
+    image = _c(image)
+    out = np.empty_like(image)
+    rc = _ref_morph(saturate_32s).ref_imhmin(DT[image.dtype], _p(image), *image.shape, float(h), conn, _p(out))
+    assert rc == 0, rc
+    return out
+
+
+def ref_bwselect(image, seeds, conn, saturate_32s=False):
+    image, seeds = _c(image), _c(seeds)
+    out = np.empty_like(image)
+    rc = _ref_morph(saturate_32s).ref_bwselect(DT[image.dtype], _p(image), _p(seeds), *image.shape, conn, _p(out))
+    assert rc == 0, rc
+    return out
+
+
+def ref_threshold_gt(image, thr):
+    image = _c(image)
+    out = np.empty(image.shape, np.uint8)
+    assert _ref_morph().ref_threshold_gt(DT[image.dtype], _p(image), *image.shape, float(thr), _p(out)) == 0
+    return out
+
+
+def ref_bwlabel2(binary, conn, relab):
+    binary = _c(binary).astype(np.uint8, copy=False)
+    out = np.empty(binary.shape, np.int32)
+    n = _ref_morph().ref_bwlabel2(_p(binary), *binary.shape, conn, int(relab), _p(out))
+    assert n >= 0
+    return out, int(n)
+
+
+def ref_bwareaopen2(image, labeled, flatten, lo, hi, conn):
+    image = _c(image)
+    out = np.empty(image.shape, np.uint8 if flatten else np.int32)
+    n = _ref_morph().ref_bwareaopen2(_p(image), int(labeled), int(flatten), lo, hi, conn, *image.shape, _p(out))
+    assert n >= 0
+    return out, int(n)
+
+
+def ref_chain(marker, mask, recon_conn=8, thr=128.0, fill_conn=4, label_conn=8, lo=11, hi=1000):
+    marker, mask = _c(marker), _c(mask)
+    H, W = mask.shape
+    rec = np.empty_like(mask)
+    b = np.empty((H, W), np.uint8)
+    f = np.empty((H, W), np.uint8)
+    lab = np.empty((H, W), np.int32)
+    a = np.empty((H, W), np.uint8)
+    nl = C.c_int32(0)
+    kept = _ref_morph().ref_chain(DT[mask.dtype], _p(marker), _p(mask), H, W, recon_conn, float(thr), fill_conn,
+                                  label_conn, lo, hi, _p(rec), _p(b), _p(f), _p(lab), C.byref(nl), _p(a))
+    assert kept >= 0
+    return {"recon": rec, "thr": b, "fill": f, "labels": lab, "n_labels": int(nl.value), "area": a,
+            "n_kept": int(kept)}
+
+
+def ref_chain_replicas_seconds(marker, mask, threads: int, reps: int) -> float:
+    marker, mask = _c(marker), _c(mask)
+    t = _ref_morph().ref_chain_replicas_seconds(_p(marker), _p(mask), mask.shape[0], mask.shape[1], threads, reps)
+    if t < 0:
+        raise RuntimeError("the reference chain failed")
+    return float(t)
 
 
 def _ref() -> C.CDLL:

@@ -40,7 +40,10 @@ inline T type_min() {
 
 // src/segment/PixelOperations.cpp:18-39.  Unsigned: max - x.  Signed: bitwise_not(x) + 1
 // through OpenCV arithmetic; the one value where that overflows (INT_MIN) is taken with
-// OpenCV's saturating semantics, i.e. invert(INT_MIN) = INT_MAX.  Float: -x.
+// saturating arithmetic, i.e. invert(INT_MIN) = INT_MAX.  OpenCV itself does not saturate
+// CV_32S (it wraps, and the reference's imfillHoles<int> then returns INT_MIN everywhere;
+// tests/test_oracle_ref_recon_cpu.py pins both readings against the reference's code).
+// Float: OpenCV evaluates `-img` as `0 - img`, so the result is never -0.0.
 template <typename T>
 inline T invert_px(T x) {
   if constexpr (std::numeric_limits<T>::is_integer) {
@@ -51,7 +54,7 @@ inline T invert_px(T x) {
       return (T)(std::numeric_limits<T>::max() - x);
     }
   } else {
-    return -x;
+    return (T)0 - x;
   }
 }
 
@@ -460,12 +463,18 @@ inline int32_t bwareaopen2(const void* image, bool labeled, bool flatten, int32_
   return count;
 }
 
-// `Mat > k` (HistologicalEntities.cpp:214): 255 where strictly greater, else 0.  The
-// comparison is against the double-valued scalar, as OpenCV's compare does (k is not
-// rounded to the pixel type: u8 `> -1` is true everywhere).
+// `Mat > k` (HistologicalEntities.cpp:214): 255 where strictly greater, else 0.  OpenCV's
+// compare converts the scalar to the image's depth: an integer image compares with floor(k)
+// (the same as x > k for integer x; u8 `> -1` is true everywhere), a float image with k
+// rounded to float.
 template <typename T>
 inline void threshold_gt(const T* in, int64_t n, double k, uint8_t* out) {
-  for (int64_t i = 0; i < n; ++i) out[i] = (double)in[i] > k ? 255 : 0;
+  if constexpr (std::is_floating_point_v<T>) {
+    const T kk = (T)k;
+    for (int64_t i = 0; i < n; ++i) out[i] = in[i] > kk ? 255 : 0;
+  } else {
+    for (int64_t i = 0; i < n; ++i) out[i] = (double)in[i] > k ? 255 : 0;
+  }
 }
 
 // ---------------------------------------------------------------------------------------

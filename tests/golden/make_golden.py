@@ -13,7 +13,7 @@ Sources of truth, both independent of the oracle restatement:
     reference's own ConnComponents::boundingBox output for them.
   * synth_digest.json -- SHA-256 of generator outputs, pinning the synthetic inputs across
     machines (x86-64 here, aarch64 on the GPU hosts).
-Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [--bbox-only]
+Usage: python tests/golden/make_golden.py REFERENCE_ROOT [--bbox-only]  (or NSGB_REFERENCE_DIR=...)
 """
 from __future__ import annotations
 
@@ -115,7 +115,9 @@ def write_bbox(oracle):
 
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    ref_root = args[0] if args else "/root/reference/fastIA-master"
+    ref_root = args[0] if args else os.environ.get("NSGB_REFERENCE_DIR", "")
+    if not ref_root and "--bbox-only" not in sys.argv:
+        raise SystemExit("usage: make_golden.py REFERENCE_ROOT [--bbox-only]  (or set NSGB_REFERENCE_DIR)")
     import oracle  # noqa: E402
 
     if "--bbox-only" in sys.argv:
