@@ -11,8 +11,10 @@ MPix/s with inputs already resident in HBM (marker reset and L2 flushed outside 
 events before every step); `e2e` is the same chain through the C ABI with host buffers,
 host->device copies of marker and mask and device->host copies of labels and the area mask
 inside the timed region (steps alternate between two streams with their own buffers, so the
-copies of one step overlap the kernels of the other).  `--impl reference` times the reference's CPU algorithm (the
-oracle port in oracle/, or the reference's own code where it was compiled) on all host cores.
+copies of one step overlap the kernels of the other).  `--impl reference` times the reference's
+own CPU code for the chain (its MorphologicOperations / ConnComponents functions compiled from
+its sources into oracle/_ref/; the oracle's restatement where that was not built) on the full
+tile, one tile per host core per step, loading no device library.
 
 Multi-GPU (torchrun, one process per GPU): the path does not shard a single tile, so every
 rank processes its own tile (replicas, weak scaling); the max over ranks of the step time
@@ -45,8 +47,8 @@ CHAIN_BYTES_PER_PX = 17  # recon 3 + threshold 2 + fill 2 + bwlabel 5 + bwareaop
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=400)
-    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--steps", type=int, default=None, help="default: 400 (GPU arm), 5 (--impl reference)")
+    p.add_argument("--warmup", type=int, default=None, help="default: 10 (GPU arm), 1 (--impl reference)")
     p.add_argument("--impl", default="nsgb", choices=["nsgb", "reference"])
     p.add_argument("--size", type=int, default=4096)
     p.add_argument("--ellipses", type=int, default=6000)
@@ -67,7 +69,12 @@ def parse_args():
     p.add_argument("--candidates-only", action="store_true",
                    help="profiling aid: only the segmentation-stage sections (opening + candidates, distance)")
     p.add_argument("--large-size", type=int, default=16384)
-    return p.parse_args()
+    a = p.parse_args()
+    if a.steps is None:
+        a.steps = 5 if a.impl == "reference" else 400
+    if a.warmup is None:
+        a.warmup = 1 if a.impl == "reference" else 10
+    return a
 
 
 def dist_info():
@@ -158,51 +165,62 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline_port(marker, mask, budget_s=12.0):
-    """Single-thread oracle chain (the reference's serial algorithm) on the same tile."""
+def _cpu_chain_timer():
+    """(timer, kind, what): the reference's own compiled chain (oracle/_ref, built from the
+    reference's sources) where it was built, else the oracle's restatement of it."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
-    t = oracle.chain_replicas_seconds(marker, mask, 1, 1)
+    if oracle.ref_morph_available():
+        return (oracle.ref_chain_replicas_seconds, "reference",
+                "the reference's own imreconstruct<uchar> / imfillHoles<uchar> / bwlabel2 / bwareaopen2 "
+                "(MorphologicOperations.cpp, ConnComponents.cpp compiled from its sources, oracle/_ref)")
+    return (oracle.chain_replicas_seconds, "port",
+            "the oracle's C++ restatement of imreconstruct / imfillHoles / bwlabel2 / bwareaopen2")
+
+
+def cpu_baseline(marker, mask, budget_s=12.0):
+    """The reference's serial chain (a)-(e) on one host core, on the same tile."""
+    timer, kind, what = _cpu_chain_timer()
+    t = timer(marker, mask, 1, 1)
     reps = max(1, min(20, int(round(budget_s / max(t, 1e-3)))))
-    t = oracle.chain_replicas_seconds(marker, mask, 1, reps)
+    t = timer(marker, mask, 1, reps)
     mpix = reps * mask.size / 1e6
-    kind = "reference" if oracle.ref_available() else "port"
-    return {"value": mpix / t, "unit": "MPix/s", "cores": 1, "kind": "port",
+    return {"value": mpix / t, "unit": "MPix/s", "cores": 1, "kind": kind,
             "sample": f"{reps} serial runs of the full {mask.shape[0]}x{mask.shape[1]} u8 chain (a)-(e), "
-                      f"{t:.1f} s; oracle C++ restatement of imreconstruct/imfillHoles/bwlabel2/bwareaopen2"
-                      + ("" if kind == "port" else " (reference ConnComponents available but not used)")}
+                      f"{t:.1f} s, one thread; {what}"}
 
 
 def run_reference(args):
+    """The reference's CPU implementation of the chain on all host cores: every step runs the
+    full workload tile through the chain once per host thread (independent tiles, one per core),
+    so the sample is `threads` tiles of exactly the GPU arm's workload.  Loads only oracle/
+    libraries (the generator included), no device library."""
     rank, world, _ = dist_info()
     if rank != 0:
         return 0
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
-    from nsgb import synth
 
+    timer, kind, what = _cpu_chain_timer()
     threads = os.cpu_count() or 1
-    # Bounded sample: a 1024-row strip of the tile per thread per step (same width, same
-    # ellipse density), so that a full --steps/--warmup run stays within minutes.
-    rows = min(args.size, 1024)
-    n_ell = int(round(args.ellipses * rows / args.size))
-    mask, marker = synth.tile_u8(rows, args.size, n_ell, 0)
+    mask, marker = oracle.synth_tile_u8(args.size, args.size, args.ellipses, 0)
     for _ in range(args.warmup):
-        oracle.chain_replicas_seconds(marker, mask, threads, 1)
-    times = [oracle.chain_replicas_seconds(marker, mask, threads, 1) for _ in range(args.steps)]
+        timer(marker, mask, threads, 1)
+    times = [timer(marker, mask, threads, 1) for _ in range(args.steps)]
     ms = statistics.mean(times) * 1e3
     value = threads * mask.size / 1e6 / (ms / 1e3)
+    workload = (f"single-tile chain (a)-(e): u8 {args.size}x{args.size}, {args.ellipses} ellipses, recon 8-conn, "
+                f"threshold >128, fillHoles binary 4-conn, bwlabel 8-conn relabel, bwareaopen [11,1000)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "MPix/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": f"single-tile chain (a)-(e), u8 {args.size}x{args.size}, 6000 ellipses; "
-                               f"CPU sample {rows}x{args.size} strip per thread per step",
-                   "threads": threads},
-        "cpu_baseline": {"value": value, "unit": "MPix/s", "cores": threads,
-                         "kind": "reference" if oracle.ref_available() else "port",
-                         "sample": f"{threads} threads x one {rows}x{args.size} u8 chain (a)-(e) per step"},
+        "config": {"workload": workload, "threads": threads,
+                   "step": f"{threads} host threads, each running the full tile through the chain once"},
+        "cpu_baseline": {"value": value, "unit": "MPix/s", "cores": threads, "kind": kind,
+                         "sample": f"{threads} threads x one {args.size}x{args.size} u8 chain (a)-(e) per step; "
+                                   f"{what}"},
         "e2e": {"value": value, "unit": "MPix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -426,7 +444,7 @@ def run_nsgb(args):
         "clocks": clk,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_port(marker_h, mask_h)
+        line["cpu_baseline"] = cpu_baseline(marker_h, mask_h)
     if not args.no_batch:
         line["batched"] = batched_section(args, dev)
     if not args.no_grad:
