@@ -187,6 +187,16 @@ struct Px<float> {
   __device__ static __forceinline__ uint32_t emin(uint32_t a, uint32_t b) { return vmin(a, b); }
 };
 
+// Argument checks shared by every entry point.  Each dimension is bounded before the product
+// is formed, so a wrapped product cannot pass.
+inline bool valid_dims(int64_t rows, int64_t cols) {
+  return rows > 0 && cols > 0 && rows < INT32_MAX && cols < INT32_MAX && rows * cols < (int64_t)INT32_MAX;
+}
+inline bool valid_pitch(int64_t pitch, int64_t cols, int esz) {
+  return esz > 0 && pitch >= cols * esz && pitch % esz == 0;
+}
+inline bool valid_conn(int conn) { return conn == 4 || conn == 8; }
+
 inline int elem_size(int dtype) {
   switch (dtype) {
     case NSGB_U8: return 1;

@@ -32,19 +32,29 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void* g_scratch_ptr[kMaxDevices] = {nullptr};
 
-// Device address of the scratch on the current device, looked up once per device.
-cudaError_t scratch_address(void** out) {
+// Device address of the scratch on the current device.  Outside stream capture it is looked up
+// on every call (cheap: a table lookup in the runtime), so a context that was reset or
+// re-created since the last call -- which loads the module again, possibly at another address
+// -- is followed.  While `s` is capturing, the address recorded by the last call outside
+// capture on this device is used (a lookup could load the module inside the capture); without
+// one the call fails.
+cudaError_t scratch_address(cudaStream_t s, void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(s, &cap);
+  const bool capturing = e != cudaSuccess || cap != cudaStreamCaptureStatusNone;
+  if (e != cudaSuccess) (void)cudaGetLastError();  // e.g. the legacy stream during a global capture
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_ptr[dev]) {
+  if (!capturing) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
     g_scratch_ptr[dev] = p;
   }
+  if (!g_scratch_ptr[dev]) return cudaErrorStreamCaptureUnsupported;
   *out = g_scratch_ptr[dev];
   return cudaSuccess;
 }
@@ -56,24 +66,35 @@ extern "C" nsgb_status nsgb_imreconstruct_noalloc(int dtype, void* marker, const
                                                   nsgb_stream_t stream, const nsgb_opts* opts) {
   const int esz = nsgb::elem_size(dtype);
   if (!esz) return NSGB_ERR_UNSUPPORTED_DTYPE;
-  if (!marker || !mask || rows <= 0 || cols <= 0 || rows * cols >= (int64_t)INT32_MAX || pitch < cols * esz ||
-      pitch % esz != 0 || (conn != 4 && conn != 8))
+  if (!marker || !mask || !nsgb::valid_dims(rows, cols) || !nsgb::valid_pitch(pitch, cols, esz) ||
+      !nsgb::valid_conn(conn))
     return NSGB_ERR_BAD_ARG;
   // Too large for the built-in scratch: refuse before touching the GPU.
   if (nsgb::recon_workspace_bytes(dtype, rows, cols) > (size_t)NSGB_NOALLOC_SCRATCH_BYTES)
     return NSGB_ERR_WORKSPACE;
-  void* ws = nullptr;
-  if (scratch_address(&ws) != cudaSuccess) return NSGB_ERR_CUDA;
   cudaStream_t s = (cudaStream_t)stream;
+  void* ws = nullptr;
+  if (scratch_address(s, &ws) != cudaSuccess) return NSGB_ERR_CUDA;
   const bool ring = !erode && (dtype == NSGB_I32 || dtype == NSGB_F32);
   if (opts && opts->recon_event_begin && cudaEventRecord((cudaEvent_t)opts->recon_event_begin, s) != cudaSuccess)
     return NSGB_ERR_CUDA;
   cudaError_t e = nsgb::recon_launch(dtype, marker, marker, mask, rows, cols, pitch, conn, erode != 0, ring, ws, s,
-                                     opts ? opts->max_visits_per_tile : 0, opts ? opts->max_visit_iters : 0);
+                                     opts ? opts->max_visits_per_tile : 0, opts ? opts->max_visit_iters : 0,
+                                     opts ? opts->queue_poll_limit : 0);
   if (e != cudaSuccess) return NSGB_ERR_CUDA;
   if (opts && opts->recon_event_end && cudaEventRecord((cudaEvent_t)opts->recon_event_end, s) != cudaSuccess)
     return NSGB_ERR_CUDA;
   if (opts && !opts->sync) return NSGB_OK;
+  return nsgb_noalloc_device_status(stream);
+}
+
+// Reads the device status word at the start of the built-in scratch, after the work already on
+// `stream`: the status of the last nsgb_imreconstruct_noalloc call on this device, as long as
+// no later call has started (each call resets it).
+extern "C" nsgb_status nsgb_noalloc_device_status(nsgb_stream_t stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  void* ws = nullptr;
+  if (scratch_address(s, &ws) != cudaSuccess) return NSGB_ERR_CUDA;
   int dev_status = 0;
   if (cudaMemcpyAsync(&dev_status, ws, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return NSGB_ERR_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return NSGB_ERR_CUDA;

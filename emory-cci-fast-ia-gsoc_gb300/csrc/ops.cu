@@ -42,8 +42,9 @@ __device__ __forceinline__ T* pxp(void* base, int64_t pitch, int y, int x) {
 
 // ------------------------------------------------------------------------------------------
 // `x > thr` with thr a double, as OpenCV's `Mat > k` compares (HistologicalEntities.cpp:214),
-// without double arithmetic on the device: for integer x it equals x > floor(thr), for float x
-// it equals x > (the largest float <= thr); both are prepared on the host.
+// without double arithmetic on the device: an integer image compares with floor(thr) (x > thr
+// for integer x); a float image with thr converted to float (rounded to nearest), since
+// OpenCV's compare converts the scalar to the image's depth.  Both are prepared on the host.
 template <typename T>
 struct GtThr {
   using K = std::conditional_t<std::is_floating_point<T>::value, float, int64_t>;
@@ -51,9 +52,7 @@ struct GtThr {
   static GtThr make(double thr) {
     GtThr g;
     if constexpr (std::is_floating_point<T>::value) {
-      float f = (float)thr;
-      if ((double)f > thr) f = nextafterf(f, -INFINITY);
-      g.k = f;
+      g.k = (float)thr;
     } else {
       if (thr != thr) g.k = INT64_MAX;  // NaN: nothing is greater
       else if (thr >= 9.0e18) g.k = INT64_MAX;
@@ -364,7 +363,18 @@ __device__ __forceinline__ T invert_value(T v) {
       return (T)(std::numeric_limits<T>::max() - v);
     }
   } else {
-    return -v;
+    return (T)0 - v;  // OpenCV's `-img` is `0 - img`: +0.0 for both zeros
+  }
+}
+
+// -0.0 -> +0.0 over a float plane.  The reference's float imhmin and imfillHoles end with
+// PixelOperations::invert (`0 - x`, never -0.0); the order-reversed reconstruction here flips
+// the sign bit instead, so their outputs pass through this once.
+__global__ void canon_zero_f32_kernel(float* out, int64_t pitch, int H, int W) {
+  NSGB_FOR_QUADS {
+    unsigned* o = (unsigned*)((char*)out + (int64_t)y * pitch) + x;
+    for (int k = 0; k < 4 && x + k < W; ++k)
+      if (o[k] == 0x80000000u) o[k] = 0u;
   }
 }
 
@@ -546,7 +556,7 @@ cudaError_t recon_timed(const nsgb_opts* o, int dtype, const Plan& P, int conn, 
   cudaError_t e = record(o, true, s);
   if (e != cudaSuccess) return e;
   e = recon_launch_batch(dtype, P.I, P.t.r_tiles, conn, erode, ring, ws, s, o ? o->max_visits_per_tile : 0,
-                         o ? o->max_visit_iters : 0, resweeps);
+                         o ? o->max_visit_iters : 0, resweeps, o ? o->queue_poll_limit : 0);
   if (e != cudaSuccess) return e;
   return record(o, false, s);
 }
@@ -650,11 +660,6 @@ using namespace nsgb;
 
 namespace {
 
-bool valid_dims(int64_t rows, int64_t cols) {
-  return rows > 0 && cols > 0 && rows * cols < (int64_t)INT_MAX && rows < INT_MAX && cols < INT_MAX;
-}
-bool valid_pitch(int64_t pitch, int64_t cols, int esz) { return pitch >= cols * esz && pitch % esz == 0; }
-bool valid_conn(int conn) { return conn == 4 || conn == 8; }
 bool want_sync(const nsgb_opts* o) { return o == nullptr || o->sync != 0; }
 
 nsgb_status cuda_status(cudaError_t e) { return e == cudaSuccess ? NSGB_OK : NSGB_ERR_CUDA; }
@@ -819,6 +824,10 @@ nsgb_status nsgb_imfill_holes(int dtype, const void* image, void* out, int64_t r
   }
   const Plan R = single_plan(dtype, out, image, rows, cols, pitch);
   e = recon_timed(opts, dtype, R, conn, true, false, ws, s, 2);  // front from the border: re-sweep
+  if (e == cudaSuccess && dtype == NSGB_F32) {
+    canon_zero_f32_kernel<<<quad_grid(rows, cols), 256, 0, s>>>((float*)out, pitch, H, W);
+    e = cudaGetLastError();
+  }
   return finish(e, ws, s, opts);
 }
 
@@ -842,6 +851,10 @@ nsgb_status nsgb_imhmin(int dtype, const void* image, void* out, int64_t rows, i
   // reference's 0-valued padding ring taken in the inverted domain.
   const Plan P = single_plan(dtype, out, image, rows, cols, pitch);
   cudaError_t e = recon_timed(opts, dtype, P, conn, true, true, ws, s);
+  if (e == cudaSuccess && dtype == NSGB_F32) {
+    canon_zero_f32_kernel<<<quad_grid(rows, cols), 256, 0, s>>>((float*)out, pitch, H, W);
+    e = cudaGetLastError();
+  }
   return finish(e, ws, s, opts);
 }
 

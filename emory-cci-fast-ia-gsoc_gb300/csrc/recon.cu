@@ -32,6 +32,8 @@
 #include <stdint.h>
 #include <stdlib.h>
 
+#include <atomic>
+
 #include "batch.cuh"
 #include "common.cuh"
 #include "recon.cuh"
@@ -862,10 +864,12 @@ int tiles_x_for(int64_t W) { return (int)((W + 32 * Px<T>::E - 1) / (32 * Px<T>:
 // images before the next colour: on the 256-tile u8 workload 24k re-runs instead of 525k with
 // the checkerboard).  NSGB_RECON_ORDER overrides it for experiments.
 inline int recon_order(int elems_per_word, bool batch) {
-  static int order = -2;
+  static std::atomic<int> cached{-2};
+  int order = cached.load(std::memory_order_relaxed);
   if (order == -2) {
     const char* e = getenv("NSGB_RECON_ORDER");
     order = (e && *e) ? atoi(e) : -1;
+    cached.store(order, std::memory_order_relaxed);
   }
   if (order >= 0) return order;
   return (elems_per_word == 2 && !batch) ? 1 : 2;
@@ -873,7 +877,7 @@ inline int recon_order(int elems_per_word, bool batch) {
 
 template <typename T, int CONN, bool BATCH, bool RS>
 cudaError_t launch_typed(const Imgs& I, int ntiles, bool erode, bool ring, void* ws, cudaStream_t s,
-                         int max_visits_per_tile, int max_iters, int resweeps) {
+                         int max_visits_per_tile, int max_iters, int resweeps, long long poll_limit) {
   Args a;
   a.I = I;
   a.ntiles = ntiles;
@@ -895,6 +899,7 @@ cudaError_t launch_typed(const Imgs& I, int ntiles, bool erode, bool ring, void*
   a.c.slots = (Slot*)(a.c.state + ((ntiles + 1) & ~1));
   a.c.max_visits = (long long)(max_visits_per_tile > 0 ? max_visits_per_tile : 1 << 20) * ntiles;
   a.c.budget_step = max_visits_per_tile > 0 ? 1 : 16;
+  a.c.spin_limit = poll_limit > 0 ? poll_limit : kSpinLimit;
 
   cudaError_t e = cudaMemsetAsync(wi, 0, sizeof(int) * kHdrInts, s);
   if (e != cudaSuccess) return e;
@@ -903,20 +908,28 @@ cudaError_t launch_typed(const Imgs& I, int ntiles, bool erode, bool ring, void*
   if (e != cudaSuccess) return e;
 
   const size_t smem = sizeof(WarpBuf) * kWarps;
-  static int occ_cache[8] = {0};  // per device, for this instantiation
+  // The shared-memory opt-in is set on every launch (it belongs to the context, which a device
+  // reset replaces); the co-resident grid size is computed once per device and instantiation.
+  // Two host threads' first calls may both compute it: they store the same value.
+  e = cudaFuncSetAttribute(recon_kernel<T, CONN, BATCH, RS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  constexpr int kOccDevices = 64;
+  static std::atomic<int> occ_cache[kOccDevices];
   int dev = 0;
-  cudaGetDevice(&dev);
-  int& occ = occ_cache[dev & 7];
+  e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const bool cached = dev >= 0 && dev < kOccDevices;
+  int occ = cached ? occ_cache[dev].load(std::memory_order_relaxed) : 0;
   if (occ == 0) {
-    e = cudaFuncSetAttribute(recon_kernel<T, CONN, BATCH, RS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
     int bps = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, recon_kernel<T, CONN, BATCH, RS>, kWarps * 32, smem);
     if (e != cudaSuccess) return e;
     int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
     occ = bps * sms;
     if (occ <= 0) return cudaErrorLaunchOutOfResources;
+    if (cached) occ_cache[dev].store(occ, std::memory_order_relaxed);
   }
   int grid = (ntiles + kWarps - 1) / kWarps;
   if (grid > occ) grid = occ;
@@ -958,24 +971,25 @@ namespace {
 // re-sweeps are offered for single images, where hole filling uses them).
 template <typename T, bool RS>
 cudaError_t dispatch_conn(const Imgs& I, int ntiles, int conn, bool erode, bool ring, void* ws, cudaStream_t s,
-                          int max_visits, int max_iters, int resweeps) {
+                          int max_visits, int max_iters, int resweeps, long long poll) {
   if (I.d)
-    return conn == 8 ? launch_typed<T, 8, true, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, 0)
-                     : launch_typed<T, 4, true, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, 0);
-  return conn == 8 ? launch_typed<T, 8, false, RS>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps)
-                   : launch_typed<T, 4, false, RS>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps);
+    return conn == 8 ? launch_typed<T, 8, true, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, 0, poll)
+                     : launch_typed<T, 4, true, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, 0, poll);
+  return conn == 8
+             ? launch_typed<T, 8, false, RS>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps, poll)
+             : launch_typed<T, 4, false, RS>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps, poll);
 }
 }  // namespace
 
 cudaError_t recon_launch_batch(int dtype, const Imgs& I, int ntiles, int conn, bool erode, bool ring, void* ws,
-                               cudaStream_t s, int max_visits, int max_iters, int resweeps) {
+                               cudaStream_t s, int max_visits, int max_iters, int resweeps, long long poll_limit) {
   switch (dtype) {
 #define NSGB_RECON_CASE(CODE, TYPE)                                                                           \
   case CODE:                                                                                                   \
     return resweeps > 0 ? dispatch_conn<TYPE, true>(I, ntiles, conn, erode, ring, ws, s, max_visits, max_iters,  \
-                                                    resweeps)                                                   \
+                                                    resweeps, poll_limit)                                       \
                         : dispatch_conn<TYPE, false>(I, ntiles, conn, erode, ring, ws, s, max_visits, max_iters, \
-                                                     resweeps);
+                                                     resweeps, poll_limit);
     NSGB_RECON_CASE(NSGB_U8, uint8_t)
     NSGB_RECON_CASE(NSGB_U16, uint16_t)
     NSGB_RECON_CASE(NSGB_I32, int32_t)
@@ -1003,7 +1017,7 @@ Img recon_image(int dtype, void* plane, const void* mask, int64_t H, int64_t W, 
 
 cudaError_t recon_launch(int dtype, void* out, const void* marker, const void* mask, int64_t H, int64_t W,
                          int64_t pitch, int conn, bool erode, bool ring, void* ws, cudaStream_t s, int max_visits,
-                         int max_iters) {
+                         int max_iters, long long poll_limit) {
   if (marker != out) {
     // The kernel works in place; start from a copy of the marker.
     const int esz = elem_size(dtype);
@@ -1014,7 +1028,7 @@ cudaError_t recon_launch(int dtype, void* out, const void* marker, const void* m
   I.n = 1;
   I.one = recon_image(dtype, out, mask, H, W, pitch);
   return recon_launch_batch(dtype, I, I.one.r_tiles_x * I.one.r_tiles_y, conn, erode, ring, ws, s, max_visits,
-                            max_iters);
+                            max_iters, 0, poll_limit);
 }
 
 }  // namespace nsgb

@@ -19,8 +19,10 @@ Img recon_image(int dtype, void* plane, const void* mask, int64_t H, int64_t W, 
 // mask) in one persistent launch over all their tiles.  resweeps: how often a tile marked
 // dirty while it ran is swept again at once from its registers (after a halo reload) instead
 // of being queued again -- worth it for front-like propagation such as hole filling.
+// poll_limit: polls of a queue wait before it reports NSGB_ERR_TIMEOUT (0 = kSpinLimit).
 cudaError_t recon_launch_batch(int dtype, const Imgs& I, int ntiles, int conn, bool erode, bool ring, void* ws,
-                               cudaStream_t s, int max_visits, int max_iters, int resweeps = 0);
+                               cudaStream_t s, int max_visits, int max_iters, int resweeps = 0,
+                               long long poll_limit = 0);
 
 // Workspace bytes for a reconstruction of an H x W image of `dtype`.
 size_t recon_workspace_bytes(int dtype, int64_t H, int64_t W);
@@ -32,6 +34,6 @@ size_t recon_workspace_bytes(int dtype, int64_t H, int64_t W);
 // (only meaningful for signed / float dilation).  Status words live at the start of `ws`.
 cudaError_t recon_launch(int dtype, void* out, const void* marker, const void* mask, int64_t H, int64_t W,
                          int64_t pitch, int conn, bool erode, bool ring, void* ws, cudaStream_t s, int max_visits,
-                         int max_iters);
+                         int max_iters, long long poll_limit = 0);
 
 }  // namespace nsgb

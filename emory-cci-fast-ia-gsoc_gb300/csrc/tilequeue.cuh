@@ -33,6 +33,7 @@ struct Ctl {
   unsigned long long* prof;         // [8] phase cycle counters (profiling builds only)
   unsigned cap;       // ring capacity (power of two >= ntiles)
   long long max_visits;
+  long long spin_limit;  // polls before a queue wait gives up (kSpinLimit unless overridden)
   int budget_step;
 };
 
@@ -47,7 +48,7 @@ __device__ __forceinline__ bool queue_push(const Ctl& c, int t) {
   Slot* sl = &c.slots[p & (c.cap - 1)];
   long long spins = 0;
   while (ld_acquire_u(&sl->seq) != p) {
-    if (++spins > kSpinLimit || ld_relaxed(c.status) != 0) {
+    if (++spins > c.spin_limit || ld_relaxed(c.status) != 0) {
       set_status(c.status, kDevTimeout);
       return false;
     }
@@ -76,7 +77,7 @@ __device__ __forceinline__ int queue_pop(const Ctl& c) {
     ++spins;
     if ((spins & 1) == 0 && ld_relaxed(c.done) != 0) return -1;
     if ((spins & 63) == 0 && ld_relaxed(c.status) != 0) return -1;
-    if (spins > kSpinLimit) {
+    if (spins > c.spin_limit) {
       set_status(c.status, kDevTimeout);
       return -1;
     }

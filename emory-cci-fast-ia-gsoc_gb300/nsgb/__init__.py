@@ -94,10 +94,12 @@ def _contig(t: torch.Tensor) -> torch.Tensor:
 
 
 def imreconstruct(seeds: torch.Tensor, image: torch.Tensor, connectivity: int, erode: bool = False,
-                  max_visits_per_tile: int = 0, max_visit_iters: int = 0) -> torch.Tensor:
+                  max_visits_per_tile: int = 0, max_visit_iters: int = 0, queue_poll_limit: int = 0) -> torch.Tensor:
     """nscale::imreconstruct<T>(seeds, image, connectivity) (MorphologicOperations.cpp:665-838) /
     nscale::gpu::imreconstruct<T> (MorphologicOperationsGPU.cpp:172-200): reconstruction by
-    dilation of `seeds` under `image`.  `erode=True` gives the dual (reconstruction by erosion)."""
+    dilation of `seeds` under `image`.  `erode=True` gives the dual (reconstruction by erosion).
+    The budgets (nsgb_opts) bound the device work: exceeding them raises NsgbError with
+    NSGB_ERR_NOT_CONVERGED (visits, sweeps) or NSGB_ERR_TIMEOUT (queue polls)."""
     _check_image(seeds, "seeds")
     _check_image(image, "image")
     _same_shape(seeds, image, "imreconstruct")
@@ -106,7 +108,7 @@ def imreconstruct(seeds: torch.Tensor, image: torch.Tensor, connectivity: int, e
     mask = _contig(image)
     rows, cols = out.shape
     ws, nb = _ws(_ffi.OP_IMRECONSTRUCT, dt, rows, cols, out.device)
-    opts = _ffi.Opts(1, max_visits_per_tile, max_visit_iters)
+    opts = _ffi.Opts(1, max_visits_per_tile, max_visit_iters, queue_poll_limit)
     st = lib.nsgb_imreconstruct(dt, out.data_ptr(), mask.data_ptr(), rows, cols, _pitch(out), connectivity,
                                 1 if erode else 0, ws, nb, _stream(), C.byref(opts))
     _ffi.check(st, "imreconstruct")

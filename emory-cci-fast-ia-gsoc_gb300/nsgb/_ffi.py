@@ -36,7 +36,8 @@ class NsgbError(RuntimeError):
 
 class Opts(C.Structure):
     _fields_ = [("sync", C.c_int), ("max_visits_per_tile", C.c_int), ("max_visit_iters", C.c_int),
-                ("reserved", C.c_int * 5), ("recon_event_begin", C.c_void_p), ("recon_event_end", C.c_void_p)]
+                ("queue_poll_limit", C.c_int), ("reserved", C.c_int * 4), ("recon_event_begin", C.c_void_p),
+                ("recon_event_end", C.c_void_p)]
 
 
 class Tile(C.Structure):
@@ -68,6 +69,7 @@ _SIGS = {
     "nsgb_device_status": (_int, [_vp, _vp]),
     "nsgb_imreconstruct": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _int, _int, _vp, _sz, _vp, _optp]),
     "nsgb_imreconstruct_noalloc": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _int, _int, _vp, _optp]),
+    "nsgb_noalloc_device_status": (_int, [_vp]),
     "nsgb_imreconstruct_binary": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _int, _vp, _sz, _vp, _optp]),
     "nsgb_imfill_holes": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _int, _int, _vp, _sz, _vp, _optp]),
     "nsgb_imhmin": (_int, [_int, _vp, _vp, _i64, _i64, _i64, _dbl, _int, _vp, _sz, _vp, _optp]),

@@ -196,16 +196,22 @@ inline void check(nsgb_status st, const char* where) {
   if (st != NSGB_OK) throw cv::Exception(-(int)st, std::string(where) + ": " + nsgb_status_string(st));
 }
 
-// Device workspace cached per device, grown on demand.
-inline void* workspace(size_t bytes) {
+// Device workspace cached per (device, stream) and grown on demand, so calls on different
+// streams never share one.  A buffer is replaced only after the device has finished all work
+// queued so far (cudaDeviceSynchronize), since a kernel of an earlier call may still use it.
+inline void* workspace(size_t bytes, cudaStream_t stream) {
   static std::mutex mu;
-  static std::map<int, std::pair<void*, size_t>> cache;
+  static std::map<std::pair<int, cudaStream_t>, std::pair<void*, size_t>> cache;
   std::lock_guard<std::mutex> lock(mu);
   int dev = 0;
-  cudaGetDevice(&dev);
-  auto& e = cache[dev];
+  if (cudaGetDevice(&dev) != cudaSuccess) throw cv::Exception(-217, "cudaGetDevice failed");
+  auto& e = cache[{dev, stream}];
   if (e.second < bytes) {
-    if (e.first) cudaFree(e.first);
+    if (e.first) {
+      if (cudaDeviceSynchronize() != cudaSuccess) throw cv::Exception(-217, "cudaDeviceSynchronize failed");
+      cudaFree(e.first);
+      e = {nullptr, 0};
+    }
     void* p = nullptr;
     if (cudaMalloc(&p, bytes) != cudaSuccess) throw cv::Exception(-217, "workspace cudaMalloc failed");
     e = {p, bytes};
@@ -214,6 +220,7 @@ inline void* workspace(size_t bytes) {
 }
 
 inline nsgb_stream_t raw(cv::gpu::Stream& s) { return (nsgb_stream_t)s.raw(); }
+inline void* workspace(size_t bytes, cv::gpu::Stream& s) { return workspace(bytes, (cudaStream_t)s.raw()); }
 
 }  // namespace detail
 
@@ -230,12 +237,15 @@ GpuMat imreconstruct(const GpuMat& seeds, const GpuMat& image, int connectivity,
   NSGB_CV_ASSERT(image.rows == seeds.rows && image.cols == seeds.cols);
   GpuMat out = seeds.clone();
   const size_t nb = nsgb_workspace_size(NSGB_OP_IMRECONSTRUCT, detail::DType<T>::code, image.rows, image.cols);
-  void* ws = detail::workspace(nb);
+  void* ws = detail::workspace(nb, stream);
   detail::check(nsgb_imreconstruct(detail::DType<T>::code, out.data, image.data, image.rows, image.cols,
                                    (int64_t)image.step, connectivity, 0, ws, nb, detail::raw(stream), nullptr),
                 "imreconstruct");
+  // the workspace header holds {status, visits}: read it on the call's stream
   int hdr[2] = {0, 0};
-  cudaMemcpy(hdr, ws, sizeof(hdr), cudaMemcpyDeviceToHost);
+  if (cudaMemcpyAsync(hdr, ws, sizeof(hdr), cudaMemcpyDeviceToHost, (cudaStream_t)stream.raw()) != cudaSuccess ||
+      cudaStreamSynchronize((cudaStream_t)stream.raw()) != cudaSuccess)
+    throw cv::Exception(-217, "imreconstruct: reading the visit count failed");
   iter = (unsigned)hdr[1];
   return out;
 }
@@ -254,10 +264,15 @@ GpuMat imreconstructQueue(const GpuMat& seeds, const GpuMat& image, int connecti
   return imreconstruct<T>(seeds, image, connectivity, stream);
 }
 template <typename T>
+GpuMat imreconstructBinary(const GpuMat& seeds, const GpuMat& binaryImage, int connectivity, Stream& stream);
+// binary = true is the reference's binary first pass (imreconstructBinaryCallerBuildQueue,
+// MorphologicOperationsGPU.cpp:319-323), which keeps the marker where the mask is 0 as
+// imreconstructBinary does: it maps to the binary reconstruction.
+template <typename T>
 GpuMat imreconstructQueueSpeedup(GpuMat& seeds, GpuMat& image, int connectivity, int /*nItFirstPass*/,
                                  Stream& stream, int /*nBlocks*/ = 14, bool binary = false) {
-  return binary ? imreconstruct<T>(seeds, image, connectivity, stream) : imreconstruct<T>(seeds, image, connectivity,
-                                                                                           stream);
+  if (binary) return imreconstructBinary<T>(seeds, image, connectivity, stream);
+  return imreconstruct<T>(seeds, image, connectivity, stream);
 }
 inline GpuMat imreconstructQueueSpeedupFloat(GpuMat& seeds, GpuMat& image, int connectivity, int /*nItFirstPass*/,
                                              Stream& stream, int /*nBlocks*/ = 14) {
@@ -287,7 +302,7 @@ std::vector<GpuMat> imreconstructQueueThroughput(std::vector<GpuMat>& seeds, std
   const size_t nb = nsgb_batch_workspace_size(detail::DType<T>::code, tiles.data(), (int)tiles.size());
   NSGB_CV_ASSERT(nb > 0);
   nsgb_batch batch;
-  detail::check(nsgb_batch_prepare(detail::DType<T>::code, tiles.data(), (int)tiles.size(), detail::workspace(nb), nb,
+  detail::check(nsgb_batch_prepare(detail::DType<T>::code, tiles.data(), (int)tiles.size(), detail::workspace(nb, stream), nb,
                                    &batch),
                 "imreconstructQueueThroughput");
   detail::check(nsgb_imreconstruct_batch(&batch, connectivity, 0, detail::raw(stream), nullptr),
@@ -305,7 +320,7 @@ GpuMat imreconstructBinary(const GpuMat& seeds, const GpuMat& binaryImage, int c
       nsgb_workspace_size(NSGB_OP_IMRECONSTRUCT_BINARY, detail::DType<T>::code, binaryImage.rows, binaryImage.cols);
   detail::check(nsgb_imreconstruct_binary(detail::DType<T>::code, out.data, binaryImage.data, binaryImage.rows,
                                           binaryImage.cols, (int64_t)binaryImage.step, connectivity,
-                                          detail::workspace(nb), nb, detail::raw(stream), nullptr),
+                                          detail::workspace(nb, stream), nb, detail::raw(stream), nullptr),
                 "imreconstructBinary");
   return out;
 }
@@ -323,7 +338,7 @@ GpuMat imfillHoles(const GpuMat& image, bool binary, int connectivity, Stream& s
   GpuMat out(image.rows, image.cols, image.type());
   const size_t nb = nsgb_workspace_size(NSGB_OP_FILL_HOLES, detail::DType<T>::code, image.rows, image.cols);
   detail::check(nsgb_imfill_holes(detail::DType<T>::code, image.data, out.data, image.rows, image.cols,
-                                  (int64_t)image.step, binary ? 1 : 0, connectivity, detail::workspace(nb), nb,
+                                  (int64_t)image.step, binary ? 1 : 0, connectivity, detail::workspace(nb, stream), nb,
                                   detail::raw(stream), nullptr),
                 "imfillHoles");
   return out;
@@ -337,7 +352,7 @@ GpuMat bwselect(const GpuMat& binaryImage, const GpuMat& seeds, int connectivity
   GpuMat out(binaryImage.rows, binaryImage.cols, binaryImage.type());
   const size_t nb = nsgb_workspace_size(NSGB_OP_BWSELECT, detail::DType<T>::code, binaryImage.rows, binaryImage.cols);
   detail::check(nsgb_bwselect(detail::DType<T>::code, binaryImage.data, seeds.data, out.data, binaryImage.rows,
-                              binaryImage.cols, (int64_t)binaryImage.step, connectivity, detail::workspace(nb), nb,
+                              binaryImage.cols, (int64_t)binaryImage.step, connectivity, detail::workspace(nb, stream), nb,
                               detail::raw(stream), nullptr),
                 "bwselect");
   return out;
@@ -350,7 +365,7 @@ inline GpuMat bwlabel(const GpuMat& binaryImage, int connectivity, bool relab, S
   const size_t nb = nsgb_workspace_size(NSGB_OP_BWLABEL, NSGB_U8, binaryImage.rows, binaryImage.cols);
   detail::check(nsgb_bwlabel(binaryImage.data, (int32_t*)out.data, binaryImage.rows, binaryImage.cols,
                              (int64_t)binaryImage.step, (int64_t)out.step, connectivity, relab ? 1 : 0, nullptr,
-                             detail::workspace(nb), nb, detail::raw(stream), nullptr),
+                             detail::workspace(nb, stream), nb, detail::raw(stream), nullptr),
                 "bwlabel");
   return out;
 }
@@ -366,7 +381,7 @@ inline GpuMat bwareaopen2(const GpuMat& binaryImage, bool labeled, bool flatten,
   detail::check(nsgb_bwareaopen(binaryImage.data, labeled ? 1 : 0, flatten ? nullptr : (int32_t*)out.data,
                                 flatten ? out.data : nullptr, binaryImage.rows, binaryImage.cols,
                                 (int64_t)binaryImage.step, (int64_t)out.step, (int64_t)out.step, minSize, maxSize,
-                                connectivity, &c, detail::workspace(nb), nb, detail::raw(stream), nullptr),
+                                connectivity, &c, detail::workspace(nb, stream), nb, detail::raw(stream), nullptr),
                 "bwareaopen2");
   count = c;
   return out;
@@ -389,7 +404,7 @@ inline int* boundingBox2(const int w, const int h, int* d_label, int bgval, int&
     throw cv::Exception(-217, "boundingBox2: cudaMalloc failed");
   int32_t c = 0;
   const nsgb_status st = nsgb_bounding_boxes(d_label, h, w, (int64_t)w * 4, bgval, tmp, cap, &c, nullptr,
-                                             detail::workspace(nb), nb, (nsgb_stream_t)stream, nullptr);
+                                             detail::workspace(nb, stream), nb, (nsgb_stream_t)stream, nullptr);
   if (st != NSGB_OK) {
     cudaFree(tmp);
     detail::check(st, "boundingBox2");
@@ -418,7 +433,7 @@ GpuMat imhmin(const GpuMat& image, T h, int connectivity, Stream& stream) {
   GpuMat out(image.rows, image.cols, image.type());
   const size_t nb = nsgb_workspace_size(NSGB_OP_HMIN, detail::DType<T>::code, image.rows, image.cols);
   detail::check(nsgb_imhmin(detail::DType<T>::code, image.data, out.data, image.rows, image.cols, (int64_t)image.step,
-                            (double)h, connectivity, detail::workspace(nb), nb, detail::raw(stream), nullptr),
+                            (double)h, connectivity, detail::workspace(nb, stream), nb, detail::raw(stream), nullptr),
                 "imhmin");
   return out;
 }
@@ -437,7 +452,7 @@ GpuMat morphOpen(const GpuMat& image, const cv::Mat& kernel, Stream& stream) {
   GpuMat out(image.rows, image.cols, image.type());
   const size_t nb = nsgb_workspace_size(NSGB_OP_MORPH_OPEN, NSGB_U8, image.rows, image.cols);
   detail::check(nsgb_morph_open(image.data, out.data, image.rows, image.cols, (int64_t)image.step,
-                                (int64_t)out.step, k.data(), kernel.rows, detail::workspace(nb), nb,
+                                (int64_t)out.step, k.data(), kernel.rows, detail::workspace(nb, stream), nb,
                                 detail::raw(stream), nullptr),
                 "morphOpen");
   return out;
@@ -454,7 +469,7 @@ inline GpuMat distanceTransform(const GpuMat& mask, Stream& stream, bool calcDis
   GpuMat out(mask.rows, mask.cols, CV_32FC1);
   const size_t nb = nsgb_workspace_size(NSGB_OP_DISTANCE, NSGB_U8, mask.rows, mask.cols);
   detail::check(nsgb_distance_transform(mask.data, (float*)out.data, mask.rows, mask.cols, (int64_t)mask.step,
-                                        (int64_t)out.step, 0, detail::workspace(nb), nb, detail::raw(stream), nullptr),
+                                        (int64_t)out.step, 0, detail::workspace(nb, stream), nb, detail::raw(stream), nullptr),
                 "distanceTransform");
   return out;
 }

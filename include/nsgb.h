@@ -60,7 +60,10 @@ typedef struct {
   int max_visits_per_tile; /* reconstruction: cap on tile visits, in units of the number of
                              tiles (0 = default, effectively unbounded) */
   int max_visit_iters; /* reconstruction: cap on row/column sweeps per tile visit (0 = default) */
-  int reserved[5];
+  int queue_poll_limit; /* reconstruction: polls a warp makes on the tile queue before it gives
+                           up with NSGB_ERR_TIMEOUT (0 = default, about 2 s of polling); a small
+                           value makes an idle warp's wait run out, for testing that path */
+  int reserved[4];
   /* Optional CUDA events (cudaEvent_t) recorded on the call's stream immediately before and
    * after the reconstruction kernel (nsgb_imreconstruct, nsgb_chain), for timing it alone. */
   void* recon_event_begin;
@@ -296,15 +299,24 @@ nsgb_status nsgb_imreconstruct_batch(const nsgb_batch* batch, int conn, int erod
  * scratch is a fixed NSGB_NOALLOC_SCRATCH_BYTES array in the library's own device memory,
  * held by every GPU that loads the library until the process exits.
  *   - Larger images are refused with NSGB_ERR_WORKSPACE before any GPU work.
- *   - The first call on a device looks up the scratch's device address for that device
- *     (cudaGetSymbolAddress, with that device current); make that first call before any
- *     stream capture.
+ *   - Each call outside stream capture looks up the scratch's device address on the current
+ *     device (cudaGetSymbolAddress), so a device reset or a re-created context is followed; a
+ *     call made while its stream is capturing uses the address of the last call outside
+ *     capture on that device.  Make one call on each device before any stream capture.
  *   - It calls no cudaMalloc / cudaFree and no allocating library routine.
  *   - All calls share the one scratch array and each call re-initialises it; calls whose work
- *     overlaps on the GPU (other streams or host threads) race on it, so serialise them. */
+ *     overlaps on the GPU (other streams or host threads) race on it, so serialise them.
+ *   - With opts->sync == 0 the call returns once its work is enqueued; its device status
+ *     (NOT_CONVERGED, TIMEOUT) is then read with nsgb_noalloc_device_status before the next
+ *     call starts, which resets it. */
 nsgb_status nsgb_imreconstruct_noalloc(int dtype, void* marker, const void* mask, int64_t rows,
                                        int64_t cols, int64_t pitch, int conn, int erode,
                                        nsgb_stream_t stream, const nsgb_opts* opts);
+/* No counterpart in the reference: waits for the work on `stream` and returns the device
+ * status of the last nsgb_imreconstruct_noalloc call on the current device (NSGB_OK,
+ * NSGB_ERR_NOT_CONVERGED, NSGB_ERR_TIMEOUT), read from the built-in scratch.  Allocates
+ * nothing. */
+nsgb_status nsgb_noalloc_device_status(nsgb_stream_t stream);
 
 /* ---------------------------------------------------------------------------------------
  * Differentiable float32 reconstruction by dilation.  No counterpart in the reference (its

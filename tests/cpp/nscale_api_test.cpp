@@ -65,6 +65,21 @@ int main(int argc, char** argv) {
   batch[1].download(b1);
   save(dir, "batch0.u8", b0);
   save(dir, "batch1.u8", b1);
+  // the queue variant (MorphologicOperations.h:105-116): grayscale, and binary (the binary
+  // reconstruction of the dark objects from a few seed pixels)
+  cv::gpu::GpuMat gsp = nscale::gpu::imreconstructQueueSpeedup<unsigned char>(gmarker, gmask, 8, 1, stream);
+  cv::Mat sp;
+  gsp.download(sp);
+  save(dir, "speedup8.u8", sp);
+  cv::Mat bseed(H, W, CV_8UC1);
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) bseed.ptr<unsigned char>(y)[x] = ((x * 7 + y * 13) % 97 == 0) ? 255 : 0;
+  cv::gpu::GpuMat gbseed(bseed), gbin(bin_mask);
+  cv::gpu::GpuMat gspb = nscale::gpu::imreconstructQueueSpeedup<unsigned char>(gbseed, gbin, 8, 1, stream, 14, true);
+  cv::Mat spb;
+  gspb.download(spb);
+  save(dir, "speedup_bin8.u8", spb);
+  save(dir, "bseed.u8", bseed);
 
   // per-label bounding boxes of the raster labels (cuda/ccl_uf.cuh:16), device in / device out
   int* d_lab = nullptr;

@@ -71,6 +71,11 @@ def test_argument_errors_need_no_gpu():
     assert lib.nsgb_imreconstruct(0, 1, 1, 4, 4, 3, 8, 0, 1, 1 << 20, None, None) == 1
     assert lib.nsgb_imreconstruct(0, 1, 1, 4, 4, 4, 8, 0, None, 0, None, None) == 3
     assert lib.nsgb_bwlabel(None, 1, 4, 4, 4, 16, 8, 1, None, 1, 1 << 20, None, None) == 1
+    # the allocation-free entry point checks arguments like the others: a product of dimensions
+    # that wraps in 64 bits, a pitch below the row and a bad connectivity are refused
+    assert lib.nsgb_imreconstruct_noalloc(0, 1, 1, 1 << 37, 1 << 27, 1 << 27, 8, 0, None, None) == 1
+    assert lib.nsgb_imreconstruct_noalloc(0, 1, 1, 4, 4, 3, 8, 0, None, None) == 1
+    assert lib.nsgb_imreconstruct_noalloc(0, 1, 1, 4, 4, 4, 5, 0, None, None) == 1
     assert lib.nsgb_imhmin(2, 1, 2, 4, 4, 16, 1.0, 8, 1, 1 << 20, None, None) == 2
     # bounding boxes: null labels, pitch below the row, capacity without an output buffer
     assert lib.nsgb_bounding_boxes(None, 4, 4, 16, 0, 1, 4, None, None, 1, 1 << 20, None, None) == 1

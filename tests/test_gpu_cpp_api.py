@@ -28,6 +28,10 @@ def test_cpp_api_matches_oracle(nsgb, oracle, tmp_path):
     assert np.array_equal(load("recon4.u8", np.uint8), oracle.imreconstruct(marker, mask, 4))
     assert np.array_equal(load("batch0.u8", np.uint8), rec8)
     assert np.array_equal(load("batch1.u8", np.uint8), rec8)
+    assert np.array_equal(load("speedup8.u8", np.uint8), rec8)
+    bin_dark = np.where(mask < 128, 255, 0).astype(np.uint8)
+    assert np.array_equal(load("speedup_bin8.u8", np.uint8),
+                          oracle.imreconstruct_binary(load("bseed.u8", np.uint8), bin_dark, 8))
     fill = oracle.imfill_holes(oracle.threshold_gt(rec8, 128.0), True, 4)
     assert np.array_equal(load("fill4.u8", np.uint8), fill)
     lab, _ = oracle.bwlabel2(fill, 8, True)

@@ -351,3 +351,18 @@ def test_device_budgets_report_status(nsgb):
     assert e.value.status == 4
     out = nsgb.imreconstruct(to_dev(marker), to_dev(mask), 8)  # still works afterwards
     assert out.shape == mask.shape
+
+
+def test_queue_wait_timeout_reports_status(nsgb, oracle):
+    """Failure detection of the queue waits without a fault: with a poll limit of a few polls,
+    warps that wait for work on the tile queue (most of the grid, on a 128-tile image) give up
+    and the call returns NSGB_ERR_TIMEOUT through the status word; the context stays usable and
+    the next call with the default limit is bit-exact."""
+    from nsgb import synth
+
+    mask, marker = synth.tile_u8(512, 512, 60, 2)
+    with pytest.raises(nsgb.NsgbError) as e:
+        nsgb.imreconstruct(to_dev(marker), to_dev(mask), 8, queue_poll_limit=2)
+    assert e.value.status == 5
+    out = nsgb.imreconstruct(to_dev(marker), to_dev(mask), 8)
+    assert np.array_equal(to_np(out), oracle.imreconstruct(marker, mask, 8))

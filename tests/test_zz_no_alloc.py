@@ -63,3 +63,25 @@ def test_noalloc_refuses_images_beyond_its_scratch(nsgb):
     assert _ffi.lib.nsgb_workspace_size(_ffi.OP_IMRECONSTRUCT, 0, 16384, 16384) > _ffi.NOALLOC_SCRATCH_BYTES
     st = _ffi.lib.nsgb_imreconstruct_noalloc(0, 256, 256, 16384, 16384, 16384, 8, 0, None, None)
     assert st == 3  # NSGB_ERR_WORKSPACE
+
+
+def test_noalloc_async_status_is_read_back(nsgb):
+    """With opts->sync == 0 the call returns once enqueued; its device status is read from the
+    built-in scratch with nsgb_noalloc_device_status.  A one-sweep budget on an input that needs
+    more ends NOT_CONVERGED there; the next call, with the default budget, is bit-exact against
+    the workspace entry point."""
+    import torch
+    from nsgb import _ffi, synth
+
+    mask, marker = synth.tile_u8(512, 512, 60, 2)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    out = torch.from_numpy(marker).cuda()
+    m = torch.from_numpy(mask).cuda()
+    opts = _ffi.Opts(0, 0, 1)  # sync = 0, max_visit_iters = 1
+    st = _ffi.lib.nsgb_imreconstruct_noalloc(0, out.data_ptr(), m.data_ptr(), 512, 512, 512, 8, 0, stream,
+                                             C.byref(opts))
+    assert st == 0
+    assert _ffi.lib.nsgb_noalloc_device_status(stream) == 4  # NSGB_ERR_NOT_CONVERGED
+    ref, got = _both(nsgb, marker, mask, 8)
+    assert np.array_equal(got, ref)
+    assert _ffi.lib.nsgb_noalloc_device_status(stream) == 0
