@@ -16,9 +16,16 @@
 // (2) per row, D^2(x) = min over x' of (x - x')^2 + g(x')^2, one CTA per row: each pixel
 //     searches outward along the row and stops once the column offset alone reaches its best
 //     squared distance (at most g(x) columns each way), which is cheap while the row's mean g is
-//     small (objects of tens of pixels); a row with a large mean g is instead done by one thread
-//     with the lower envelope of the parabolas, in integer arithmetic (the breakpoint between
-//     two parabolas is a floor division), its stacks in the workspace.  Both are exact.
+//     small (objects of tens of pixels).  A row with a large mean g (far from every zero pixel,
+//     or crossing columns without one) is done by the whole CTA by divide and conquer: the
+//     matrix (x - i)^2 + g(i)^2 is Monge, so the leftmost minimising column A(x) never
+//     decreases with x, and the row minimum at the midpoint of two computed positions a < b
+//     only needs the columns A(a) .. A(b).  Level by level (log2 W levels) every position's
+//     candidate columns are laid end to end and split evenly over the threads, each keeping
+//     one running minimum per position it touches (64-bit keys: D^2 above the column, so
+//     atomicMin keeps the leftmost minimum).  Rows wider than the shared-memory tables
+//     (12288 columns) fall back to the lower envelope of the parabolas (Meijster) on one
+//     thread.  All three are exact integer arithmetic.
 // Output: the distance (float), or the basins of the watershed step (HistologicalEntities.cpp:
 // 347-356): -distance on mask pixels, -FLT_MAX elsewhere.  No zero pixel at all: +inf.
 #include <cfloat>
@@ -139,18 +146,125 @@ __device__ void envelope_row(const int* __restrict__ gr, int* s, int* t, float* 
   }
 }
 
+constexpr int kRowThreads = 256;
+// A row whose mean g exceeds this takes the divide and conquer instead of the per-pixel search.
+constexpr int64_t kMeanG = 32;
+// Widest row for the divide and conquer's shared-memory tables (8 bytes per column).
+constexpr int kDcMaxW = 12288;
+
+__device__ __forceinline__ int dc_levels(int W) {
+  int L = 1;
+  while ((1 << L) < W + 1) ++L;
+  return L;
+}
+
+// Exclusive prefix sum of a[0 .. n) in place by the whole CTA; returns the total.
+__device__ int block_exclusive_scan(int* a, int n) {
+  __shared__ int s_warp[kRowThreads / 32];
+  __shared__ int s_total;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int per = (n + kRowThreads - 1) / kRowThreads;
+  const int b = min(n, tid * per), e = min(n, b + per);
+  int sum = 0;
+  for (int k = b; k < e; ++k) sum += a[k];
+  int incl = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(NSGB_FULL, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) s_warp[wid] = incl;
+  __syncthreads();
+  int base = 0;
+  for (int w = 0; w < wid; ++w) base += s_warp[w];
+  if (tid == kRowThreads - 1) s_total = base + incl;
+  int run = base + incl - sum;
+  for (int k = b; k < e; ++k) {
+    const int v = a[k];
+    a[k] = run;
+    run += v;
+  }
+  __syncthreads();
+  return s_total;
+}
+
+// Divide and conquer over the row (see the file comment).  Level l computes the positions
+// x = (2k + 1) h - 1, h = 2^(L-1-l), whose neighbours x - h and x + h were computed before (or
+// lie outside the row: A = 0 on the left, W - 1 on the right).  Shared memory: A (u16 per
+// column), the level's keys (u64 per position) and candidate offsets (int per position + 1).
+template <bool BASINS>
+__device__ void dc_row(const int* __restrict__ gr, float* o, const uint8_t* mrow, int W, int64_t inf2,
+                       unsigned char* smem) {
+  uint16_t* A = (uint16_t*)smem;
+  const int max_nodes = W / 2 + 1;
+  unsigned long long* key = (unsigned long long*)(smem + (((size_t)W * 2 + 15) & ~(size_t)15));
+  int* off = (int*)(key + max_nodes);
+  const int L = dc_levels(W);
+  const int tid = threadIdx.x;
+  for (int l = 0; l < L; ++l) {
+    const int h = 1 << (L - 1 - l);
+    const int n = (W / h + 1) / 2;  // positions of this level inside the row
+    for (int k = tid; k < n; k += kRowThreads) {
+      const int x = (2 * k + 1) * h - 1;
+      const int lo = x - h < 0 ? 0 : A[x - h];
+      const int hi = x + h >= W ? W - 1 : A[x + h];
+      off[k] = hi - lo + 1;
+      key[k] = ~0ull;
+    }
+    __syncthreads();
+    const int total = block_exclusive_scan(off, n);
+    if (tid == 0) off[n] = total;
+    __syncthreads();
+    const int chunk = (total + kRowThreads - 1) / kRowThreads;
+    int j = tid * chunk;
+    const int end = min(total, j + chunk);
+    if (j < end) {
+      // the position holding candidate j: the last k with off[k] <= j
+      int a = 0, b = n - 1;
+      while (a < b) {
+        const int m = (a + b + 1) >> 1;
+        if (off[m] <= j) a = m;
+        else b = m - 1;
+      }
+      int k = a;
+      while (j < end) {
+        const int x = (2 * k + 1) * h - 1;
+        const int lo = x - h < 0 ? 0 : A[x - h];
+        const int stop = min(end, off[k + 1]);
+        unsigned long long best = ~0ull;
+        for (; j < stop; ++j) {
+          const int i = lo + (j - off[k]);
+          const unsigned long long d2 = (unsigned long long)(sq((int64_t)x - i) + sq(__ldg(gr + i)));
+          const unsigned long long kk = (d2 << 24) | (unsigned long long)i;
+          best = kk < best ? kk : best;
+        }
+        atomicMin(&key[k], best);
+        ++k;
+      }
+    }
+    __syncthreads();
+    for (int k = tid; k < n; k += kRowThreads) {
+      const int x = (2 * k + 1) * h - 1;
+      const unsigned long long kk = key[k];
+      A[x] = (uint16_t)(kk & 0xFFFFFFull);
+      store_px<BASINS>(o, mrow, x, (int64_t)(kk >> 24), inf2);
+    }
+    __syncthreads();
+  }
+}
+
 // One CTA per row.  D(x) <= g(x), so a pixel's search along the row stops after at most g(x)
 // columns each way (once k^2 reaches the best squared distance so far); when the row's g sum
-// keeps that work small (mean g <= kMeanG) all threads search their pixels, otherwise one thread
-// builds the row's envelope (rows far from every zero pixel, or in columns without one).
-constexpr int kRowThreads = 256;
-constexpr int64_t kMeanG = 256;
+// keeps that work small (mean g <= kMeanG) all threads search their pixels, otherwise the CTA
+// runs the divide and conquer (`dc`: the row fits the shared tables and its squared distances
+// fit the 40-bit keys), or one thread builds the row's lower envelope.
 
 template <bool BASINS>
 __global__ void __launch_bounds__(kRowThreads) edt_rows(const uint8_t* __restrict__ mask, int64_t pitch_in,
                                                         const int* __restrict__ g, int* __restrict__ stack_s,
                                                         int* __restrict__ stack_t, float* __restrict__ out,
-                                                        int64_t pitch_out, int H, int W) {
+                                                        int64_t pitch_out, int H, int W, bool dc) {
+  extern __shared__ __align__(16) unsigned char dc_smem[];
   __shared__ long long s_sum[kRowThreads / 32];
   const int64_t inf2 = sq((int64_t)H + W);
   for (int y = blockIdx.x; y < H; y += gridDim.x) {
@@ -175,6 +289,8 @@ __global__ void __launch_bounds__(kRowThreads) edt_rows(const uint8_t* __restric
         }
         store_px<BASINS>(o, mrow, x, best, inf2);
       }
+    } else if (dc) {
+      dc_row<BASINS>(gr, o, mrow, W, inf2, dc_smem);
     } else if (threadIdx.x == 0) {
       envelope_row<BASINS>(gr, stack_s + (int64_t)y * W, stack_t + (int64_t)y * W, o, mrow, W, inf2);
     }
@@ -205,10 +321,22 @@ cudaError_t edt_launch(const uint8_t* mask, int64_t pitch_in, float* out, int64_
   edt_chunk_zeros<<<cgrid, kThreads, 0, s>>>(mask, pitch_in, rows, cols, first0, last0);
   edt_columns<<<cgrid, kThreads, 0, s>>>(mask, pitch_in, rows, cols, first0, last0, g);
   const int rblocks = rows < (1 << 20) ? rows : (1 << 20);
-  if (basins)
-    edt_rows<true><<<rblocks, kRowThreads, 0, s>>>(mask, pitch_in, g, st_s, st_t, out, pitch_out, rows, cols);
-  else
-    edt_rows<false><<<rblocks, kRowThreads, 0, s>>>(mask, pitch_in, g, st_s, st_t, out, pitch_out, rows, cols);
+  // divide and conquer: tables fit (u16 columns, 24-bit column field) and 2 (H + W)^2 < 2^40
+  const bool dc = cols <= kDcMaxW && (int64_t)rows + cols < (1 << 19);
+  const size_t smem = dc ? (((size_t)cols * 2 + 15) & ~(size_t)15) + (size_t)(cols / 2 + 1) * 8 +
+                               (size_t)(cols / 2 + 2) * 4
+                         : 0;
+  cudaError_t e = cudaSuccess;
+  if (basins) {
+    if (smem > 48 * 1024) e = cudaFuncSetAttribute(edt_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      edt_rows<true><<<rblocks, kRowThreads, smem, s>>>(mask, pitch_in, g, st_s, st_t, out, pitch_out, rows, cols, dc);
+  } else {
+    if (smem > 48 * 1024) e = cudaFuncSetAttribute(edt_rows<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      edt_rows<false><<<rblocks, kRowThreads, smem, s>>>(mask, pitch_in, g, st_s, st_t, out, pitch_out, rows, cols, dc);
+  }
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 

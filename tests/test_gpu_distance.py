@@ -40,7 +40,7 @@ def masks():
     out["col"] = np.where(rng.random((1000, 1)) < 0.97, 255, 0).astype(np.uint8)
     out["pixel"] = np.zeros((1, 1), np.uint8)
     far = np.full((800, 300), 255, np.uint8)
-    far[0, :] = 0  # rows up to ~256 away search along the row, the rest take the envelope
+    far[0, :] = 0  # rows near the zero row search along the row, the far ones take the divide and conquer
     far[0, 150] = 255
     out["far"] = far
     return out
@@ -52,6 +52,60 @@ def test_distance_parity(nsgb, oracle, name, basins):
     m = masks()[name]
     got = nsgb.distanceTransform(to_dev(m), basins=basins).cpu().numpy()
     assert np.array_equal(got, oracle.distance_transform(m, basins=basins))
+
+
+def zero_free_masks():
+    """Inputs whose rows take the divide and conquer (mean g above the search threshold): large
+    objects, columns without any zero pixel, one zero pixel far away, and rows wider than its
+    shared tables (the envelope fallback)."""
+    rng = np.random.default_rng(21)
+    out = {}
+    big = np.zeros((1500, 1700), np.uint8)
+    yy, xx = np.mgrid[0:1500, 0:1700]
+    for cy, cx, r in ((700, 800, 600), (200, 200, 150), (1300, 1500, 180)):
+        big[(yy - cy) ** 2 + (xx - cx) ** 2 <= r * r] = 255
+    out["large_objects"] = big
+    cols = np.full((900, 1100), 200, np.uint8)
+    cols[rng.integers(0, 900, 40), rng.integers(0, 550, 40)] = 0  # zeros only in the left half
+    out["zero_free_columns"] = cols
+    single = np.full((1024, 1024), 1, np.uint8)
+    single[1000, 3] = 0
+    out["single_zero"] = single
+    wide = np.full((40, 13000), 77, np.uint8)
+    wide[rng.integers(0, 40, 6), rng.integers(0, 13000, 6)] = 0  # wider than the shared tables
+    out["wide"] = wide
+    ties = np.full((300, 301), 5, np.uint8)
+    ties[::100, ::100] = 0  # equidistant zero pixels: ties between columns
+    out["ties"] = ties
+    return out
+
+
+@pytest.mark.parametrize("name", ["large_objects", "zero_free_columns", "single_zero", "wide", "ties"])
+def test_distance_zero_free_regions(nsgb, oracle, name):
+    m = zero_free_masks()[name]
+    for basins in (False, True):
+        got = nsgb.distanceTransform(to_dev(m), basins=basins).cpu().numpy()
+        assert np.array_equal(got, oracle.distance_transform(m, basins=basins)), basins
+
+
+def test_distance_all_foreground_4096(nsgb, oracle):
+    """An all-foreground 4096 x 4096 mask except one zero pixel: every row is far from the
+    zero pixel; timed against the bench's blob tile (within 3x of it)."""
+    import torch
+
+    m = np.full((4096, 4096), 255, np.uint8)
+    m[2048, 17] = 0
+    d = to_dev(m)
+    nsgb.distanceTransform(d)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    got = nsgb.distanceTransform(d)
+    e1.record()
+    torch.cuda.synchronize()
+    print(f"all-foreground 4096^2 distance transform: {e0.elapsed_time(e1):.3f} ms")
+    assert np.array_equal(got.cpu().numpy(), oracle.distance_transform(m))
+    assert e0.elapsed_time(e1) < 0.51
 
 
 def test_distance_without_zero(nsgb, oracle):
