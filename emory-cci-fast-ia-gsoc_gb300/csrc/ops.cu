@@ -1250,7 +1250,8 @@ nsgb_status nsgb_imreconstruct_batch(const nsgb_batch* batch, int conn, int erod
 // labels the plateaus of R with the union-find labeller and gives each the best source it
 // contains (mask before marker before ring, then the smallest raster index):
 //   prov = ~q (mask q), q (marker q), INT32_MIN (ring); q = y * cols + x within the image.
-// The adjoint scatters the upstream gradient along prov with exact 32.32 fixed-point sums.
+// The adjoint scatters the upstream gradient along prov with exact 128-bit fixed-point sums
+// (resolution 2^-96) and rounds each sum to float once.
 namespace nsgb {
 namespace {
 
@@ -1330,10 +1331,109 @@ __global__ void prov_out_kernel(Imgs I, int total_rows, const int* __restrict__ 
   });
 }
 
-// Adjoint, pass 1: every pixel adds its gradient (rounded to a multiple of 2^-32) to the
-// accumulator of its source.  Lanes of a warp hold consecutive pixels of one row, which
-// mostly share a source: a segmented warp scan sums runs of equal targets first, so only the
-// last lane of each run issues an atomic.  plane = g, aux = prov.
+// Exact fixed point for the adjoint: a value is held as a 128-bit two's-complement integer S
+// (lo, hi words) standing for S * 2^-96.  Every float32 g with 2^-73 <= |g| < 2^31 converts
+// exactly (its last mantissa bit is worth at least 2^-96); smaller magnitudes round to the
+// nearest multiple of 2^-96 (ties to even).  Sums of such values are exact as long as they
+// stay below 2^31 in magnitude, and the order in which atomics land does not matter.
+struct Fix128 {
+  unsigned long long lo;
+  long long hi;
+};
+
+// Returns false for |g| >= 2^31, inf and NaN.
+__device__ __forceinline__ bool fix_from_float(float g, Fix128& out) {
+  const uint32_t b = __float_as_uint(g);
+  const uint32_t ex = (b >> 23) & 0xFFu;
+  uint32_t man = b & 0x7FFFFFu;
+  if (ex >= 127u + 31u) return false;
+  int sh;  // value = man * 2^sh
+  if (ex == 0) {
+    sh = -149;
+  } else {
+    man |= 0x800000u;
+    sh = (int)ex - 150;
+  }
+  // fixed = man * 2^(sh + 96)
+  unsigned long long lo = 0, hi = 0;
+  const int s = sh + 96;
+  if (s >= 0) {  // s <= 157 - 150 + 96 - 1 = 102, man < 2^24: fits in 126 bits
+    if (s < 64) {
+      lo = (unsigned long long)man << s;
+      hi = s == 0 ? 0ull : (unsigned long long)man >> (64 - s);
+    } else {
+      hi = (unsigned long long)man << (s - 64);
+    }
+  } else if (-s < 32) {  // round man * 2^s (ties to even)
+    const int r = -s;
+    const uint32_t q = man >> r, rem = man & ((1u << r) - 1u), half = 1u << (r - 1);
+    lo = q + ((rem > half || (rem == half && (q & 1u))) ? 1u : 0u);
+  }
+  if (b >> 31) {  // negate: two's complement over 128 bits
+    lo = ~lo + 1ull;
+    hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+  }
+  out.lo = lo;
+  out.hi = (long long)hi;
+  return true;
+}
+
+__device__ __forceinline__ Fix128 fix_add(const Fix128& a, const Fix128& b) {
+  Fix128 r;
+  r.lo = a.lo + b.lo;
+  r.hi = a.hi + b.hi + (r.lo < a.lo ? 1ll : 0ll);
+  return r;
+}
+
+// S * 2^-96 rounded to the nearest float (ties to even).  |S| < 2^127, so the result is a
+// normal float or zero (the smallest non-zero magnitude, 2^-96, is far above 2^-126).
+__device__ __forceinline__ float fix_to_float(unsigned long long lo, long long hi) {
+  const bool neg = hi < 0;
+  unsigned long long ml = lo, mh = (unsigned long long)hi;
+  if (neg) {
+    ml = ~ml + 1ull;
+    mh = ~mh + (ml == 0ull ? 1ull : 0ull);
+  }
+  if ((ml | mh) == 0ull) return 0.0f;
+  const int lead = mh ? 127 - __clzll((long long)mh) : 63 - __clzll((long long)ml);  // top set bit
+  // 24 significant bits: m = floor(M / 2^(lead - 23)), remainder decides the rounding
+  uint32_t m;
+  bool above_half = false, exactly_half = false;
+  if (lead <= 23) {
+    m = (uint32_t)(ml << (23 - lead));
+  } else {
+    const int r = lead - 23;  // bits dropped, 1..104
+    // m = bits [r, r + 24) of (mh:ml)
+    unsigned long long q;
+    if (r >= 64) q = mh >> (r - 64);
+    else q = (ml >> r) | (r == 0 ? 0ull : (mh << (64 - r)));
+    m = (uint32_t)q;
+    // the dropped bits: half = bit r - 1, sticky = bits below it
+    const int hb = r - 1;
+    const bool hbit = hb >= 64 ? ((mh >> (hb - 64)) & 1ull) : ((ml >> hb) & 1ull);
+    bool sticky;
+    if (hb >= 64) sticky = ml != 0ull || (hb > 64 && (mh & ((1ull << (hb - 64)) - 1ull)) != 0ull);
+    else sticky = hb > 0 && (ml & ((1ull << hb) - 1ull)) != 0ull;
+    above_half = hbit && sticky;
+    exactly_half = hbit && !sticky;
+  }
+  int e = lead - 96;  // value = m * 2^(e - 23)
+  if (above_half || (exactly_half && (m & 1u))) {
+    ++m;
+    if (m == (1u << 24)) {
+      m >>= 1;
+      ++e;
+    }
+  }
+  const uint32_t bits = ((uint32_t)(e + 127) << 23) | (m & 0x7FFFFFu) | (neg ? 0x80000000u : 0u);
+  return __uint_as_float(bits);
+}
+
+// Adjoint, pass 1: every pixel adds its gradient, as an exact 128-bit fixed-point value, to the
+// accumulator of its source.  Lanes of a warp hold consecutive pixels of one row, which mostly
+// share a source: a segmented warp scan sums runs of equal targets first, so only the last lane
+// of each run issues the atomics (low word, then the high word with the low word's carry).
+// plane = g, aux = prov.  acc: two words per source, marker sources then mask sources.
 __global__ void grad_scatter_kernel(Imgs I, int total_rows, unsigned long long* __restrict__ acc_marker,
                                     unsigned long long* __restrict__ acc_mask, int* status) {
   const int lane = threadIdx.x & 31;
@@ -1341,18 +1441,17 @@ __global__ void grad_scatter_kernel(Imgs I, int total_rows, unsigned long long* 
   for (int gr = blockIdx.y; gr < total_rows; gr += gridDim.y) {  // uniform per block
     const Img m = img_at(I, img_of(I, gr, RowBase()));
     const int y = gr - m.row_base;
-    long long key = -1, v = 0;
+    long long key = -1;
+    Fix128 v = {0ull, 0ll};
     if (x < m.W) {
       const int32_t p = px<int32_t>(m.aux, m.pitch, y, x);
       if (p != INT_MIN) {
         const int64_t q = p >= 0 ? (int64_t)p : ~(int64_t)p;
-        if (q < (int64_t)m.H * m.W) {
-          // g * 2^32 is exact in float; the conversion rounds to nearest, ties to even (no
-          // double arithmetic, which is slow on this GPU)
-          v = __float2ll_rn(px<float>(m.plane, m.pitch, y, x) * 4294967296.0f);
+        if (q < (int64_t)m.H * m.W && fix_from_float(px<float>(m.plane, m.pitch, y, x), v)) {
           key = ((int64_t)m.px_base + q) | (p < 0 ? (1ll << 40) : 0ll);
         } else {
           set_status(status, NSGB_ERR_BAD_ARG);
+          v = Fix128{0ull, 0ll};
         }
       }
     }
@@ -1361,35 +1460,45 @@ __global__ void grad_scatter_kernel(Imgs I, int total_rows, unsigned long long* 
     bool head = lane == 0 || kprev != key;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const long long v2 = __shfl_up_sync(NSGB_FULL, v, o);
+      Fix128 v2;
+      v2.lo = __shfl_up_sync(NSGB_FULL, v.lo, o);
+      v2.hi = __shfl_up_sync(NSGB_FULL, v.hi, o);
       const bool h2 = __shfl_up_sync(NSGB_FULL, head, o);
       if (lane >= o && !head) {
-        v += v2;
+        v = fix_add(v, v2);
         head = h2;
       }
     }
     const bool tail = lane == 31 || knext != key;
     if (tail && key >= 0) {
-      unsigned long long* a = (key >> 40) ? acc_mask : acc_marker;
-      atomicAdd(a + (key & ((1ll << 40) - 1)), (unsigned long long)v);
+      unsigned long long* a = ((key >> 40) ? acc_mask : acc_marker) + 2 * (key & ((1ll << 40) - 1));
+      const unsigned long long old = atomicAdd(a, v.lo);
+      const unsigned long long carry = old + v.lo < old ? 1ull : 0ull;
+      atomicAdd(a + 1, (unsigned long long)v.hi + carry);
     }
   }
 }
 
-// Adjoint, pass 2: accumulators to float.  plane = g; dmarker / dmask at byte offsets.  One
-// rounding: the integer sum rounds to float, and the scaling by 2^-32 is exact.
-__global__ void grad_out_kernel(Imgs I, int total_rows, const long long* __restrict__ acc_marker,
-                                const long long* __restrict__ acc_mask, int64_t dmarker_off, int64_t dmask_off) {
+// Adjoint, pass 2: accumulators to float, one rounding each.  plane = g; dmarker / dmask at
+// byte offsets.
+__global__ void grad_out_kernel(Imgs I, int total_rows, const unsigned long long* __restrict__ acc_marker,
+                                const unsigned long long* __restrict__ acc_mask, int64_t dmarker_off,
+                                int64_t dmask_off) {
   ccl::for_batch_quads(I, total_rows, [&](const Img& m, int y, int x, int n) {
     const int64_t gi = (int64_t)m.px_base + (int64_t)y * m.W + x;
-    const float s = 2.3283064365386962890625e-10f;  // 2^-32
     float* dm = pxp<float>((void*)shifted(m.plane, dmarker_off), m.pitch, y, x);
     float* dk = pxp<float>((void*)shifted(m.plane, dmask_off), m.pitch, y, x);
     float a[4], b[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      a[k] = k < n ? __ll2float_rn(__ldcs(acc_marker + gi + k)) * s : 0.f;
-      b[k] = k < n ? __ll2float_rn(__ldcs(acc_mask + gi + k)) * s : 0.f;
+      if (k < n) {
+        const ulonglong2 am = __ldcs((const ulonglong2*)(acc_marker + 2 * (gi + k)));
+        const ulonglong2 ak = __ldcs((const ulonglong2*)(acc_mask + 2 * (gi + k)));
+        a[k] = fix_to_float(am.x, (long long)am.y);
+        b[k] = fix_to_float(ak.x, (long long)ak.y);
+      } else {
+        a[k] = b[k] = 0.f;
+      }
     }
     if (n == 4 && (((uintptr_t)dm | (uintptr_t)dk) & 15) == 0) {
       *(float4*)dm = make_float4(a[0], a[1], a[2], a[3]);
@@ -1450,7 +1559,7 @@ size_t f32_fwd_bytes(int64_t batch, int64_t rows, int64_t cols) {
 
 size_t f32_bwd_bytes(int64_t batch, int64_t rows, int64_t cols) {
   const size_t px = (size_t)(batch * rows * cols);
-  return 256 + 2 * align256(8 * px) + (batch > 1 ? align256(sizeof(Img) * (size_t)batch) : 0);
+  return 256 + 2 * align256(16 * px) + (batch > 1 ? align256(sizeof(Img) * (size_t)batch) : 0);
 }
 
 // Plan over the stacked images; with more than one image the table is built on the device.
@@ -1522,17 +1631,17 @@ nsgb_status nsgb_recon_f32_bwd(const float* grad_out, const int32_t* prov, float
   char* p = (char*)ws;
   int* status = (int*)p;
   auto* am = (unsigned long long*)(p + 256);
-  auto* ak = (unsigned long long*)(p + 256 + align256(8 * px));
-  Img* table = batch > 1 ? (Img*)(p + 256 + 2 * align256(8 * px)) : nullptr;
+  auto* ak = (unsigned long long*)(p + 256 + align256(16 * px));
+  Img* table = batch > 1 ? (Img*)(p + 256 + 2 * align256(16 * px)) : nullptr;
   Plan P;
   cudaError_t e = cudaMemsetAsync(status, 0, sizeof(int), s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(am, 0, 2 * align256(8 * px), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(am, 0, 2 * align256(16 * px), s);
   if (e == cudaSuccess) e = stacked_plan((void*)grad_out, prov, batch, rows, cols, pitch, image_stride, table, &P, s);
   if (e == cudaSuccess) {
     grad_scatter_kernel<<<rcb(P.t), 256, 0, s>>>(P.I, P.t.rows, am, ak, status);
     const int64_t dmo = (int64_t)((uintptr_t)grad_marker - (uintptr_t)grad_out);
     const int64_t dko = (int64_t)((uintptr_t)grad_mask - (uintptr_t)grad_out);
-    grad_out_kernel<<<qrb(P.t), 256, 0, s>>>(P.I, P.t.rows, (const long long*)am, (const long long*)ak, dmo, dko);
+    grad_out_kernel<<<qrb(P.t), 256, 0, s>>>(P.I, P.t.rows, am, ak, dmo, dko);
     e = cudaGetLastError();
   }
   return finish(e, ws, s, opts);

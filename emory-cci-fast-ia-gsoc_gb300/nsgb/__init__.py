@@ -515,8 +515,8 @@ def recon_f32(marker: torch.Tensor, mask: torch.Tensor, connectivity: int = 8):
 
 
 def recon_f32_backward(grad: torch.Tensor, prov: torch.Tensor):
-    """Adjoint of recon_f32: (d/dmarker, d/dmask) of sum(grad * out), with exact 32.32
-    fixed-point sums."""
+    """Adjoint of recon_f32: (d/dmarker, d/dmask) of sum(grad * out); each source's gradient is
+    the exact sum of its contributions rounded once to float32."""
     squeeze = grad.dim() == 2
     g = _stack3(grad, "grad")
     p = _contig(prov).view(g.shape)

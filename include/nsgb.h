@@ -334,9 +334,12 @@ nsgb_status nsgb_noalloc_device_status(nsgb_stream_t stream);
  * out must not alias marker.  NaN inputs give NSGB_ERR_BAD_ARG.
  *
  * Backward: grad_marker(q) = sum of grad_out(p) over prov(p) = q, grad_mask(q) = sum over
- * prov(p) = ~q.  Each grad_out(p) is rounded to a multiple of 2^-32 and the sums are exact
- * 64-bit integer sums (independent of order, so bit-reproducible); |grad_out| < 2^31.
- * Out-of-range prov entries are skipped and reported as NSGB_ERR_BAD_ARG. */
+ * prov(p) = ~q, each the exact sum rounded once to float (nearest, ties to even): the terms
+ * are summed as 128-bit fixed-point integers with resolution 2^-96, in which every float from
+ * 2^-73 up to 2^31 is exact (smaller magnitudes round to the nearest multiple of 2^-96), so
+ * the result does not depend on the order of summation.  |grad_out| < 2^31 and finite, and
+ * every sum below 2^31 in magnitude; other gradients, and out-of-range prov entries, are
+ * skipped and reported as NSGB_ERR_BAD_ARG. */
 size_t nsgb_recon_f32_workspace_size(int64_t batch, int64_t rows, int64_t cols, int backward);
 nsgb_status nsgb_recon_f32_fwd(const float* marker, const float* mask, float* out, int32_t* prov, int64_t batch,
                                int64_t rows, int64_t cols, int64_t pitch, int64_t image_stride, int conn, void* ws,

@@ -53,6 +53,7 @@ def _load() -> C.CDLL:
     lib.orc_recon_f32_prov.argtypes = [vp, vp, i64, i64, i64, C.c_int, vp, vp, C.c_int]
     lib.orc_recon_f32_prov.restype = C.c_int
     lib.orc_recon_f32_grad.argtypes = [vp, vp, i64, i64, i64, vp, vp, C.c_int]
+    lib.orc_recon_f32_grad.restype = C.c_int
     lib.orc_recon_fd.argtypes = [vp, vp, vp, i64, i64, C.c_int, vp, i64, C.c_double, vp, vp, C.c_int]
     lib.nsgb_synth_tile_u8.argtypes = [vp, vp, i64, i64, i64, i64, C.c_uint64]
     return lib
@@ -412,14 +413,16 @@ def recon_f32_prov(marker: np.ndarray, mask: np.ndarray, conn: int, threads: int
 
 
 def recon_f32_grad(g: np.ndarray, prov: np.ndarray, threads: int = 0):
-    """CPU reference gradient (dmarker, dmask): exact fixed-point (2^-32) sums."""
+    """CPU reference gradient (dmarker, dmask): for every source, the exact sum of the upstream
+    gradients of the pixels it feeds, rounded once to float32 (nearest, ties to even)."""
     squeeze = np.ndim(g) == 2
     gg = _stack(g)
     pp = np.ascontiguousarray(prov, dtype=np.int32).reshape(gg.shape)
     B, H, W = gg.shape
     dm = np.empty_like(gg)
     dk = np.empty_like(gg)
-    lib.orc_recon_f32_grad(_p(gg), _p(pp), B, H, W, _p(dm), _p(dk), threads or (os.cpu_count() or 1))
+    if lib.orc_recon_f32_grad(_p(gg), _p(pp), B, H, W, _p(dm), _p(dk), threads or (os.cpu_count() or 1)) != 0:
+        raise ValueError("upstream gradient not finite or |g| >= 2^31")
     return (dm[0], dk[0]) if squeeze else (dm, dk)
 
 

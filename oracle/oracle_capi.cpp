@@ -193,13 +193,18 @@ int orc_recon_f32_prov(const float* marker, const float* mask, int64_t B, int64_
   return 0;
 }
 
-// The CPU reference gradient (fixed-point sums, see recon_grad_fixed) over B stacked images.
-void orc_recon_f32_grad(const float* g, const int32_t* prov, int64_t B, int64_t H, int64_t W, float* dmarker,
-                        float* dmask, int threads) {
+// The CPU reference gradient (exact sums rounded once, see recon_grad_fixed) over B stacked
+// images.  Returns 0, or -1 if some |g| >= 2^31 or is not finite.
+int orc_recon_f32_grad(const float* g, const int32_t* prov, int64_t B, int64_t H, int64_t W, float* dmarker,
+                       float* dmask, int threads) {
   const int64_t n = H * W;
+  std::vector<int> bad((size_t)B, 0);
   parallel_for(B, threads, [&](int64_t b) {
-    orc::recon_grad_fixed(g + b * n, prov + b * n, n, dmarker + b * n, dmask + b * n);
+    bad[b] = !orc::recon_grad_fixed(g + b * n, prov + b * n, n, dmarker + b * n, dmask + b * n);
   });
+  for (int v : bad)
+    if (v) return -1;
+  return 0;
 }
 
 // Central finite differences of L = sum_p g(p) R(p) for one H x W float image, evaluated in

@@ -10,12 +10,13 @@
 // Vincent's hybrid algorithm, numeric_limits-based padding values, and the union-find
 // root = smallest raster index rule.  It is written from the algorithm, not copied.
 //
-// Parity pins: the union-find part is checked against the reference's own
-// src/segment/ConnComponents.cpp compiled from source (oracle/build_ref.sh); the
-// reconstruction part has no reference golden output (the reference's test data is not
-// distributed), so it is pinned by the uniqueness of the reconstruction fixed point, by
-// property checks, and by the reference's inline 32x32 fixture
-// (test/segment/cuda/globalQueueTest.cu:446-583).
+// Parity pins: everything restated from the reference is checked against the reference's
+// own code compiled from its sources (oracle/build_ref.sh): ConnComponents.cpp for the
+// union-find part, and MorphologicOperations.cpp's imreconstruct / imreconstructBinary /
+// imfillHoles / bwselect / imhmin / bwlabel2 / bwareaopen2 (over a small OpenCV stand-in) for
+// the reconstruction part, through committed fixtures and, where the reference builds, live
+// (tests/test_oracle_ref_recon_cpu.py).  The float provenance and adjoint have no reference
+// counterpart.
 #pragma once
 
 #include <algorithm>
@@ -539,25 +540,80 @@ bool recon_provenance(const T* marker, const T* mask, const T* R, int64_t H, int
 
 // Adjoint of R with respect to marker and mask for an upstream gradient g:
 //   dmarker(q) = sum of g(p) over p with prov(p) = q,  dmask(q) = sum over prov(p) = ~q.
-// Each g(p) is rounded to the nearest multiple of 2^-32 (ties to even) and the sums are
-// exact 64-bit integer sums, so they do not depend on the order of summation; the result
-// is rounded to float once.  |g| < 2^31 is required.
-inline void recon_grad_fixed(const float* g, const int32_t* prov, int64_t n, float* dmarker, float* dmask) {
-  std::vector<int64_t> am((size_t)n, 0), ak((size_t)n, 0);
+// The CPU reference gradient: for every source q, the exact sum of g(p) over the pixels whose
+// provenance is q, rounded once to float (nearest, ties to even).  Each g is taken as an exact
+// multiple of 2^-96 (every float32 from 2^-73 up is one; smaller magnitudes are rounded to the
+// nearest multiple, ties to even), summed in 128-bit integers, and the sum * 2^-96 is rounded
+// to float by explicit integer rounding.  |g| >= 2^31 (or not finite) returns false.
+inline bool fix96_of(float g, __int128& out) {
+  if (!std::isfinite(g) || std::fabs(g) >= 2147483648.0f) return false;
+  int e = 0;
+  const float fr = std::frexp(std::fabs(g), &e);  // |g| = fr * 2^e, fr in [0.5, 1)
+  if (fr == 0.0f) {
+    out = 0;
+    return true;
+  }
+  const int64_t m = (int64_t)std::ldexp(fr, 24);  // |g| = m * 2^(e - 24), m < 2^24 exact
+  const int s = e - 24 + 96;
+  __int128 v;
+  if (s >= 0) {
+    v = (__int128)m << s;
+  } else if (-s >= 40) {
+    v = 0;
+  } else {
+    const int r = -s;
+    const int64_t q = m >> r, rem = m & ((int64_t(1) << r) - 1), half = int64_t(1) << (r - 1);
+    v = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+  }
+  out = g < 0 ? -v : v;
+  return true;
+}
+
+inline float fix96_to_float(__int128 S) {
+  if (S == 0) return 0.0f;
+  const bool neg = S < 0;
+  unsigned __int128 M = neg ? (unsigned __int128)(-S) : (unsigned __int128)S;
+  int lead = 127;
+  while (!((M >> lead) & 1)) --lead;
+  int e = lead - 96;
+  uint32_t m;
+  if (lead <= 23) {
+    m = (uint32_t)(M << (23 - lead));
+  } else {
+    const int r = lead - 23;
+    m = (uint32_t)(M >> r);
+    const unsigned __int128 rem = M & (((unsigned __int128)1 << r) - 1), half = (unsigned __int128)1 << (r - 1);
+    if (rem > half || (rem == half && (m & 1u))) ++m;
+    if (m == (1u << 24)) {
+      m >>= 1;
+      ++e;
+    }
+  }
+  const float f = std::ldexp((float)m, e - 23);  // m < 2^24 and the exponent in range: exact
+  return neg ? -f : f;
+}
+
+inline bool recon_grad_fixed(const float* g, const int32_t* prov, int64_t n, float* dmarker, float* dmask) {
+  std::vector<__int128> am((size_t)n, 0), ak((size_t)n, 0);
+  bool ok = true;
   for (int64_t p = 0; p < n; ++p) {
     const int32_t v = prov[p];
     if (v == INT32_MIN) continue;
     const int64_t q = v >= 0 ? v : ~(int64_t)v;
     if (q >= n) continue;
-    const int64_t f = (int64_t)std::nearbyint((double)g[p] * 4294967296.0);
+    __int128 f;
+    if (!fix96_of(g[p], f)) {
+      ok = false;
+      continue;
+    }
     if (v >= 0) am[q] += f;
     else ak[q] += f;
   }
-  // one rounding: the integer sum to float (round to nearest), then an exact scaling by 2^-32
   for (int64_t q = 0; q < n; ++q) {
-    dmarker[q] = (float)am[q] * 2.3283064365386962890625e-10f;
-    dmask[q] = (float)ak[q] * 2.3283064365386962890625e-10f;
+    dmarker[q] = fix96_to_float(am[q]);
+    dmask[q] = fix96_to_float(ak[q]);
   }
+  return ok;
 }
 
 // Flat erosion (MAX = false) / dilation (MAX = true) of a u8 image by a k x k element, as
