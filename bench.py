@@ -69,6 +69,9 @@ def parse_args():
     p.add_argument("--candidates-only", action="store_true",
                    help="profiling aid: only the segmentation-stage sections (opening + candidates, distance)")
     p.add_argument("--large-size", type=int, default=16384)
+    p.add_argument("--large-dtypes", default="u8,u16,i32")
+    p.add_argument("--only", default="", choices=["", "batched", "grad", "large", "bbox", "candidates", "distance"],
+                   help="profiling aid: run this one section alone (no headline) and print it")
     a = p.parse_args()
     if a.steps is None:
         a.steps = 5 if a.impl == "reference" else 400
@@ -238,6 +241,13 @@ def run_nsgb(args):
     if args.candidates_only:
         dev = torch.device("cuda", local)
         print(json.dumps({"candidates": candidates_section(args, dev), "distance": distance_section(args, dev)}))
+        return 0
+    if args.only:
+        dev = torch.device("cuda", local)
+        fn = {"batched": lambda: batched_section(args, dev), "grad": lambda: grad_section(dev),
+              "large": lambda: large_section(args, dev), "bbox": lambda: bbox_section(args, dev),
+              "candidates": lambda: candidates_section(args, dev), "distance": lambda: distance_section(args, dev)}
+        print(json.dumps({args.only: fn[args.only]()}))
         return 0
     dist = None
     if world > 1:
@@ -986,7 +996,7 @@ def large_section(args, dev, steps=3):
                        f"erosion), threshold > 128 x scale, bwlabel 8-conn relabel; device-resident",
            "bytes_per_px": "fill 2*s (image read, result written), threshold s+1, bwlabel 5"}
     peak, _ = read_peaks()
-    for dt in ("u8", "u16", "i32"):
+    for dt in [d for d in args.large_dtypes.split(",") if d]:
         img_h = img8 if dt == "u8" else synth.scale(img8, dt)[0]
         code = {"u8": _ffi.U8, "u16": _ffi.U16, "i32": _ffi.I32}[dt]
         esz = img_h.dtype.itemsize
