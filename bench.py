@@ -97,16 +97,41 @@ def read_peaks():
         return 6800.0, "fallback"
 
 
+RECON_SOURCES = ("recon.cu", "tilequeue.cuh", "common.cuh", "batch.cuh")
+RECON_PROFILE = os.path.join(ROOT, "profiles", "recon_kernel_u8_4096.md")
+
+
+def recon_source_sha():
+    """SHA-256 over the reconstruction's device sources, in a fixed order."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for name in RECON_SOURCES:
+        with open(os.path.join(PKG, "csrc", name), "rb") as f:
+            h.update(name.encode() + b"\0" + f.read())
+    return h.hexdigest()
+
+
 def read_traffic(size):
-    """DRAM bytes per launch of the reconstruction kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "recon_kernel_u8_4096.md")
+    """DRAM bytes per reconstruction call (all its launches) from the committed ncu summary, and
+    a note.  ncu cannot run inside the bench (it replays kernels), so the capture is taken
+    separately; it is used only while the reconstruction's sources hash to the value recorded
+    with it, otherwise traffic is null and the note says why."""
+    fields = {}
     try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_launch_4096:") and size == 4096:
-                return int(line.split(":")[1].strip())
+        for line in open(RECON_PROFILE):
+            if ":" in line and line.split(":")[0] in ("traffic_bytes_per_launch_4096", "recon_source_sha256"):
+                k, v = line.split(":", 1)
+                fields[k.strip()] = v.strip()
     except OSError:
-        pass
-    return None
+        return None, "no ncu summary committed"
+    if size != 4096 or "traffic_bytes_per_launch_4096" not in fields:
+        return None, "no ncu capture for this size"
+    cur = recon_source_sha()
+    if fields.get("recon_source_sha256") != cur:
+        return None, f"stale: the reconstruction sources (sha256 {cur[:12]}) changed since the ncu capture"
+    return int(fields["traffic_bytes_per_launch_4096"]), (
+        f"ncu capture of the same bench command, reconstruction sources sha256 {cur[:12]} (see {os.path.relpath(RECON_PROFILE, ROOT)})")
 
 
 class ClockSampler:
@@ -406,7 +431,7 @@ def run_nsgb(args):
 
     peak, peak_kind = read_peaks()
     achieved = RECON_BYTES_PER_PX * n_px / (rms / 1e3) / 1e9
-    traffic = read_traffic(args.size)
+    traffic, traffic_note = read_traffic(args.size)
     line = {
         "metric": METRIC,
         "value": world * n_px / 1e6 / (ms / 1e3),
@@ -440,6 +465,7 @@ def run_nsgb(args):
             "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
             "algorithmic_bytes_per_launch": RECON_BYTES_PER_PX * n_px,
             "traffic": traffic,
+            "traffic_source": traffic_note,
         },
         "e2e": {
             "value": world * n_px / 1e6 / (e2e_ms / 1e3),

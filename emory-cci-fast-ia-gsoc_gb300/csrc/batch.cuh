@@ -16,6 +16,8 @@ struct Img {
   int H, W;
   int aligned;        // plane / aux aligned for vector tile loads
   int r_tiles_x, r_tiles_y, r_tile_base;  // reconstruction tiles
+  int r_stile_base;   // first of its tiles on the half-tile-shifted grid (streaming passes)
+  int r_tw;           // reconstruction tile width in pixels (64 for u8/u16, 32 for i32/f32)
   int r_even_base;    // first of its checkerboard colour-0 tiles among all images' colour-0 tiles
   int r_col_base[3];  // the same for the first three colours of the four-colour order
   int c_tiles_x, c_tile_base;             // 32x32 labelling tiles
@@ -82,6 +84,7 @@ struct BatchTotals {
   int n;
   int64_t px;      // total pixels (< 2^31)
   int r_tiles;     // reconstruction tiles
+  int r_stiles;    // reconstruction tiles of the half-tile-shifted grid
   int r_even;      // reconstruction tiles of checkerboard colour 0
   int r_col[3];    // reconstruction tiles of the first three colours of the four-colour order
   int c_tiles;     // labelling tiles

@@ -132,30 +132,41 @@ __global__ void __launch_bounds__(kThreads) bbox_scan(Imgs I, int32_t bgval, BWs
   }
 }
 
-// Folds each warp's row segment by label, then one update per label and field.
+// Folds each warp's row segment by label, then one update per label and field.  A thread takes
+// kAccumRows rows of its column per step and issues all their label loads before using any
+// (one load per thread and step left the kernel waiting on load latency).
+constexpr int kAccumRows = 8;
+
 __global__ void __launch_bounds__(kThreads) bbox_accum(Imgs I, int32_t bgval, BWs w) {
   const Img& m = I.one;
   const int n = m.H * m.W;
   const int stop = __ldcg(w.hdr + 1);
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
-  for (int y = blockIdx.y; y < m.H; y += gridDim.y) {
-    int key = -1;
-    if (x < m.W && y * m.W + x < stop) {
-      const int32_t l = label_at(m, y, x);
-      if (l != bgval && l >= 1 && l <= n) key = l;
+  for (int y0 = blockIdx.y * kAccumRows; y0 < m.H; y0 += gridDim.y * kAccumRows) {
+    int32_t lab[kAccumRows];
+#pragma unroll
+    for (int r = 0; r < kAccumRows; ++r) {
+      const int y = y0 + r;
+      lab[r] = (x < m.W && y < m.H && y * m.W + x < stop) ? label_at(m, y, x) : bgval;
     }
-    const unsigned peers = __match_any_sync(NSGB_FULL, key);
-    if (key < 0) continue;
-    const int xmin = __reduce_min_sync(peers, x);
-    const int xmax = __reduce_max_sync(peers, x);
-    if (lane != __ffs(peers) - 1) continue;
-    const int fi = y * m.W + xmin;
-    if (fi < w.first[key]) atomicMin(w.first + key, fi);
-    if (xmin < w.mnx[key]) atomicMin(w.mnx + key, xmin);
-    if (xmax > w.mxx[key]) atomicMax(w.mxx + key, xmax);
-    if (y < w.mny[key]) atomicMin(w.mny + key, y);
-    if (y > w.mxy[key]) atomicMax(w.mxy + key, y);
+#pragma unroll
+    for (int r = 0; r < kAccumRows; ++r) {
+      const int y = y0 + r;
+      const int32_t l = lab[r];
+      const int key = (l != bgval && l >= 1 && l <= n) ? (int)l : -1;
+      const unsigned peers = __match_any_sync(NSGB_FULL, key);
+      if (key < 0) continue;
+      const int xmin = __reduce_min_sync(peers, x);
+      const int xmax = __reduce_max_sync(peers, x);
+      if (lane != __ffs(peers) - 1) continue;
+      const int fi = y * m.W + xmin;
+      if (fi < w.first[key]) atomicMin(w.first + key, fi);
+      if (xmin < w.mnx[key]) atomicMin(w.mnx + key, xmin);
+      if (xmax > w.mxx[key]) atomicMax(w.mxx + key, xmax);
+      if (y < w.mny[key]) atomicMin(w.mny + key, y);
+      if (y > w.mxy[key]) atomicMax(w.mxy + key, y);
+    }
   }
 }
 
@@ -210,7 +221,8 @@ cudaError_t bbox_launch(const Imgs& I, const BatchTotals& t, int32_t bgval, void
   bbox_header<<<1, 1, 0, s>>>(w);
   bbox_scan<<<dim3(rows.x, rows.y < 512 ? rows.y : 512), kThreads, 0, s>>>(I, bgval, w);
   bbox_init<<<g, kThreads, 0, s>>>(w, n);
-  bbox_accum<<<rows, kThreads, 0, s>>>(I, bgval, w);
+  const int ry = (rows.y + kAccumRows - 1) / kAccumRows;
+  bbox_accum<<<dim3(rows.x, ry < 65535 ? ry : 65535), kThreads, 0, s>>>(I, bgval, w);
   bbox_mark<<<g, kThreads, 0, s>>>(w, n);
   e = ccl::rank_bits(I, t, w.bits, w.blk, w.wpre, s);
   if (e != cudaSuccess) return e;

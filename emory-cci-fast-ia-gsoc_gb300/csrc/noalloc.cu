@@ -80,7 +80,8 @@ extern "C" nsgb_status nsgb_imreconstruct_noalloc(int dtype, void* marker, const
     return NSGB_ERR_CUDA;
   cudaError_t e = nsgb::recon_launch(dtype, marker, marker, mask, rows, cols, pitch, conn, erode != 0, ring, ws, s,
                                      opts ? opts->max_visits_per_tile : 0, opts ? opts->max_visit_iters : 0,
-                                     opts ? opts->queue_poll_limit : 0);
+                                     opts ? opts->queue_poll_limit : 0, opts ? opts->recon_passes : 0,
+                                     opts ? opts->recon_order : 0, opts ? opts->recon_ctas_per_sm : 0);
   if (e != cudaSuccess) return NSGB_ERR_CUDA;
   if (opts && opts->recon_event_end && cudaEventRecord((cudaEvent_t)opts->recon_event_end, s) != cudaSuccess)
     return NSGB_ERR_CUDA;

@@ -441,6 +441,7 @@ void add_image(Img& m, BatchTotals& t) {
   m.c_tiles_x = (m.W + ccl::kTile - 1) / ccl::kTile;
   const int c_tiles_y = (m.H + ccl::kTile - 1) / ccl::kTile;
   m.r_tile_base = t.r_tiles;
+  m.r_stile_base = t.r_stiles;
   m.r_even_base = t.r_even;
   for (int c = 0; c < 3; ++c) m.r_col_base[c] = t.r_col[c];
   m.c_tile_base = t.c_tiles;
@@ -449,6 +450,7 @@ void add_image(Img& m, BatchTotals& t) {
   m.row_base = t.rows;
   const int64_t npx = (int64_t)m.H * m.W;
   t.r_tiles += m.r_tiles_x * m.r_tiles_y;
+  if (m.r_tw > 0) t.r_stiles += ((m.H + 47) / 32) * ((m.W + m.r_tw / 2 + m.r_tw - 1) / m.r_tw);
   t.r_even += even_tiles(m.r_tiles_x, m.r_tiles_y);
   for (int c = 0; c < 3; ++c) t.r_col[c] += colour_tiles(m.r_tiles_x, m.r_tiles_y, c);
   t.c_tiles += m.c_tiles_x * c_tiles_y;
@@ -556,7 +558,8 @@ cudaError_t recon_timed(const nsgb_opts* o, int dtype, const Plan& P, int conn, 
   cudaError_t e = record(o, true, s);
   if (e != cudaSuccess) return e;
   e = recon_launch_batch(dtype, P.I, P.t.r_tiles, conn, erode, ring, ws, s, o ? o->max_visits_per_tile : 0,
-                         o ? o->max_visit_iters : 0, resweeps, o ? o->queue_poll_limit : 0);
+                         o ? o->max_visit_iters : 0, resweeps, o ? o->queue_poll_limit : 0, o ? o->recon_passes : 0,
+                         P.t.r_stiles, o ? o->recon_order : 0, (long long)P.t.px, o ? o->recon_ctas_per_sm : 0);
   if (e != cudaSuccess) return e;
   return record(o, false, s);
 }
@@ -1520,6 +1523,7 @@ __global__ void stack_table_kernel(Img proto, int n, int64_t stride, BatchTotals
   m.plane = (void*)((uintptr_t)proto.plane + (uintptr_t)(i * stride));
   m.aux = (const void*)((uintptr_t)proto.aux + (uintptr_t)(i * stride));
   m.r_tile_base = i * one.r_tiles;
+  m.r_stile_base = i * one.r_stiles;
   m.r_even_base = i * even_tiles(proto.r_tiles_x, proto.r_tiles_y);
   for (int c = 0; c < 3; ++c) m.r_col_base[c] = i * colour_tiles(proto.r_tiles_x, proto.r_tiles_y, c);
   m.c_tile_base = i * one.c_tiles;
@@ -1535,6 +1539,7 @@ BatchTotals stacked_totals(const BatchTotals& one, int64_t n) {
   t.n = (int)n;
   t.px = one.px * n;
   t.r_tiles = (int)(one.r_tiles * n);
+  t.r_stiles = (int)(one.r_stiles * n);
   t.r_even = (int)(one.r_even * n);
   for (int c = 0; c < 3; ++c) t.r_col[c] = (int)(one.r_col[c] * n);
   t.c_tiles = (int)(one.c_tiles * n);

@@ -742,6 +742,266 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   }
 }
 
+// ------------------------------------------------------------------------------------------
+// Streaming passes (before the work queue).  A pass sweeps every tile of a grid to its local
+// fixed point once, with the halo read from the current state, in parallel and without queue,
+// tile states or fences (the passes are separate launches, so each sees the previous one's
+// stores).  The grid alternates between the tile grid and the grid shifted by half a tile in
+// each direction: the boundaries of one pass lie inside the tiles of the next, so what a pass
+// could not carry across its tile boundaries the next one carries inside its tiles.  All
+// updates only ever raise values towards the fixed point, so the passes give a valid starting
+// state for the queue whatever they achieve.  The last pass is on the tile grid and runs the
+// queue visit's neighbour test: every tile whose halo it could still raise is flagged in the
+// state array, and the queue starts from exactly the flagged tiles.  Every other tile was
+// swept to its local fixed point and no neighbour could raise its halo since, so the queue's
+// invariant (a tile that is not queued or running is stable) holds from the start.
+struct PassArgs {
+  Imgs I;
+  int ntiles;      // tiles of this pass's grid (all images)
+  int oy, ox;      // grid offset in pixels (0, or half a tile)
+  int flip, ring;
+  int max_iters;
+  int* status;
+  int* flags;      // last pass: the queue's tile state array (flagged neighbours set to kQueued)
+};
+
+struct RSTileBase { __device__ int operator()(const Img& m) const { return m.r_stile_base; } };
+
+template <typename T, int CONN, bool BATCH, bool FLAGS>
+__device__ __forceinline__ void pass_tile(const PassArgs& a, WarpBuf& B, int t, int lane) {
+  using P = Px<T>;
+  constexpr int E = P::E;
+  constexpr int TW = 32 * E;
+  const bool shifted = a.oy != 0;
+  const int ii = BATCH ? (shifted ? img_of(a.I, t, RSTileBase()) : img_of(a.I, t, RTileBase())) : 0;
+  const Img& m = BATCH ? a.I.d[ii] : a.I.one;
+  const int H = m.H, W = m.W;
+  const int ntx = shifted ? (W + a.ox + TW - 1) / TW : m.r_tiles_x;
+  const int lt = t - (BATCH ? (shifted ? m.r_stile_base : m.r_tile_base) : 0);
+  const int ty = lt / ntx, tx = lt - ty * ntx;
+  const int y0 = ty * kRows - a.oy, x0 = tx * TW - a.ox;
+  const bool flip = a.flip != 0, ring = a.ring != 0;
+  T* const out = (T*)m.plane;
+  const T* const mask = (const T*)m.aux;
+  const int64_t pitch = m.pitch;
+  const bool interior = y0 >= 0 && x0 >= 0 && (y0 + kRows <= H) && (x0 + TW <= W);
+  const bool fast = BATCH ? interior : interior && m.aligned;
+  const bool pairs = BATCH;
+  const int xl = x0 + E * lane;
+  const uint32_t fx = flip ? P::FLIP : 0u;
+
+  uint32_t O[32], M[32];
+  if (fast) {
+    const char* mp = (const char*)mask + (int64_t)y0 * pitch + (int64_t)xl * sizeof(T);
+    const char* op = (const char*)out + (int64_t)y0 * pitch + (int64_t)xl * sizeof(T);
+#pragma unroll
+    for (int i = 0; i < 32; ++i) M[i] = fast_word<T>(mp + i * pitch, false, fx, pairs);
+#pragma unroll
+    for (int i = 0; i < 32; ++i) O[i] = fast_word<T>(op + i * pitch, true, fx, pairs);
+  } else {
+#pragma unroll 1
+    for (int i = 0; i < 32; ++i) {
+      B.xp[lane * kS + i] = load_word<T>(mask, pitch, y0 + i, xl, H, W, false, false, flip);
+      B.mh[lane * kS + i] = load_word<T>(out, pitch, y0 + i, xl, H, W, false, true, flip);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      M[i] = B.xp[lane * kS + i];
+      O[i] = B.mh[lane * kS + i];
+    }
+    __syncwarp();
+  }
+  const bool fast_top = fast && !pairs && y0 > 0;
+  const bool fast_bot = fast && !pairs && y0 + kRows < H;
+  const uint32_t topm = load_word<T>(mask, pitch, y0 - 1, xl, H, W, fast_top, false, flip);
+  const uint32_t topv_raw = load_word<T>(out, pitch, y0 - 1, xl, H, W, fast_top, true, flip);
+  const uint32_t botm = load_word<T>(mask, pitch, y0 + kRows, xl, H, W, fast_bot, false, flip);
+  const uint32_t botv_raw = load_word<T>(out, pitch, y0 + kRows, xl, H, W, fast_bot, true, flip);
+  uint32_t hm[4], hv[4];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const int k = lane + 32 * j;
+    const int y = y0 - 1 + k;
+    const bool ok = k < 34;
+    hm[2 * j] = ok ? load_elem_at<T>(mask, pitch, y, x0 - 1, H, W, false, flip) : P::LOW;
+    hm[2 * j + 1] = ok ? load_elem_at<T>(mask, pitch, y, x0 + TW, H, W, false, flip) : P::LOW;
+    hv[2 * j] = ok ? load_elem_at<T>(out, pitch, y, x0 - 1, H, W, true, flip) : P::LOW;
+    hv[2 * j + 1] = ok ? load_elem_at<T>(out, pitch, y, x0 + TW, H, W, true, flip) : P::LOW;
+  }
+  uint32_t any_change = 0;
+#pragma unroll
+  for (int i = 0; i < 32; i += 2) sts2(B.mv + lane * kS + i, M[i], M[i + 1]);
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    const uint32_t v = init_word<T>(O[i], M[i], y0 + i, xl, H, W, ring);
+    any_change |= v ^ O[i];
+    O[i] = v;
+  }
+  const uint32_t topv = init_word<T>(topv_raw, topm, y0 - 1, xl, H, W, ring);
+  const uint32_t botv = init_word<T>(botv_raw, botm, y0 + kRows, xl, H, W, ring);
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const int k = lane + 32 * j;
+    if (k < 34) {
+      const int y = y0 - 1 + k;
+      B.lm[k] = hm[2 * j];
+      B.rm[k] = hm[2 * j + 1];
+      B.lv[k] = init_elem<T>(hv[2 * j], hm[2 * j], y, x0 - 1, H, W, ring);
+      B.rv[k] = init_elem<T>(hv[2 * j + 1], hm[2 * j + 1], y, x0 + TW, H, W, ring);
+    }
+  }
+  __syncwarp();
+  halo_carries<T, CONN>(B, lane);
+  if constexpr (E == 2) {
+    const int q = lane & 15, half = lane >> 4;
+#pragma unroll
+    for (int j = 0; j < 32; j += 2) {
+      const uint2 mm = lds2(B.mv + (16 * half + (j >> 1)) * kS + 2 * q);
+      sts2(B.mh + lane * kS + j, __byte_perm(mm.x, mm.y, 0x5410), __byte_perm(mm.x, mm.y, 0x7632));
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) B.mh[lane * kS + j] = B.mv[j * kS + lane];
+  }
+  __syncwarp();
+
+  int it = 0;
+  for (;;) {
+    col_to_row<E>(O, B.xp, lane);
+    const uint32_t racc = row_pass<T>(O, B.mh, B, lane);
+    any_change |= racc;
+    row_to_col<E>(O, B.xp, lane);
+    if (CONN == 4 && it > 0 && !__any_sync(NSGB_FULL, racc != 0)) break;
+    const uint32_t acc = col_pass<T, CONN>(O, B, topv, botv, lane);
+    any_change |= acc;
+    ++it;
+    if (!__any_sync(NSGB_FULL, acc != 0)) break;
+    if (it >= a.max_iters) {
+      if (lane == 0) set_status(a.status, kDevNotConverged);
+      break;
+    }
+  }
+
+  if (__any_sync(NSGB_FULL, any_change != 0)) {
+    if (fast) {
+      char* sp = (char*)out + (int64_t)y0 * pitch + (int64_t)xl * sizeof(T);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) fast_store<T>(sp + i * pitch, O[i], fx, pairs);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 32; ++i) B.xp[lane * kS + i] = O[i];
+      __syncwarp();
+#pragma unroll 1
+      for (int i = 0; i < 32; ++i) store_word<T>(out, pitch, y0 + i, xl, H, W, B.xp[lane * kS + i], false, flip);
+      __syncwarp();
+    }
+  }
+  if constexpr (FLAGS) {
+    // the queue visit's neighbour test: which neighbouring tiles could the border raise?
+    unsigned dirs = 0;
+    {
+      uint32_t c_top = O[0], c_bot = O[31];
+      if constexpr (CONN == 8) {
+        uint32_t l = __shfl_up_sync(NSGB_FULL, O[0], 1), r = __shfl_down_sync(NSGB_FULL, O[0], 1);
+        if (lane == 0) l = P::LOW;
+        if (lane == 31) r = P::LOW;
+        c_top = P::vmax(c_top, P::vmax(P::from_left(l, O[0]), P::from_right(O[0], r)));
+        l = __shfl_up_sync(NSGB_FULL, O[31], 1);
+        r = __shfl_down_sync(NSGB_FULL, O[31], 1);
+        if (lane == 0) l = P::LOW;
+        if (lane == 31) r = P::LOW;
+        c_bot = P::vmax(c_bot, P::vmax(P::from_left(l, O[31]), P::from_right(O[31], r)));
+      }
+      c_top = P::vmin(c_top, topm);
+      c_bot = P::vmin(c_bot, botm);
+      if (__any_sync(NSGB_FULL, P::vmax(topv, c_top) != topv)) dirs |= 1u << 1;
+      if (__any_sync(NSGB_FULL, P::vmax(botv, c_bot) != botv)) dirs |= 1u << 7;
+    }
+    {
+      if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) B.c0[i] = P::elem(O[i], 0);
+      }
+      if (lane == 31) {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) B.c1[i] = P::elem(O[i], E - 1);
+      }
+      __syncwarp();
+      const int r = lane;
+      uint32_t cl = B.c0[r], cr = B.c1[r];
+      if constexpr (CONN == 8) {
+        if (r > 0) {
+          cl = P::emax(cl, B.c0[r - 1]);
+          cr = P::emax(cr, B.c1[r - 1]);
+        }
+        if (r < 31) {
+          cl = P::emax(cl, B.c0[r + 1]);
+          cr = P::emax(cr, B.c1[r + 1]);
+        }
+      }
+      const bool rl = P::lt(B.lv[r + 1], P::emin(cl, B.lm[r + 1]));
+      const bool rr = P::lt(B.rv[r + 1], P::emin(cr, B.rm[r + 1]));
+      if (__any_sync(NSGB_FULL, rl)) dirs |= 1u << 3;
+      if (__any_sync(NSGB_FULL, rr)) dirs |= 1u << 5;
+      if constexpr (CONN == 8) {
+        if (P::lt(B.lv[0], P::emin(B.c0[0], B.lm[0]))) dirs |= 1u << 0;
+        if (P::lt(B.rv[0], P::emin(B.c1[0], B.rm[0]))) dirs |= 1u << 2;
+        if (P::lt(B.lv[33], P::emin(B.c0[31], B.lm[33]))) dirs |= 1u << 6;
+        if (P::lt(B.rv[33], P::emin(B.c1[31], B.rm[33]))) dirs |= 1u << 8;
+      }
+      __syncwarp();
+    }
+    if (lane < 9 && ((dirs >> lane) & 1u)) {
+      const int ny = ty + lane / 3 - 1, nx = tx + lane % 3 - 1;
+      if (ny >= 0 && ny < m.r_tiles_y && nx >= 0 && nx < m.r_tiles_x)
+        a.flags[(BATCH ? m.r_tile_base : 0) + ny * m.r_tiles_x + nx] = kQueued;
+    }
+    __syncwarp();
+  }
+}
+
+// One warp per tile of the pass's grid.
+template <typename T, int CONN, bool BATCH, bool FLAGS>
+__global__ void __launch_bounds__(kWarps * 32, 4) recon_pass_kernel(PassArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  WarpBuf& B = reinterpret_cast<WarpBuf*>(smem_raw)[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int t = blockIdx.x * kWarps + (threadIdx.x >> 5);
+  if (t >= a.ntiles) return;
+  pass_tile<T, CONN, BATCH, FLAGS>(a, B, t, lane);
+}
+
+// The queue's starting state after the passes: the tiles the last pass flagged (state
+// kQueued) go into the ring, every other tile is idle.  If none was flagged the done flag is
+// raised at once, so the queue kernel ends without work.
+__global__ void recon_seed_kernel(Ctl c, int ntiles, unsigned* counter) {
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < c.cap; i += gridDim.x * blockDim.x) {
+    if ((int)i < ntiles && c.state[i] == kQueued) {
+      const unsigned k = atomicAdd(counter, 1u);
+      c.slots[k].val = (int)i;
+      c.slots[k].seq = k + 1u;
+    }
+  }
+}
+// The passes' tile visits count towards the visit budget: the queue's counter starts there.
+__global__ void recon_seed_finish_kernel(Ctl c, const unsigned* counter, unsigned long long pass_visits) {
+  // slots k >= count: empty for this lap
+  const unsigned n = *counter;
+  for (unsigned i = n + blockIdx.x * blockDim.x + threadIdx.x; i < c.cap; i += gridDim.x * blockDim.x) {
+    c.slots[i].val = -1;
+    c.slots[i].seq = i;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *c.head = 0u;
+    *c.tail = n;
+    *c.pending = (int)n;
+    *c.visit_count = pass_visits;
+    if (pass_visits > (unsigned long long)c.max_visits) set_status(c.status, kDevNotConverged);
+    if (n == 0) *c.done = 1;
+  }
+}
+
 template <typename T, int CONN, bool BATCH, bool RS>
 __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -848,36 +1108,119 @@ __global__ void recon_init_kernel(Ctl c, Imgs I, int ntiles, int order) {
 }
 
 // Workspace layout (ints): [0] status, [1..4] stats (visits, sweeps, re-runs, re-sweeps),
-// [5] profiler visit index, [6..7] visit counter (64-bit), [32] head, [64] tail, [96] pending,
+// [5] profiler visit index, [6..7] visit counter (64-bit), [8] tiles seeded by the streaming
+// passes, [32] head, [64] tail, [96] pending,
 // [128] done flag, [160..175] phase timers (8 x 64-bit); from int kHdrInts: state[ntiles],
 // then the ring (2 ints per slot, cap slots).  Head, tail, pending and the done flag sit on
 // separate 128-byte lines: the atomics of the working warps and the polls of the waiting
 // ones then do not queue behind one another.
 constexpr int kHdrInts = 192;
+constexpr int kSeedCounter = 8;  // header int: tiles flagged by the last streaming pass
 
 template <typename T>
 int tiles_x_for(int64_t W) { return (int)((W + 32 * Px<T>::E - 1) / (32 * Px<T>::E)); }
 
-// Initial queue order (see initial_tile), measured best on the synthetic tiles: for a single
-// image, checkerboard for the 32 x 64 tiles of 8/16-bit pixels and four colours for the
-// 32 x 32 tiles of 32-bit pixels; for a batch, four colours for every type (each colour of all
-// images before the next colour: on the 256-tile u8 workload 24k re-runs instead of 525k with
-// the checkerboard).  NSGB_RECON_ORDER overrides it for experiments.
-inline int recon_order(int elems_per_word, bool batch) {
-  static std::atomic<int> cached{-2};
-  int order = cached.load(std::memory_order_relaxed);
-  if (order == -2) {
-    const char* e = getenv("NSGB_RECON_ORDER");
-    order = (e && *e) ? atoi(e) : -1;
-    cached.store(order, std::memory_order_relaxed);
+// The schedule's tuned defaults: the autotuner (tune.py) writes tuning.json, and the build
+// compiles it into kTuning (tuning.inc, generated): per dtype, connectivity, direction, single
+// image or batch and image size, the number of streaming passes and the initial ring order.
+// Without an entry: no passes, and the ring order measured best on the synthetic tiles (single
+// images: checkerboard for 32 x 64 tiles, four colours for 32 x 32; batches: four colours).  NSGB_RECON_PASSES / NSGB_RECON_ORDER override the defaults for experiments.
+struct TuneEntry {
+  int dtype, conn, erode, batch;
+  long long max_px;
+  int passes, order, ctas;
+};
+#include "tuning.inc"
+
+struct Schedule {
+  int passes, order, ctas;  // ctas: queue CTAs per SM, 0 = as many as fit
+};
+
+int env_int(const char* name, std::atomic<int>& cache) {
+  int v = cache.load(std::memory_order_relaxed);
+  if (v == -2) {
+    const char* e = getenv(name);
+    v = (e && *e) ? atoi(e) : -1;
+    cache.store(v, std::memory_order_relaxed);
   }
-  if (order >= 0) return order;
-  return (elems_per_word == 2 && !batch) ? 1 : 2;
+  return v;
+}
+
+Schedule tuned_schedule(int dtype, int conn, bool erode, bool batch, long long px) {
+  Schedule sc;
+  sc.passes = 0;
+  sc.ctas = 0;
+  sc.order = batch ? 2 : ((dtype == NSGB_U8 || dtype == NSGB_U16) ? 1 : 2);
+  for (const TuneEntry& t : kTuning) {
+    if (t.max_px > 0 && t.dtype == dtype && t.conn == conn && t.erode == (erode ? 1 : 0) &&
+        t.batch == (batch ? 1 : 0) && px <= t.max_px) {
+      sc.passes = t.passes;
+      sc.order = t.order;
+      sc.ctas = t.ctas;
+      break;
+    }
+  }
+  static std::atomic<int> env_passes{-2}, env_order{-2}, env_ctas{-2};
+  const int ep = env_int("NSGB_RECON_PASSES", env_passes), eo = env_int("NSGB_RECON_ORDER", env_order);
+  const int ec = env_int("NSGB_RECON_CTAS", env_ctas);
+  if (ep >= 0) sc.passes = ep;
+  if (eo >= 0) sc.order = eo;
+  if (ec >= 0) sc.ctas = ec;
+  return sc;
+}
+
+// Streaming passes before the queue (see recon_pass_kernel): `passes` launches alternating
+// between the shifted and the tile grid, the last on the tile grid with neighbour flags, then
+// the ring is seeded with the flagged tiles.  Returns false if the passes do not apply (a
+// batch without shifted-grid bases).
+template <typename T, int CONN, bool BATCH>
+cudaError_t run_passes(const Imgs& I, int ntiles, int nstiles, const Ctl& c, int* wi, bool erode, bool ring,
+                       int max_iters, int passes, cudaStream_t s) {
+  constexpr int TW = 32 * Px<T>::E;
+  const size_t smem = sizeof(WarpBuf) * kWarps;
+  cudaError_t e = cudaMemsetAsync(c.state, 0, sizeof(int) * (size_t)ntiles, s);
+  if (e != cudaSuccess) return e;
+  PassArgs p;
+  p.I = I;
+  p.flip = erode ? 1 : 0;
+  p.ring = ring ? 1 : 0;
+  p.max_iters = max_iters;
+  p.status = c.status;
+  p.flags = c.state;
+  for (int k = 0; k < passes; ++k) {
+    const bool shifted = ((passes - 1 - k) & 1) != 0;
+    const bool last = k == passes - 1;
+    p.oy = shifted ? kRows / 2 : 0;
+    p.ox = shifted ? TW / 2 : 0;
+    p.ntiles = shifted ? nstiles : ntiles;
+    const dim3 grid((p.ntiles + kWarps - 1) / kWarps);
+    if (last) {
+      e = cudaFuncSetAttribute(recon_pass_kernel<T, CONN, BATCH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+      if (e != cudaSuccess) return e;
+      recon_pass_kernel<T, CONN, BATCH, true><<<grid, kWarps * 32, smem, s>>>(p);
+    } else {
+      e = cudaFuncSetAttribute(recon_pass_kernel<T, CONN, BATCH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+      if (e != cudaSuccess) return e;
+      recon_pass_kernel<T, CONN, BATCH, false><<<grid, kWarps * 32, smem, s>>>(p);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  unsigned* counter = (unsigned*)(wi + kSeedCounter);
+  const int sgrid = (int)((c.cap + 255) / 256);
+  unsigned long long visits = 0;
+  for (int k = 0; k < passes; ++k) visits += (((passes - 1 - k) & 1) != 0) ? (unsigned)nstiles : (unsigned)ntiles;
+  recon_seed_kernel<<<sgrid, 256, 0, s>>>(c, ntiles, counter);
+  recon_seed_finish_kernel<<<sgrid, 256, 0, s>>>(c, counter, visits);
+  return cudaGetLastError();
 }
 
 template <typename T, int CONN, bool BATCH, bool RS>
 cudaError_t launch_typed(const Imgs& I, int ntiles, bool erode, bool ring, void* ws, cudaStream_t s,
-                         int max_visits_per_tile, int max_iters, int resweeps, long long poll_limit) {
+                         int max_visits_per_tile, int max_iters, int resweeps, long long poll_limit, int passes,
+                         int nstiles, int order, int ctas) {
   Args a;
   a.I = I;
   a.ntiles = ntiles;
@@ -903,8 +1246,12 @@ cudaError_t launch_typed(const Imgs& I, int ntiles, bool erode, bool ring, void*
 
   cudaError_t e = cudaMemsetAsync(wi, 0, sizeof(int) * kHdrInts, s);
   if (e != cudaSuccess) return e;
-  recon_init_kernel<<<(a.c.cap + 255) / 256, 256, 0, s>>>(a.c, I, ntiles, recon_order(Px<T>::E, BATCH));
-  e = cudaGetLastError();
+  if (passes > 0 && (!BATCH || nstiles > 0)) {
+    e = run_passes<T, CONN, BATCH>(I, ntiles, nstiles, a.c, wi, erode, ring, a.max_iters, passes, s);
+  } else {
+    recon_init_kernel<<<(a.c.cap + 255) / 256, 256, 0, s>>>(a.c, I, ntiles, order);
+    e = cudaGetLastError();
+  }
   if (e != cudaSuccess) return e;
 
   const size_t smem = sizeof(WarpBuf) * kWarps;
@@ -931,6 +1278,12 @@ cudaError_t launch_typed(const Imgs& I, int ntiles, bool erode, bool ring, void*
     if (occ <= 0) return cudaErrorLaunchOutOfResources;
     if (cached) occ_cache[dev].store(occ, std::memory_order_relaxed);
   }
+  if (ctas > 0) {
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    if ((long long)ctas * sms < occ) occ = ctas * sms;
+  }
   int grid = (ntiles + kWarps - 1) / kWarps;
   if (grid > occ) grid = occ;
   if (grid < 1) grid = 1;
@@ -955,6 +1308,14 @@ int recon_tiles_x(int dtype, int64_t W) {
 
 int recon_tiles_y(int64_t H) { return (int)((H + kRows - 1) / kRows); }
 
+// Tiles of the grid shifted by half a tile (rows -16 .., columns -TW/2 ..) covering the image.
+int recon_stiles(int dtype, int64_t H, int64_t W) {
+  const int E = (dtype == NSGB_U8 || dtype == NSGB_U16) ? 2 : 1;
+  const int64_t TW = 32 * E;
+  const int64_t ny = (H + kRows / 2 + kRows - 1) / kRows, nx = (W + TW / 2 + TW - 1) / TW;
+  return (int)(ny * nx);
+}
+
 size_t recon_workspace_bytes_tiles(int64_t nt) {
   return sizeof(int) * (size_t)(kHdrInts + ((nt + 1) & ~1) + 2 * (int64_t)ring_cap(nt));
 }
@@ -971,25 +1332,39 @@ namespace {
 // re-sweeps are offered for single images, where hole filling uses them).
 template <typename T, bool RS>
 cudaError_t dispatch_conn(const Imgs& I, int ntiles, int conn, bool erode, bool ring, void* ws, cudaStream_t s,
-                          int max_visits, int max_iters, int resweeps, long long poll) {
+                          int max_visits, int max_iters, int resweeps, long long poll, int passes, int nstiles,
+                          int order, int ctas) {
   if (I.d)
-    return conn == 8 ? launch_typed<T, 8, true, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, 0, poll)
-                     : launch_typed<T, 4, true, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, 0, poll);
-  return conn == 8
-             ? launch_typed<T, 8, false, RS>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps, poll)
-             : launch_typed<T, 4, false, RS>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps, poll);
+    return conn == 8 ? launch_typed<T, 8, true, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, 0, poll,
+                                                       passes, nstiles, order, ctas)
+                     : launch_typed<T, 4, true, false>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, 0, poll,
+                                                       passes, nstiles, order, ctas);
+  return conn == 8 ? launch_typed<T, 8, false, RS>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps, poll,
+                                                   passes, nstiles, order, ctas)
+                   : launch_typed<T, 4, false, RS>(I, ntiles, erode, ring, ws, s, max_visits, max_iters, resweeps, poll,
+                                                   passes, nstiles, order, ctas);
 }
+
 }  // namespace
 
 cudaError_t recon_launch_batch(int dtype, const Imgs& I, int ntiles, int conn, bool erode, bool ring, void* ws,
-                               cudaStream_t s, int max_visits, int max_iters, int resweeps, long long poll_limit) {
+                               cudaStream_t s, int max_visits, int max_iters, int resweeps, long long poll_limit,
+                               int passes, int nstiles, int order, long long total_px, int ctas) {
+  if (!I.d) {
+    nstiles = recon_stiles(dtype, I.one.H, I.one.W);
+    total_px = (long long)I.one.H * I.one.W;
+  }
+  const Schedule sc = tuned_schedule(dtype, conn, erode, I.d != nullptr, I.d ? total_px / (I.n > 0 ? I.n : 1) : total_px);
+  passes = passes > 0 ? passes : passes < 0 ? 0 : sc.passes;
+  order = order > 0 ? order - 1 : sc.order;
+  ctas = ctas > 0 ? ctas : sc.ctas;
   switch (dtype) {
 #define NSGB_RECON_CASE(CODE, TYPE)                                                                           \
   case CODE:                                                                                                   \
     return resweeps > 0 ? dispatch_conn<TYPE, true>(I, ntiles, conn, erode, ring, ws, s, max_visits, max_iters,  \
-                                                    resweeps, poll_limit)                                       \
+                                                    resweeps, poll_limit, passes, nstiles, order, ctas)         \
                         : dispatch_conn<TYPE, false>(I, ntiles, conn, erode, ring, ws, s, max_visits, max_iters, \
-                                                     resweeps, poll_limit);
+                                                     resweeps, poll_limit, passes, nstiles, order, ctas);
     NSGB_RECON_CASE(NSGB_U8, uint8_t)
     NSGB_RECON_CASE(NSGB_U16, uint16_t)
     NSGB_RECON_CASE(NSGB_I32, int32_t)
@@ -1012,12 +1387,14 @@ Img recon_image(int dtype, void* plane, const void* mask, int64_t H, int64_t W, 
   m.r_tiles_x = recon_tiles_x(dtype, W);
   m.r_tiles_y = recon_tiles_y(H);
   m.r_tile_base = 0;
+  m.r_tw = (dtype == NSGB_U8 || dtype == NSGB_U16) ? 64 : 32;
+  m.r_stile_base = 0;
   return m;
 }
 
 cudaError_t recon_launch(int dtype, void* out, const void* marker, const void* mask, int64_t H, int64_t W,
                          int64_t pitch, int conn, bool erode, bool ring, void* ws, cudaStream_t s, int max_visits,
-                         int max_iters, long long poll_limit) {
+                         int max_iters, long long poll_limit, int passes, int order, int ctas) {
   if (marker != out) {
     // The kernel works in place; start from a copy of the marker.
     const int esz = elem_size(dtype);
@@ -1028,7 +1405,7 @@ cudaError_t recon_launch(int dtype, void* out, const void* marker, const void* m
   I.n = 1;
   I.one = recon_image(dtype, out, mask, H, W, pitch);
   return recon_launch_batch(dtype, I, I.one.r_tiles_x * I.one.r_tiles_y, conn, erode, ring, ws, s, max_visits,
-                            max_iters, 0, poll_limit);
+                            max_iters, 0, poll_limit, passes, 0, order, 0, ctas);
 }
 
 }  // namespace nsgb

@@ -36,7 +36,9 @@ class NsgbError(RuntimeError):
 
 class Opts(C.Structure):
     _fields_ = [("sync", C.c_int), ("max_visits_per_tile", C.c_int), ("max_visit_iters", C.c_int),
-                ("queue_poll_limit", C.c_int), ("reserved", C.c_int * 4), ("recon_event_begin", C.c_void_p),
+                ("queue_poll_limit", C.c_int), ("recon_passes", C.c_int), ("recon_order", C.c_int),
+                ("recon_ctas_per_sm", C.c_int), ("reserved", C.c_int * 1),
+                ("recon_event_begin", C.c_void_p),
                 ("recon_event_end", C.c_void_p)]
 
 

@@ -63,7 +63,14 @@ typedef struct {
   int queue_poll_limit; /* reconstruction: polls a warp makes on the tile queue before it gives
                            up with NSGB_ERR_TIMEOUT (0 = default, about 2 s of polling); a small
                            value makes an idle warp's wait run out, for testing that path */
-  int reserved[4];
+  int recon_passes; /* reconstruction: streaming passes over all tiles before the work queue
+                       (> 0 that many, < 0 none, 0 the library's tuned default) */
+  int recon_order;  /* reconstruction: initial order of the work queue when it starts with every
+                       tile (1 raster, 2 checkerboard, 3 four colours; 0 the tuned default) */
+  int recon_ctas_per_sm; /* reconstruction: CTAs of 4 tile workers per SM for the work queue (1 .. 4;
+                            0 the tuned default).  Fewer workers waste fewer visits where only a
+                            front of tiles has work, as in hole filling */
+  int reserved[1];
   /* Optional CUDA events (cudaEvent_t) recorded on the call's stream immediately before and
    * after the reconstruction kernel (nsgb_imreconstruct, nsgb_chain), for timing it alone. */
   void* recon_event_begin;
