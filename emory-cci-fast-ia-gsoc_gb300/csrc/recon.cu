@@ -289,60 +289,73 @@ __device__ __forceinline__ void row_to_col(uint32_t (&O)[32], uint32_t* xp, int 
   __syncwarp();
 }
 
-// Row pass on the row layout: left-to-right then right-to-left clamp propagation.
-// f_j(v) = min(max(v, o_j), m_j).  For E = 2 each row is split over two lanes; the composed
-// clamps (lo, hi) of each half carry the value that enters the other half.  Both directions'
-// compositions are taken from the values before the pass, in one loop (independent chains):
-// the value flowing right-to-left out of the right half needs no left-to-right update, since a
-// value that went right and comes back left is bounded by the one that never left.
+// Change tracking.  Values only ever rise during the sweeps, so for u8 (two 16-bit lanes per
+// word, each at most 255) the warp-wide sum of all pixels changes if and only if some pixel
+// changed: 32 words per lane sum to at most 32 * 255 per 16-bit lane, so nothing carries from
+// the low lane of the sum into the high one, and the total does not depend on the layout.  The
+// other types compare every word (xor / or), which costs about four times the instructions.
 template <typename T>
-__device__ __forceinline__ uint32_t row_pass(uint32_t (&O)[32], const uint32_t* mh, const WarpBuf& B, int lane) {
+struct SumTrack { static constexpr bool value = false; };
+template <>
+struct SumTrack<uint8_t> { static constexpr bool value = true; };
+
+template <typename T>
+__device__ __forceinline__ uint32_t tile_sum(const uint32_t (&O)[32]) {
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < 32; i += 2) s += O[i] + O[i + 1];
+  s = (s & 0xFFFFu) + (s >> 16);
+  return __reduce_add_sync(NSGB_FULL, s);
+}
+
+// Row pass on the row layout: left-to-right then right-to-left clamp propagation,
+// f_j(v) = min(max(v, o_j), m_j).  For E = 2 each row is split over two lanes (columns 0..31 in
+// lane q, 32..63 in lane q + 16).  The value entering a half across that seam is the other
+// half's current boundary word (before the pass for the left-to-right scan, after it for the
+// right-to-left one), so both halves scan at once.  That is a valid update (it only uses actual
+// values), but not necessarily a complete one: `exact` reports whether the seam is stable after
+// the pass, i.e. whether neither boundary pixel can raise the other.  Only then is the state
+// after the pass stable along every row (each half's two scans leave it stable inside the half
+// and against the constant halo carries).  If the pass changes nothing, its seam inputs were the
+// final values, so it is exact as well.  TRACK: return the xor / or change word.
+template <typename T, bool TRACK>
+__device__ __forceinline__ uint32_t row_pass(uint32_t (&O)[32], const uint32_t* mh, const WarpBuf& B, int lane,
+                                             bool& exact) {
   using P = Px<T>;
   uint32_t acc = 0;
   if constexpr (P::E == 2) {
     const int q = lane & 15, half = lane >> 4;
-    uint32_t lo = P::LOW, hi = P::HIGH, lo2 = P::LOW, hi2 = P::HIGH;
-#pragma unroll
-    for (int j = 0; j < 32; j += 2) {
-      const uint2 m = lds2(mh + lane * kS + j);
-      lo = P::vmin(P::vmax(lo, O[j]), m.x);
-      hi = P::vmin(P::vmax(hi, O[j]), m.x);
-      lo = P::vmin(P::vmax(lo, O[j + 1]), m.y);
-      hi = P::vmin(P::vmax(hi, O[j + 1]), m.y);
-      const uint2 m2 = lds2(mh + lane * kS + 30 - j);
-      lo2 = P::vmin(P::vmax(lo2, O[31 - j]), m2.y);
-      hi2 = P::vmin(P::vmax(hi2, O[31 - j]), m2.y);
-      lo2 = P::vmin(P::vmax(lo2, O[30 - j]), m2.x);
-      hi2 = P::vmin(P::vmax(hi2, O[30 - j]), m2.x);
-    }
     const uint32_t carry_l = P::pack(B.hl[2 * q], B.hl[2 * q + 1]);
     const uint32_t carry_r = P::pack(B.hr[2 * q], B.hr[2 * q + 1]);
-    const uint32_t ex_l = P::vmin(P::vmax(carry_l, lo), hi);     // leaves the left half rightwards
-    const uint32_t ex_r = P::vmin(P::vmax(carry_r, lo2), hi2);   // leaves the right half leftwards
-    const uint32_t from0 = __shfl_up_sync(NSGB_FULL, ex_l, 16);
-    const uint32_t from1 = __shfl_down_sync(NSGB_FULL, ex_r, 16);
-    uint32_t v = half ? from0 : carry_l;
+    const uint32_t seam_l = __shfl_sync(NSGB_FULL, O[31], q);  // left half's last word, before the pass
+    uint32_t v = half ? seam_l : carry_l;
 #pragma unroll
     for (int j = 0; j < 32; j += 2) {
       const uint2 m = lds2(mh + lane * kS + j);
       const uint32_t n0 = P::vmin(P::vmax(O[j], v), m.x);
       const uint32_t n1 = P::vmin(P::vmax(O[j + 1], n0), m.y);
-      acc |= (n0 ^ O[j]) | (n1 ^ O[j + 1]);
+      if constexpr (TRACK) acc |= (n0 ^ O[j]) | (n1 ^ O[j + 1]);
       O[j] = n0;
       O[j + 1] = n1;
       v = n1;
     }
-    v = half ? carry_r : from1;
+    const uint32_t seam_r = __shfl_sync(NSGB_FULL, O[0], q + 16);  // right half's first word, after it
+    v = half ? carry_r : seam_r;
 #pragma unroll
     for (int j = 30; j >= 0; j -= 2) {
       const uint2 m = lds2(mh + lane * kS + j);
       const uint32_t n1 = P::vmin(P::vmax(O[j + 1], v), m.y);
       const uint32_t n0 = P::vmin(P::vmax(O[j], n1), m.x);
-      acc |= (n0 ^ O[j]) | (n1 ^ O[j + 1]);
+      if constexpr (TRACK) acc |= (n0 ^ O[j]) | (n1 ^ O[j + 1]);
       O[j] = n0;
       O[j + 1] = n1;
       v = n0;
     }
+    // seam test: can the word across the seam raise this lane's boundary word?
+    const uint32_t own = half ? O[0] : O[31];
+    const uint32_t other = __shfl_xor_sync(NSGB_FULL, own, 16);
+    const uint32_t own_m = mh[lane * kS + (half ? 0 : 31)];
+    exact = !__any_sync(NSGB_FULL, P::vmax(own, P::vmin(other, own_m)) != own);
   } else {
     uint32_t v = B.hl[lane];
 #pragma unroll
@@ -350,7 +363,7 @@ __device__ __forceinline__ uint32_t row_pass(uint32_t (&O)[32], const uint32_t* 
       const uint2 m = lds2(mh + lane * kS + j);
       const uint32_t n0 = P::vmin(P::vmax(O[j], v), m.x);
       const uint32_t n1 = P::vmin(P::vmax(O[j + 1], n0), m.y);
-      acc |= (n0 ^ O[j]) | (n1 ^ O[j + 1]);
+      if constexpr (TRACK) acc |= (n0 ^ O[j]) | (n1 ^ O[j + 1]);
       O[j] = n0;
       O[j + 1] = n1;
       v = n1;
@@ -361,29 +374,33 @@ __device__ __forceinline__ uint32_t row_pass(uint32_t (&O)[32], const uint32_t* 
       const uint2 m = lds2(mh + lane * kS + j);
       const uint32_t n1 = P::vmin(P::vmax(O[j + 1], v), m.y);
       const uint32_t n0 = P::vmin(P::vmax(O[j], n1), m.x);
-      acc |= (n0 ^ O[j]) | (n1 ^ O[j + 1]);
+      if constexpr (TRACK) acc |= (n0 ^ O[j]) | (n1 ^ O[j + 1]);
       O[j] = n0;
       O[j + 1] = n1;
       v = n0;
     }
+    exact = true;
   }
   return acc;
 }
 
-// What a row of the column layout gives the row below (or above): each pixel itself, and for
-// 8-connectivity its left and right neighbours.  The shuffles return the lane's own word at
-// lanes 0 and 31; the neighbour read there instead of one beyond the tile edge is another
-// 8-neighbour of the target pixel (the pixel two columns over in the row of the source
-// word, or the pixel above it), so it adds nothing beyond the tile.
+// One step of a column pass: pixel word o (row i) against the new word of the row before it,
+// min(mask, max(o, prev and, for 8-connectivity, prev's left and right neighbours)).  max(o, prev)
+// is taken while the shuffles are in flight, so the chain from one row to the next is shuffle,
+// funnel shift, two max and one min.  The shuffles return the lane's own word at lanes 0 and 31;
+// the neighbour read there instead of one beyond the tile edge is another 8-neighbour of the
+// target pixel (the pixel two columns over in the row of the source word, or the pixel above
+// it), so it adds nothing beyond the tile.
 template <typename T, int CONN>
-__device__ __forceinline__ uint32_t dilate_row(uint32_t w) {
+__device__ __forceinline__ uint32_t col_step(uint32_t o, uint32_t prev, uint32_t m) {
   using P = Px<T>;
+  const uint32_t t = P::vmax(o, prev);
   if constexpr (CONN == 8) {
-    const uint32_t l = __shfl_up_sync(NSGB_FULL, w, 1);
-    const uint32_t r = __shfl_down_sync(NSGB_FULL, w, 1);
-    return P::vmax(w, P::vmax(P::from_left(l, w), P::from_right(w, r)));
+    const uint32_t l = __shfl_up_sync(NSGB_FULL, prev, 1);
+    const uint32_t r = __shfl_down_sync(NSGB_FULL, prev, 1);
+    return P::vmin(P::vmax(t, P::vmax(P::from_left(l, prev), P::from_right(prev, r))), m);
   } else {
-    return w;
+    return P::vmin(t, m);
   }
 }
 
@@ -391,28 +408,73 @@ __device__ __forceinline__ uint32_t dilate_row(uint32_t w) {
 // previous row's new values (and their left/right neighbours for 8-connectivity).  The halo
 // columns' contributions (diagonals and corners included) enter through the row pass's
 // carries, so the first and last lanes see nothing beyond the tile here.
-template <typename T, int CONN>
+//
+// The rows are scanned as kColChains interleaved chains of 32 / kColChains rows each, so that
+// the dependent steps of one chain (shuffle, funnel shift, max, min) overlap those of the others.
+// A chain that starts inside the tile takes the value of the row before it as it was before the
+// pass (top-down) or after the top-down scan (bottom-up).  That is a valid update but may leave a
+// seam between chains unstable; a pass that changes nothing has used the final values
+// throughout, and the sweep loop only ends on such a pass.
+#ifndef NSGB_COL_CHAINS
+#define NSGB_COL_CHAINS 2
+#endif
+constexpr int kColChains = NSGB_COL_CHAINS;
+
+// 4-connectivity only: are the seams between the chains stable after a column pass, i.e. can
+// no row at a seam raise the row across it?  (The 4-connected sweep loop may end on an unchanged
+// row pass, which needs the column pass before it to have left every column stable.)
+template <typename T>
+__device__ __forceinline__ bool col_seams_stable(const uint32_t (&O)[32], const WarpBuf& B, int lane) {
+  using P = Px<T>;
+  constexpr int L = 32 / kColChains;
+  bool ok = true;
+#pragma unroll
+  for (int k = 1; k < kColChains; ++k) {
+    const int i = k * L;  // the seam between rows i - 1 and i (i is even)
+    const uint32_t m_above = lds2(B.mv + lane * kS + i - 2).y;  // mask of row i - 1
+    const uint32_t m_below = lds2(B.mv + lane * kS + i).x;      // mask of row i
+    ok &= P::vmax(O[i], P::vmin(O[i - 1], m_below)) == O[i];
+    ok &= P::vmax(O[i - 1], P::vmin(O[i], m_above)) == O[i - 1];
+  }
+  return __all_sync(NSGB_FULL, ok);
+}
+
+template <typename T, int CONN, bool TRACK>
 __device__ __forceinline__ uint32_t col_pass(uint32_t (&O)[32], const WarpBuf& B, uint32_t top, uint32_t bot,
                                              int lane) {
-  using P = Px<T>;
+  constexpr int NC = kColChains, L = 32 / NC;
   uint32_t acc = 0;
-  uint32_t up = top;
+  uint32_t up[NC];
+  up[0] = top;
 #pragma unroll
-  for (int i = 0; i < 32; ++i) {
-    const uint32_t m = (i & 1) ? lds2(B.mv + lane * kS + i - 1).y : lds2(B.mv + lane * kS + i).x;
-    const uint32_t n = P::vmin(P::vmax(O[i], dilate_row<T, CONN>(up)), m);
-    acc |= n ^ O[i];
-    O[i] = n;
-    up = n;
+  for (int k = 1; k < NC; ++k) up[k] = O[k * L - 1];
+#pragma unroll
+  for (int s = 0; s < L; ++s) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      const int i = k * L + s;
+      const uint32_t m = (i & 1) ? lds2(B.mv + lane * kS + i - 1).y : lds2(B.mv + lane * kS + i).x;
+      const uint32_t n = col_step<T, CONN>(O[i], up[k], m);
+      if constexpr (TRACK) acc |= n ^ O[i];
+      O[i] = n;
+      up[k] = n;
+    }
   }
-  uint32_t dn = bot;
+  uint32_t dn[NC];
+  dn[NC - 1] = bot;
 #pragma unroll
-  for (int i = 31; i >= 0; --i) {
-    const uint32_t m = (i & 1) ? lds2(B.mv + lane * kS + i - 1).y : lds2(B.mv + lane * kS + i).x;
-    const uint32_t n = P::vmin(P::vmax(O[i], dilate_row<T, CONN>(dn)), m);
-    acc |= n ^ O[i];
-    O[i] = n;
-    dn = n;
+  for (int k = 0; k < NC - 1; ++k) dn[k] = O[(k + 1) * L];
+#pragma unroll
+  for (int s = 0; s < L; ++s) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      const int i = (k + 1) * L - 1 - s;
+      const uint32_t m = (i & 1) ? lds2(B.mv + lane * kS + i - 1).y : lds2(B.mv + lane * kS + i).x;
+      const uint32_t n = col_step<T, CONN>(O[i], dn[k], m);
+      if constexpr (TRACK) acc |= n ^ O[i];
+      O[i] = n;
+      dn[k] = n;
+    }
   }
   return acc;
 }
@@ -428,6 +490,58 @@ __device__ __forceinline__ void halo_carries(WarpBuf& B, int lane) {
   B.hl[lane] = hl;
   B.hr[lane] = hr;
   __syncwarp();
+}
+
+// Sweeps a tile in registers (column layout) to its local fixed point: a row pass, then a
+// column pass, until a column pass changes nothing after an exact row pass (the state is then
+// stable along rows and along columns, diagonals included).  With 4-connectivity both passes
+// are idempotent, so a row pass that changes nothing after a column pass ends it too.  Returns
+// the number of column passes; a change of any value sets a bit of `any_change` in some lane.
+// After `max_iters` column passes the status word gets kDevNotConverged.
+template <typename T, int CONN>
+__device__ __forceinline__ int sweep_tile(uint32_t (&O)[32], WarpBuf& B, uint32_t topv, uint32_t botv, int lane,
+                                          int max_iters, int* status, uint32_t& any_change) {
+  constexpr int E = Px<T>::E;
+  constexpr bool SUM = SumTrack<T>::value;
+  uint32_t total = 0, total0 = 0;
+  if constexpr (SUM) total0 = total = tile_sum<T>(O);
+  int it = 0;
+  bool col_exact = true;  // the last column pass left every column stable (4-connectivity)
+  for (;;) {
+    col_to_row<E>(O, B.xp, lane);
+    bool exact;
+    const uint32_t racc = row_pass<T, !SUM>(O, B.mh, B, lane, exact);
+    bool rch = true;
+    if constexpr (SUM) {
+      const uint32_t s = tile_sum<T>(O);
+      rch = s != total;
+      total = s;
+    } else {
+      any_change |= racc;
+      if constexpr (CONN == 4) rch = __any_sync(NSGB_FULL, racc != 0);
+    }
+    row_to_col<E>(O, B.xp, lane);
+    if (CONN == 4 && it > 0 && !rch && col_exact) break;
+    const uint32_t acc = col_pass<T, CONN, !SUM>(O, B, topv, botv, lane);
+    if constexpr (CONN == 4 && kColChains > 1) col_exact = col_seams_stable<T>(O, B, lane);
+    bool cch;
+    if constexpr (SUM) {
+      const uint32_t s = tile_sum<T>(O);
+      cch = s != total;
+      total = s;
+    } else {
+      any_change |= acc;
+      cch = __any_sync(NSGB_FULL, acc != 0);
+    }
+    ++it;
+    if (!cch && exact) break;
+    if (it >= max_iters) {
+      if (lane == 0) set_status(status, kDevNotConverged);
+      break;
+    }
+  }
+  if constexpr (SUM) any_change |= total != total0 ? 1u : 0u;
+  return it;
 }
 
 // Image fields: from the kernel parameters for a single image (constant bank, nothing pinned
@@ -462,21 +576,19 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   const int xl = x0 + E * lane;
   const uint32_t fx = flip ? P::FLIP : 0u;
 
-  // The mask never changes: an interior tile's mask loads are issued before the fence below,
-  // so that their latency overlaps it.
+  // The caller has taken the tile with an acquire exchange (lane 0); the warp barrier orders
+  // every lane's loads after it.
   uint32_t O[32], M[32];
+  __syncwarp();
+  PROF_MARK(1);
+
+  // All loads of the tile and its halo are issued before any is used, so the visit waits for
+  // about one L2 round trip instead of a chain of them.
   if (fast) {
     const char* mp = (const char*)mask + (int64_t)y0 * pitch + (int64_t)xl * sizeof(T);
 #pragma unroll
     for (int i = 0; i < 32; ++i) M[i] = fast_word<T>(mp + i * pitch, false, fx, pairs);
   }
-  // The caller has set the tile RUNNING; order that before reading the neighbours' pixels.
-  __syncwarp();
-  __threadfence();
-  PROF_MARK(1);
-
-  // All loads of the tile and its halo are issued before any is used, so the visit waits for
-  // about one L2 round trip instead of a chain of them.
   if (fast) {  // interior tile: straight-line loads through running row pointers, no checks
     const char* op = (const char*)src + (int64_t)y0 * pitch + (int64_t)xl * sizeof(T);
 #pragma unroll
@@ -559,27 +671,7 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   PROF_MARK(2);
 #pragma unroll 1
   for (int round = 0;; ++round) {
-  // Sweep to the local fixed point.  A row pass is idempotent (exact left / right scans); with
-  // 4-connectivity so is a column pass, so once a row pass after a column pass changes nothing
-  // the tile is stable and the final column pass can be skipped.  With 8-connectivity the
-  // diagonals make the column pass order-dependent and the loop ends on an unchanged column
-  // pass.
-  int it = 0;
-  for (;;) {
-    col_to_row<E>(O, B.xp, lane);
-    const uint32_t racc = row_pass<T>(O, B.mh, B, lane);
-    any_change |= racc;
-    row_to_col<E>(O, B.xp, lane);
-    if (CONN == 4 && it > 0 && !__any_sync(NSGB_FULL, racc != 0)) break;
-    const uint32_t acc = col_pass<T, CONN>(O, B, topv, botv, lane);
-    any_change |= acc;
-    ++it;
-    if (!__any_sync(NSGB_FULL, acc != 0)) break;
-    if (it >= a.max_iters) {
-      if (lane == 0) set_status(a.c.status, kDevNotConverged);
-      break;
-    }
-  }
+  const int it = sweep_tile<T, CONN>(O, B, topv, botv, lane, a.max_iters, a.c.status, any_change);
   if (lane == 0) {
     atomicAdd(&a.c.stats[0], 1);
     atomicAdd(&a.c.stats[1], it);
@@ -658,7 +750,7 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
       if (P::lt(B.rv[33], P::emin(B.c1[31], B.rm[33]))) dirs |= 1u << 8;
     }
   }
-  __threadfence();
+  // The warp barrier orders every lane's stores before the release atomics below.
   __syncwarp();
   PROF_MARK(5);
   // Lane d marks the neighbour in direction d (one copy of the marking code, up to eight
@@ -682,10 +774,10 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
     // (without re-sweeps the loop body runs once: kept separate so that the compiler emits
     // one copy of the sweep code)
     if (lane == 0) {
-      if (atomicCAS(&a.c.state[t], kRunning, kIdle) == kRunning) {
+      if (atom_cas_acq_rel(&a.c.state[t], kRunning, kIdle) == kRunning) {
         pending_release(a.c);
       } else {
-        atomicExch(&a.c.state[t], kQueued);
+        atom_exch_acq_rel(&a.c.state[t], kQueued);
         atomicAdd(&a.c.stats[2], 1);
         queue_push(a.c, t);
       }
@@ -695,24 +787,23 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   }
   int st = 0;
   if (lane == 0) {
-    if (atomicCAS(&a.c.state[t], kRunning, kIdle) == kRunning) {
+    if (atom_cas_acq_rel(&a.c.state[t], kRunning, kIdle) == kRunning) {
       pending_release(a.c);
       st = 0;
     } else if (round < a.resweeps) {
-      atomicExch(&a.c.state[t], kRunning);
+      atom_exch_acq_rel(&a.c.state[t], kRunning);
       atomicAdd(&a.c.stats[3], 1);
       st = 1;
     } else {
-      atomicExch(&a.c.state[t], kQueued);
+      atom_exch_acq_rel(&a.c.state[t], kQueued);
       atomicAdd(&a.c.stats[2], 1);
       queue_push(a.c, t);
       st = 0;
     }
   }
   if (__shfl_sync(NSGB_FULL, st, 0) == 0) return;
-  // order the state change before reading the halo again, as at the start of a visit
+  // the acquire exchange above orders reading the halo again after the markers' stores
   __syncwarp();
-  __threadfence();
   {
     const uint32_t tv = load_word<T>(src, pitch, y0 - 1, xl, H, W, fast_top, coh, flip);
     const uint32_t bv = load_word<T>(src, pitch, y0 + kRows, xl, H, W, fast_bot, coh, flip);
@@ -866,22 +957,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs& a, WarpBuf& B, int t, 
   }
   __syncwarp();
 
-  int it = 0;
-  for (;;) {
-    col_to_row<E>(O, B.xp, lane);
-    const uint32_t racc = row_pass<T>(O, B.mh, B, lane);
-    any_change |= racc;
-    row_to_col<E>(O, B.xp, lane);
-    if (CONN == 4 && it > 0 && !__any_sync(NSGB_FULL, racc != 0)) break;
-    const uint32_t acc = col_pass<T, CONN>(O, B, topv, botv, lane);
-    any_change |= acc;
-    ++it;
-    if (!__any_sync(NSGB_FULL, acc != 0)) break;
-    if (it >= a.max_iters) {
-      if (lane == 0) set_status(a.status, kDevNotConverged);
-      break;
-    }
-  }
+  sweep_tile<T, CONN>(O, B, topv, botv, lane, a.max_iters, a.status, any_change);
 
   if (__any_sync(NSGB_FULL, any_change != 0)) {
     if (fast) {
@@ -1025,7 +1101,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4) recon_kernel(Args a) {
       if (k < (1u << 20)) g_prof_times[k] = global_ns();
     }
 #endif
-    if (lane == 0) atomicExch(&a.c.state[t], kRunning);
+    if (lane == 0) atom_exch_acquire(&a.c.state[t], kRunning);
     visit<T, CONN, BATCH, RS>(a, B, t, lane);
 #ifdef NSGB_RECON_PROFILE
     const long long _pe = clock64();

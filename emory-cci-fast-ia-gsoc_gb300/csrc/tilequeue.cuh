@@ -92,32 +92,43 @@ __device__ __forceinline__ void pending_release(const Ctl& c) {
   if (atomicSub(c.pending, 1) == 1) atomicExch(c.done, 1);
 }
 
-// Claims a neighbour whose state the first compare-and-swap found running or running-dirty:
-// a running neighbour is marked dirty (its owner re-runs it).  A neighbour that went idle in
-// between is claimed with a fresh idle -> queued compare-and-swap; it is never pushed while its
-// state still reads idle, which would let a second marker push it again and two warps run the
-// same tile at once.  Returns true when this call queued it.  Rolled and out of line: the
-// retries are rare, and the visit's instruction stream stays short.
-__device__ __noinline__ bool mark_claim_retry(const Ctl& c, int nt, int s) {
-#pragma unroll 1
-  for (int guard = 0; guard < 1024; ++guard) {
-    if (s == kIdle) return true;
-    if (s == kQueued || s == kRunningDirty) return false;  // will load after our stores
-    s = atomicCAS(&c.state[nt], kRunning, kRunningDirty);
-    if (s == kRunning) return false;  // its owner re-runs it
-    s = atomicCAS(&c.state[nt], kIdle, kQueued);
-  }
-  set_status(c.status, kDevTimeout);
-  return false;
+// Tile states and the memory order of tile visits.  Every change of a tile's state is an atomic
+// read-modify-write, so all of them are totally ordered per tile.  A visit takes its tile with an
+// acquire exchange (QUEUED -> RUNNING) before it reads any pixel; a warp that stored pixels marks
+// a neighbour with a release `or 1` (IDLE -> QUEUED, RUNNING -> RUNNING_DIRTY, the others
+// unchanged), and releases its own tile with a release compare-and-swap.  For a visit V of tile
+// t and a marker U of t, either U's `or` comes before V's exchange in t's order -- then V's
+// acquire reads from U's release (or a later read-modify-write of the same sequence) and V's
+// loads see U's stores -- or after it, and then U sees RUNNING and the visit is run again.  No
+// fence is needed on either side.
+__device__ __forceinline__ int atom_or_release(int* p, int v) {
+  int old;
+  asm volatile("atom.release.gpu.global.or.b32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+__device__ __forceinline__ int atom_exch_acquire(int* p, int v) {
+  int old;
+  asm volatile("atom.acquire.gpu.global.exch.b32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+__device__ __forceinline__ int atom_exch_acq_rel(int* p, int v) {
+  int old;
+  asm volatile("atom.acq_rel.gpu.global.exch.b32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+__device__ __forceinline__ int atom_cas_acq_rel(int* p, int cmp, int v) {
+  int old;
+  asm volatile("atom.acq_rel.gpu.global.cas.b32 %0, [%1], %2, %3;" : "=r"(old) : "l"(p), "r"(cmp), "r"(v) : "memory");
+  return old;
 }
 
-// A neighbour's values may have become stale: make sure it (re)reads them.  The common case
-// (an idle neighbour) takes one atomic.
+// A neighbour's values may have become stale: make sure it (re)reads them.  One release `or`:
+// an idle neighbour becomes queued (and this call pushes it), a running one becomes
+// running-dirty (its owner runs it again), a queued one will load after the stores that the
+// release orders before the `or`.  The caller's pixel stores are ordered before it by a warp
+// barrier.
 __device__ __forceinline__ void mark_tile(const Ctl& c, int nt) {
-  const int s = atomicCAS(&c.state[nt], kIdle, kQueued);
-  bool queued = s == kIdle;
-  if (!queued && s != kQueued && s != kRunningDirty) queued = mark_claim_retry(c, nt, s);
-  if (queued) {
+  if (atom_or_release(&c.state[nt], 1) == kIdle) {
     atomicAdd(c.pending, 1);
     queue_push(c, nt);
   }
