@@ -1,7 +1,8 @@
 // Image tables: every kernel works on a batch of images (a single-image call is a batch of
 // one).  Work items of all images (reconstruction tiles, labelling tiles, rank blocks, rows)
-// are numbered consecutively; each image records where its range starts, and a kernel finds
-// the image of a work item with a binary search over those starts.
+// are numbered consecutively; each image records where its range starts.  Tiles find their
+// image through a per-tile map; other work items with a binary search over the range starts
+// (row kernels look it up once per range of rows).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -34,6 +35,12 @@ struct Imgs {
   const Img* d;  // device table (batches), or null: a single image passed in `one`
   int n;
   Img one;       // the image itself when d == null (kernel parameter, no table needed)
+  // Batches: the image of every reconstruction tile and of every labelling tile (written by
+  // nsgb_batch_prepare), so that a work item finds its image with one load.  A stack of equal
+  // images has no maps; its tiles per image divide the tile index instead.
+  const int* r_img;
+  const int* c_img;
+  int r_per, c_per;  // stack: reconstruction / labelling tiles per image (0: not a stack)
 };
 
 __device__ __forceinline__ Img img_at(const Imgs& I, int i) { return I.d ? I.d[i] : I.one; }
@@ -49,6 +56,15 @@ __device__ __forceinline__ int img_of(const Imgs& I, int key, F field) {
     else hi = mid - 1;
   }
   return lo;
+}
+
+// Image of reconstruction tile / labelling tile `t` (tile map, stack division, or the search).
+template <typename F>
+__device__ __forceinline__ int img_of_tile(const Imgs& I, int t, const int* map, int per, F field) {
+  if (!I.d) return 0;
+  if (map) return __ldg(map + t);
+  if (per > 0) return t / per;
+  return img_of(I, t, field);
 }
 
 struct RTileBase { __device__ int operator()(const Img& m) const { return m.r_tile_base; } };

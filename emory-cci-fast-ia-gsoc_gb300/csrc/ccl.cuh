@@ -133,7 +133,7 @@ struct TileAt {
 };
 __device__ __forceinline__ TileAt tile_at(const Imgs& I, int b) {
   TileAt t;
-  t.m = img_at(I, img_of(I, b, CTileBase()));
+  t.m = img_at(I, img_of_tile(I, b, I.c_img, I.c_per, CTileBase()));
   const int lt = b - t.m.c_tile_base;
   const int ty = lt / t.m.c_tiles_x;
   t.x0 = (lt - ty * t.m.c_tiles_x) * kTile;

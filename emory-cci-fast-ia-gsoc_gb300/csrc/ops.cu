@@ -11,6 +11,7 @@
 #include <cmath>
 #include <limits>
 #include <type_traits>
+#include <algorithm>
 #include <vector>
 
 #include "../../include/nsgb.h"
@@ -472,7 +473,7 @@ Plan single_plan(int dtype, void* plane, const void* aux, int64_t H, int64_t W, 
 }
 
 struct WsSizes {
-  size_t recon, L, A, R, roots, bits, tmp, wpre, F, table, total;
+  size_t recon, L, A, R, roots, bits, tmp, wpre, F, table, maps, total;
 };
 
 WsSizes ws_sizes(const BatchTotals& t) {
@@ -487,7 +488,8 @@ WsSizes ws_sizes(const BatchTotals& t) {
   z.wpre = align256(sizeof(int) * 32 * (size_t)t.blocks);
   z.F = align256((size_t)t.px);
   z.table = t.n > 1 ? align256(sizeof(Img) * (size_t)t.n) : 0;
-  z.total = z.recon + z.L + z.A + z.R + z.roots + z.bits + z.tmp + z.wpre + z.F + z.table;
+  z.maps = t.n > 1 ? align256(sizeof(int) * ((size_t)t.r_tiles + (size_t)t.c_tiles)) : 0;
+  z.total = z.recon + z.L + z.A + z.R + z.roots + z.bits + z.tmp + z.wpre + z.F + z.table + z.maps;
   return z;
 }
 
@@ -505,6 +507,8 @@ struct Ws {
   int* wpre;     // 32 per rank block
   uint8_t* F;
   Img* table;
+  int* r_img;  // batches: image of every reconstruction tile
+  int* c_img;  // batches: image of every labelling tile
   size_t bits_bytes;
   ccl::Forest forest(bool areas) const { return ccl::Forest{L, areas ? A : nullptr, roots, nroots}; }
 };
@@ -536,6 +540,9 @@ Ws carve(void* ws, const BatchTotals& t) {
   w.F = (uint8_t*)p;
   p += z.F;
   w.table = t.n > 1 ? (Img*)p : nullptr;
+  p += z.table;
+  w.r_img = t.n > 1 ? (int*)p : nullptr;
+  w.c_img = t.n > 1 ? w.r_img + t.r_tiles : nullptr;
   return w;
 }
 
@@ -1154,6 +1161,8 @@ nsgb_status batch_plan(const nsgb_batch* b, Plan* P, Ws* w) {
   P->I = Imgs{};
   P->I.n = t.n;
   P->I.d = w->table;
+  P->I.r_img = w->r_img;
+  P->I.c_img = w->c_img;
   return NSGB_OK;
 }
 
@@ -1176,8 +1185,19 @@ nsgb_status nsgb_batch_prepare(int dtype, const nsgb_tile* tiles, int n_tiles, v
   nsgb_status st = check_ws_bytes(ws, ws_bytes, nsgb_batch_workspace_size(dtype, tiles, n_tiles));
   if (st != NSGB_OK) return st;
   Ws w = carve(ws, table_totals(t));
-  // Synchronous copy: the host array goes away when this returns.
+  // The tile maps: image of every reconstruction tile, then of every labelling tile.
+  std::vector<int> maps((size_t)t.r_tiles + (size_t)t.c_tiles);
+  for (int i = 0; i < (int)imgs.size(); ++i) {
+    const Img& m = imgs[i];
+    const int nr = m.r_tiles_x * m.r_tiles_y;
+    const int nc = m.c_tiles_x * ((m.H + ccl::kTile - 1) / ccl::kTile);
+    std::fill(maps.begin() + m.r_tile_base, maps.begin() + m.r_tile_base + nr, i);
+    std::fill(maps.begin() + t.r_tiles + m.c_tile_base, maps.begin() + t.r_tiles + m.c_tile_base + nc, i);
+  }
+  // Synchronous copies: the host arrays go away when this returns.
   if (cudaMemcpy(w.table, imgs.data(), sizeof(Img) * imgs.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return NSGB_ERR_CUDA;
+  if (cudaMemcpy(w.r_img, maps.data(), sizeof(int) * maps.size(), cudaMemcpyHostToDevice) != cudaSuccess)
     return NSGB_ERR_CUDA;
   memset(batch, 0, sizeof(*batch));
   batch->dtype = dtype;
@@ -1579,6 +1599,8 @@ cudaError_t stacked_plan(void* plane, const void* aux, int64_t batch, int64_t ro
   proto.aligned = proto.aligned && (stride % 4 == 0);
   P->I.one = proto;
   P->I.d = table;
+  P->I.r_per = P1.t.r_tiles;
+  P->I.c_per = P1.t.c_tiles;
   stack_table_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, s>>>(proto, (int)batch, stride, P1.t, table);
   return cudaGetLastError();
 }

@@ -553,7 +553,7 @@ __device__ __forceinline__ void visit(const Args& a, WarpBuf& B, int t, int lane
   using P = Px<T>;
   constexpr int E = P::E;
   constexpr int TW = 32 * E;
-  const int ii = BATCH ? img_of(a.I, t, RTileBase()) : 0;
+  const int ii = BATCH ? img_of_tile(a.I, t, a.I.r_img, a.I.r_per, RTileBase()) : 0;
   const int lt = t - IMF(r_tile_base);
   const int ty = lt / IMF(r_tiles_x), tx = lt - ty * IMF(r_tiles_x);
   const int y0 = ty * kRows, x0 = tx * TW;
@@ -864,7 +864,8 @@ __device__ __forceinline__ void pass_tile(const PassArgs& a, WarpBuf& B, int t, 
   constexpr int E = P::E;
   constexpr int TW = 32 * E;
   const bool shifted = a.oy != 0;
-  const int ii = BATCH ? (shifted ? img_of(a.I, t, RSTileBase()) : img_of(a.I, t, RTileBase())) : 0;
+  const int ii = BATCH ? (shifted ? img_of(a.I, t, RSTileBase()) : img_of_tile(a.I, t, a.I.r_img, a.I.r_per, RTileBase()))
+                       : 0;
   const Img& m = BATCH ? a.I.d[ii] : a.I.one;
   const int H = m.H, W = m.W;
   const int ntx = shifted ? (W + a.ox + TW - 1) / TW : m.r_tiles_x;
