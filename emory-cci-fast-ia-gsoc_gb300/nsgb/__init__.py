@@ -238,23 +238,30 @@ def bwareaopen2(image: torch.Tensor, labeled: bool, flatten: bool, minSize: int,
     return out, int(cnt.value)
 
 
-def bounding_boxes(labels: torch.Tensor, bgval: int = 0) -> torch.Tensor:
+def bounding_boxes(labels: torch.Tensor, bgval: int = 0, capacity: Optional[int] = None) -> torch.Tensor:
     """ConnComponents::boundingBox (ConnComponents.cpp:241-284) of an int32 label image on the
     device: int32 tensor (5, count) of label, min x, max x, min y, max y per label other than
-    `bgval`, in the order of each label's first pixel in raster order."""
+    `bgval`, in the order of each label's first pixel in raster order.
+
+    `capacity` bounds the labels the output is first sized for (default: 65536, or rows*cols if
+    smaller).  The call reports the number of labels; if it exceeds the capacity, the boxes are
+    computed again into an output of exactly that size, so the result is always complete."""
     _check_image(labels, "labels")
     if labels.dtype != torch.int32:
         raise NsgbError(2, "labels must be int32")
     lab = _contig(labels)
     rows, cols = lab.shape
     ws, nb = _ws(_ffi.OP_BOUNDING_BOX, _ffi.I32, rows, cols, lab.device)
-    cap = rows * cols
-    boxes = torch.empty((5, cap), dtype=torch.int32, device=lab.device)
-    cnt = C.c_int32(0)
-    st = lib.nsgb_bounding_boxes(lab.data_ptr(), rows, cols, _pitch(lab), int(bgval), boxes.data_ptr(), cap,
-                                 C.byref(cnt), None, ws, nb, _stream(), None)
-    _ffi.check(st, "bounding_boxes")
-    return boxes[:, :int(cnt.value)].contiguous()
+    cap = min(rows * cols, 65536 if capacity is None else max(1, int(capacity)))
+    while True:
+        boxes = torch.empty((5, cap), dtype=torch.int32, device=lab.device)
+        cnt = C.c_int32(0)
+        st = lib.nsgb_bounding_boxes(lab.data_ptr(), rows, cols, _pitch(lab), int(bgval), boxes.data_ptr(), cap,
+                                     C.byref(cnt), None, ws, nb, _stream(), None)
+        _ffi.check(st, "bounding_boxes")
+        if int(cnt.value) <= cap:
+            return boxes[:, :int(cnt.value)].contiguous()
+        cap = int(cnt.value)
 
 
 def threshold(image: torch.Tensor, thr: float) -> torch.Tensor:

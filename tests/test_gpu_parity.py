@@ -265,6 +265,17 @@ def test_bounding_boxes_random(nsgb, oracle):
     assert np.array_equal(to_np(nsgb.bounding_boxes(to_dev(lab), 7)), oracle.bounding_box(lab, 7))
 
 
+def test_bounding_boxes_capacity_retry(nsgb, oracle):
+    """An output sized below the number of labels is redone at the reported count."""
+    rng = np.random.default_rng(5)
+    img = ((rng.random((300, 400)) < 0.3) * 255).astype(np.uint8)
+    rel, n = oracle.bwlabel2(img, 8, True)
+    assert n > 100
+    exp = oracle.bounding_box(rel, 0)
+    for cap in (1, 17, n - 1, n, n + 5):
+        assert np.array_equal(to_np(nsgb.bounding_boxes(to_dev(rel), 0, capacity=cap)), exp), cap
+
+
 def test_bounding_boxes_chain_labels(nsgb, oracle):
     """The boxes of the chain's labelled output (HistologicalEntities.cpp:573 takes them after
     bwlabel2), on the inverted workload with thousands of components."""
