@@ -25,6 +25,8 @@ struct Img {
   int px_base;        // first pixel in the concatenated label planes
   int blk_base;       // first 1024-pixel rank block
   int row_base;       // first row in the concatenated row space
+  int b_base;         // first word of its bit planes (hole filling on bits)
+  int f_tile_base;    // first of its flood tiles (32 rows x 1024 pixels)
   // outputs of the chain (dense rows, may be null)
   uint8_t* fill;
   int32_t* labels;
@@ -72,6 +74,7 @@ struct CTileBase { __device__ int operator()(const Img& m) const { return m.c_ti
 struct BlkBase { __device__ int operator()(const Img& m) const { return m.blk_base; } };
 struct RowBase { __device__ int operator()(const Img& m) const { return m.row_base; } };
 struct PxBase { __device__ int operator()(const Img& m) const { return m.px_base; } };
+struct FTileBase { __device__ int operator()(const Img& m) const { return m.f_tile_base; } };
 struct REvenBase { __device__ int operator()(const Img& m) const { return m.r_even_base; } };
 struct ROddBase { __device__ int operator()(const Img& m) const { return m.r_tile_base - m.r_even_base; } };
 
@@ -99,6 +102,8 @@ struct RColBase {
 struct BatchTotals {
   int n;
   int64_t px;      // total pixels (< 2^31)
+  int64_t b_words; // words of one bit plane over all images (rows x ceil(cols / 32))
+  int f_tiles;     // flood tiles
   int r_tiles;     // reconstruction tiles
   int r_stiles;    // reconstruction tiles of the half-tile-shifted grid
   int r_even;      // reconstruction tiles of checkerboard colour 0

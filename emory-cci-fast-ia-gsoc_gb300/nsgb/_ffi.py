@@ -50,7 +50,8 @@ class Tile(C.Structure):
 class Batch(C.Structure):
     _fields_ = [("dtype", C.c_int), ("n", C.c_int), ("total_px", C.c_int64), ("recon_tiles", C.c_int),
                 ("label_tiles", C.c_int), ("rank_blocks", C.c_int), ("total_rows", C.c_int), ("max_cols", C.c_int),
-                ("max_perimeter", C.c_int), ("ws", C.c_void_p), ("ws_bytes", C.c_size_t), ("reserved", C.c_int * 8)]
+                ("max_perimeter", C.c_int), ("ws", C.c_void_p), ("ws_bytes", C.c_size_t), ("flood_tiles", C.c_int),
+                ("bit_words", C.c_int), ("reserved", C.c_int * 6)]
 
 
 def _load() -> C.CDLL:

@@ -270,7 +270,8 @@ typedef struct {
   int recon_tiles, label_tiles, rank_blocks, total_rows, max_cols, max_perimeter;
   void* ws;
   size_t ws_bytes;
-  int reserved[8];
+  int flood_tiles, bit_words;
+  int reserved[6];
 } nsgb_batch;
 
 /* Workspace bytes for a batch (total pixels must stay below 2^31). */

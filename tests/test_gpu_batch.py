@@ -39,6 +39,29 @@ def test_chain_batch_matches_single_tiles(nsgb, oracle, dtype):
         assert got["n_labels"] == exp["n_labels"] and got["n_kept"] == exp["n_kept"]
 
 
+@pytest.mark.parametrize("fill_conn", [4, 8])
+def test_chain_batch_hole_fill_edges(nsgb, oracle, fill_conn):
+    """The batch's bit-plane hole fill (a flood from outside each image): widths around the
+    32-pixel words and the 1024-pixel flood tiles, one-pixel images, heights around the 32-row
+    tiles, inverted tiles (the open class is the whole background, so the flood crosses every
+    image) and both fill connectivities, against the oracle tile by tile."""
+    import torch
+
+    sizes = [(31, 1023), (32, 1024), (33, 1025), (65, 2049), (1, 1), (1, 40), (40, 1), (100, 31), (100, 33),
+             (64, 3000), (95, 64), (257, 1100)]
+    tiles = _tiles("u8", sizes, 70)
+    # every other tile inverted: dark background, bright objects
+    tiles = [((255 - m).astype(np.uint8), np.maximum((255 - m).astype(np.int16) - 10, 0).astype(np.uint8))
+             if i % 2 else (m, k) for i, (m, k) in enumerate(tiles)]
+    res = nsgb.chain_batch([torch.from_numpy(k).cuda() for _, k in tiles],
+                           [torch.from_numpy(m).cuda() for m, _ in tiles], fill_conn=fill_conn)
+    for i, ((m, k), got) in enumerate(zip(tiles, res)):
+        exp = oracle.chain(k, m, fill_conn=fill_conn)
+        assert np.array_equal(got["fill"].cpu().numpy(), exp["fill"]), (i, sizes[i])
+        assert np.array_equal(got["labels"].cpu().numpy(), exp["labels"]), (i, sizes[i])
+        assert got["n_labels"] == exp["n_labels"] and got["n_kept"] == exp["n_kept"]
+
+
 @pytest.mark.parametrize("conn", [4, 8])
 def test_reconstruct_batch_matches_oracle(nsgb, oracle, conn):
     import torch
