@@ -16,8 +16,9 @@
 //     three ballots per row: a flood enters lane l from the left if lane l-1 ends flooded, or
 //     if lane l-1 is entirely open and a flood entered it, and the same add on the lane masks
 //     finds every lane such a chain reaches (and from the right, reversed);
-//   * column pass: top-down and bottom-up, each row seeded from the row before it (and its
-//     diagonal neighbours for 8-connectivity), then flooded along its runs.
+//   * column pass: top-down and bottom-up, each row flooded where the row before it is (or,
+//     for 8-connectivity, a diagonal neighbour of it) and the pixel is open: two operations per
+//     row and word, so the pass is a short chain; the runs are left to the next row pass.
 // It ends on a column pass that changes nothing.  The halo (the rows above and below, the pixel
 // columns left and right, each with its open and flooded bits) enters as constants; outside the
 // image everything is open and flooded.  Scheduling is the reconstruction's (tilequeue.cuh):
@@ -192,7 +193,7 @@ __device__ __forceinline__ void flood_visit(const FloodArgs& a, int t, int lane)
     uint32_t prev = ft;
 #pragma unroll
     for (int i = 0; i < 32; ++i) {
-      const uint32_t n = fill_runs(f[i] | spread_vertical<CONN>(prev, lane), p[i]);
+      const uint32_t n = f[i] | (spread_vertical<CONN>(prev, lane) & p[i]);
       cch |= n ^ f[i];
       f[i] = n;
       prev = n;
@@ -200,7 +201,7 @@ __device__ __forceinline__ void flood_visit(const FloodArgs& a, int t, int lane)
     prev = fb;
 #pragma unroll
     for (int i = 31; i >= 0; --i) {
-      const uint32_t n = fill_runs(f[i] | spread_vertical<CONN>(prev, lane), p[i]);
+      const uint32_t n = f[i] | (spread_vertical<CONN>(prev, lane) & p[i]);
       cch |= n ^ f[i];
       f[i] = n;
       prev = n;
