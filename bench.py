@@ -37,9 +37,31 @@ PKG = os.path.join(ROOT, "emory-cci-fast-ia-gsoc_gb300")
 sys.path.insert(0, PKG)
 
 METRIC = "imreconstruct+bwlabel MPix/s, uint8 4096², plain vs batched GPU; % of HBM peak"
-# recon init + recon, fill (local, merge, flatten, border seeds, output), label (local, merge,
-# flatten), rank (mark, count, scan, assign), label/area output: see csrc/ops.cu chain_impl
+# recon init + recon, fill (local, merge, flatten, border seeds, output; a batch: pack, flood seed,
+# flood seed finish, flood, output), label (local, merge, flatten), rank (mark, count, scan,
+# assign), label/area output: see csrc/ops.cu chain_impl.  A tuned schedule with streaming
+# passes replaces recon init by its passes and two seed kernels (tuned_passes below).
 KERNELS_PER_CHAIN = 15
+
+
+def tuned_passes(dtype, conn, batch, px):
+    """Streaming passes of the reconstruction's tuned schedule (tuning.json, compiled into the
+    library) for a call: 0 when the ring starts with every tile."""
+    try:
+        with open(os.path.join(PKG, "tuning.json")) as f:
+            entries = json.load(f)["entries"]
+    except (OSError, ValueError, KeyError):
+        return 0
+    for e in entries:
+        if (e["dtype"] == dtype and int(e["conn"]) == conn and not e["erode"] and bool(e["batch"]) == batch
+                and px <= int(e["max_px"])):
+            return int(e["passes"])
+    return 0
+
+
+def chain_kernels(dtype, batch, px):
+    p = tuned_passes(dtype, 8, batch, px)
+    return KERNELS_PER_CHAIN + (p + 1 if p > 0 else 0)
 RECON_BYTES_PER_PX = 3  # marker read + mask read + result write (u8)
 CHAIN_BYTES_PER_PX = 17  # recon 3 + threshold 2 + fill 2 + bwlabel 5 + bwareaopen 5
 
@@ -476,7 +498,7 @@ def run_nsgb(args):
             "path": "nsgb_chain C ABI, pinned host marker/mask in, labels + area mask out; steps alternate "
                     "between two streams with their own buffers, so one step's copies overlap the other's kernels",
         },
-        "gpu_launches": KERNELS_PER_CHAIN * args.steps,
+        "gpu_launches": chain_kernels("u8", False, args.size * args.size) * args.steps,
         "clocks": clk,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -660,25 +682,29 @@ def run_batched(args, dev, tiles_u8, dtype):
         "batched_graph_mpix_s": mp / (t_batch / 1e3), "batched_ms": t_batch,
         "speedup_vs_plain": t_plain / t_batch, "speedup_vs_plain_async": t_plain_async / t_batch,
         "batch_equals_single_tile": bool(same),
-        "gpu_launches_per_batch": KERNELS_PER_CHAIN,
+        "gpu_launches_per_batch": chain_kernels(dtype, True, total_px // max(1, n)),
     }
 
 
 def cpu_tile_parallel(tiles_u8, budget_tiles):
-    """The oracle chain, one tile per host thread, on the first `budget_tiles` tiles."""
+    """The reference's own CPU chain (oracle/_ref, built from its sources; the oracle's
+    restatement where that was not built), one tile per host thread, on the first
+    `budget_tiles` tiles."""
     from concurrent.futures import ThreadPoolExecutor
 
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
+    ref = oracle.ref_morph_available()
+    fn = oracle.ref_chain if ref else oracle.chain
     sample = tiles_u8[:budget_tiles]
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     with ThreadPoolExecutor(threads) as ex:
-        list(ex.map(lambda mk: oracle.chain(mk[1], mk[0]), sample))
+        list(ex.map(lambda mk: fn(mk[1], mk[0]), sample))
     dt = time.perf_counter() - t0
     px = sum(m.size for m, _ in sample)
-    return {"value": px / 1e6 / dt, "unit": "MPix/s", "cores": threads, "kind": "port",
+    return {"value": px / 1e6 / dt, "unit": "MPix/s", "cores": threads, "kind": "reference" if ref else "port",
             "sample": f"first {len(sample)} of the u8 tiles, one tile per thread, {dt:.1f} s"}
 
 
