@@ -10,8 +10,8 @@ One step = one pass of the chain over the tile.  `value` is the whole-job throug
 MPix/s with inputs already resident in HBM (marker reset and L2 flushed outside the timed
 events before every step); `e2e` is the same chain through the C ABI with host buffers,
 host->device copies of marker and mask and device->host copies of labels and the area mask
-inside the timed region (steps alternate between two streams with their own buffers, so the
-copies of one step overlap the kernels of the other).  `--impl reference` times the reference's
+inside the timed region (steps rotate over four streams with their own buffers, so the
+copies of some steps overlap the kernels of another).  `--impl reference` times the reference's
 own CPU code for the chain (its MorphologicOperations / ConnComponents functions compiled from
 its sources into oracle/_ref/; the oracle's restatement where that was not built) on the full
 tile, one tile per host core per step, loading no device library.
@@ -42,6 +42,7 @@ METRIC = "imreconstruct+bwlabel MPix/s, uint8 4096², plain vs batched GPU; % of
 # assign), label/area output: see csrc/ops.cu chain_impl.  A tuned schedule with streaming
 # passes replaces recon init by its passes and two seed kernels (tuned_passes below).
 KERNELS_PER_CHAIN = 15
+E2E_LANES = 4  # streams the end-to-end steps rotate over
 
 
 def tuned_passes(dtype, conn, batch, px):
@@ -395,13 +396,15 @@ def run_nsgb(args):
 
     # End to end through the C ABI with host buffers.  Every step copies its marker and mask in
     # from pinned host memory, runs the chain and copies its labels and area mask out.  Steps
-    # alternate between two streams, each with its own device buffers and workspace, so the
-    # copies of one step overlap the kernels of the other (the way a caller streams tiles).
+    # rotate over E2E_LANES streams, each with its own device buffers and workspace, so the
+    # copies of some steps overlap the kernels of another (the way a caller streams tiles).  A
+    # step's copies (33.5 MB in, 83.9 MB out at about 200 GB/s each way) take longer than its
+    # kernels; two streams left the copy engines the bound (0.67 ms per step), four hide them.
     pin_marker = torch.from_numpy(marker_h).pin_memory()
     pin_mask = torch.from_numpy(mask_h).pin_memory()
     e2e_opts = _ffi.Opts(0, 0, 0)
     lanes = []
-    for j in range(2):
+    for j in range(E2E_LANES):
         st_j = torch.cuda.Stream(dev)
         ws_j = torch.empty(ws_bytes + 256, dtype=torch.uint8, device=dev)
         lanes.append({
@@ -414,7 +417,7 @@ def run_nsgb(args):
         })
 
     def e2e_step(i):
-        ln = lanes[i % 2]
+        ln = lanes[i % E2E_LANES]
         with torch.cuda.stream(ln["stream"]):
             ln["work"].copy_(pin_marker, non_blocking=True)
             ln["mask"].copy_(pin_mask, non_blocking=True)
@@ -495,8 +498,8 @@ def run_nsgb(args):
             "h2d_bytes_per_step": 2 * n_px,
             "d2h_bytes_per_step": 5 * n_px,
             "ms_per_step": e2e_ms,
-            "path": "nsgb_chain C ABI, pinned host marker/mask in, labels + area mask out; steps alternate "
-                    "between two streams with their own buffers, so one step's copies overlap the other's kernels",
+            "path": f"nsgb_chain C ABI, pinned host marker/mask in, labels + area mask out; steps rotate over "
+                    f"{E2E_LANES} streams with their own buffers, so some steps' copies overlap another's kernels",
         },
         "gpu_launches": chain_kernels("u8", False, args.size * args.size) * args.steps,
         "clocks": clk,
