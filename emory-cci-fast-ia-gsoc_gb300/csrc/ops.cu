@@ -608,11 +608,18 @@ inline dim3 rcb(const BatchTotals& t) { return ccl::rowcol_grid(t.rows, t.max_w)
 inline dim3 qr(int64_t rows, int64_t cols) { return ccl::quadrow_grid((int)rows, (int)cols); }
 inline dim3 qrb(const BatchTotals& t) { return ccl::quadrow_grid(t.rows, t.max_w); }
 
-// Records the caller's optional timing event around the reconstruction kernel.
+// Records the caller's optional timing event around the reconstruction kernel.  While the
+// stream is being captured into a CUDA graph the record becomes an external event-record node,
+// so the event is recorded at every replay (a plain record in a capture only orders streams).
 cudaError_t record(const nsgb_opts* o, bool begin, cudaStream_t s) {
   if (!o) return cudaSuccess;
   void* ev = begin ? o->recon_event_begin : o->recon_event_end;
-  return ev ? cudaEventRecord((cudaEvent_t)ev, s) : cudaSuccess;
+  if (!ev) return cudaSuccess;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(s, &cap);
+  if (e != cudaSuccess) return e;
+  return cap == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags((cudaEvent_t)ev, s, cudaEventRecordExternal)
+                                              : cudaEventRecord((cudaEvent_t)ev, s);
 }
 
 // Reconstruction of the whole plan bracketed by the optional timing events.

@@ -72,7 +72,9 @@ typedef struct {
                             front of tiles has work, as in hole filling */
   int reserved[1];
   /* Optional CUDA events (cudaEvent_t) recorded on the call's stream immediately before and
-   * after the reconstruction kernel (nsgb_imreconstruct, nsgb_chain), for timing it alone. */
+   * after the reconstruction kernel (nsgb_imreconstruct, nsgb_chain), for timing it alone.  In
+   * a call captured into a CUDA graph they become external event-record nodes, recorded at
+   * every replay. */
   void* recon_event_begin;
   void* recon_event_end;
 } nsgb_opts;
