@@ -333,6 +333,103 @@ def test_chain(nsgb, oracle, size, n):
     assert got["n_kept"] == exp["n_kept"]
 
 
+def test_chain_in_cuda_graph_with_timing_events(nsgb, oracle):
+    """nsgb_chain captured into a CUDA graph and replayed: the results match the oracle on every
+    replay, and the reconstruction's timing events (recorded by event-record nodes of the
+    graph) give a positive time on each replay."""
+    import ctypes as C
+
+    import torch
+    from nsgb import _ffi, synth
+
+    lib = _ffi.lib
+    H, W = 300, 500
+    mask_h, marker_h = synth.tile_u8(H, W, 60, 3)
+    exp = oracle.chain(marker_h, mask_h)
+    mask, marker0 = to_dev(mask_h), to_dev(marker_h)
+    work = marker0.clone()
+    fill = torch.empty_like(mask)
+    labels = torch.empty((H, W), dtype=torch.int32, device="cuda")
+    area = torch.empty_like(mask)
+    nb = lib.nsgb_workspace_size(_ffi.OP_CHAIN, _ffi.U8, H, W)
+    wst = torch.empty(nb + 256, dtype=torch.uint8, device="cuda")
+    ws = (wst.data_ptr() + 255) & ~255
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    ev1.record()
+    opts = _ffi.Opts(0, 0, 0)
+    opts.recon_event_begin = C.c_void_p(ev0.cuda_event)
+    opts.recon_event_end = C.c_void_p(ev1.cuda_event)
+    cs = torch.cuda.Stream()
+
+    def call(stream):
+        st = lib.nsgb_chain(_ffi.U8, work.data_ptr(), mask.data_ptr(), H, W, W, 8, 128.0, 4, 8, 11, 1000,
+                            fill.data_ptr(), labels.data_ptr(), area.data_ptr(), None, None, ws, nb,
+                            C.c_void_p(stream.cuda_stream), C.byref(opts))
+        assert st == 0
+
+    torch.cuda.synchronize()
+    with torch.cuda.stream(cs):
+        call(cs)  # warm-up outside the capture (first-call set-up)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=cs):
+        call(cs)
+    for _ in range(3):
+        work.copy_(marker0)
+        g.replay()
+        torch.cuda.synchronize()
+        assert ev0.elapsed_time(ev1) > 0
+        assert np.array_equal(to_np(work), exp["recon"])
+        assert np.array_equal(to_np(fill), exp["fill"])
+        assert np.array_equal(to_np(labels), exp["labels"])
+        assert np.array_equal(to_np(area), exp["area"])
+    assert lib.nsgb_device_status(C.c_void_p(ws), None) == 0
+
+
+def _nested_rings(H, W, seed):
+    """Concentric rectangular rings of alternating brightness around random centres, with random
+    gaps cut into some rings: components enclosed by components several levels deep."""
+    rng = np.random.default_rng(seed)
+    img = np.full((H, W), 200, np.uint8)
+    yy, xx = np.mgrid[0:H, 0:W]
+    for _ in range(max(1, H * W // 600)):
+        cy, cx = rng.integers(0, H), rng.integers(0, W)
+        d = np.maximum(np.abs(yy - cy), np.abs(xx - cx))
+        for r in range(int(rng.integers(2, 14)), 0, -1):
+            ring = d == r
+            if rng.random() < 0.3:  # a gap
+                ring &= ~((yy == cy) & (xx > cx))
+            img[ring] = 40 if r % 2 else 220
+    return img
+
+
+@pytest.mark.parametrize("fill_conn,label_conn", [(4, 8), (8, 4), (4, 4), (8, 8)])
+def test_chain_hole_fill_and_labels_nested(nsgb, oracle, fill_conn, label_conn):
+    """The single-image chain's hole fill and labelling on inputs built to stress the enclosure
+    tree (nested rings with gaps, salt-and-pepper noise around the threshold), widths and heights
+    around the 32-pixel labelling tiles, one-pixel images, three dtypes and every pair of fill /
+    label connectivities, against the oracle.  The marker equals the mask, so the
+    reconstruction is the image itself and the threshold splits it directly."""
+    rng = np.random.default_rng(11)
+    sizes = [(1, 1), (1, 40), (40, 1), (2, 2), (31, 33), (33, 31), (64, 64), (65, 97), (200, 300), (257, 1100)]
+    for i, (h, w) in enumerate(sizes):
+        base = _nested_rings(h, w, i)
+        noise = np.where(rng.random((h, w)) < 0.5, 60, 190).astype(np.uint8)
+        for img8 in (base, noise, (255 - base).astype(np.uint8)):
+            for dt, scale in ((np.uint8, 1), (np.uint16, 257), (np.int32, -1000)):
+                img = img8.astype(np.int64) * scale
+                img = img.astype(dt)
+                thr = 128 * scale if scale > 0 else -128000.5
+                got = nsgb.chain(to_dev(img), to_dev(img), thr=thr, fill_conn=fill_conn, label_conn=label_conn)
+                exp = oracle.chain(img, img, thr=thr, fill_conn=fill_conn, label_conn=label_conn)
+                ctx = (h, w, dt.__name__, fill_conn, label_conn)
+                assert np.array_equal(to_np(got["fill"]), exp["fill"]), ctx
+                assert np.array_equal(to_np(got["labels"]), exp["labels"]), ctx
+                assert np.array_equal(to_np(got["area"]), exp["area"]), ctx
+                assert got["n_labels"] == exp["n_labels"] and got["n_kept"] == exp["n_kept"], ctx
+
+
 def test_chain_inverted_workload(nsgb, oracle):
     """The same chain on the inverted reconstruction: dark nuclei as foreground, thousands of
     components, so labelling and the area filter do real work."""
