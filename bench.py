@@ -38,11 +38,14 @@ PKG = os.path.join(ROOT, "emory-cci-fast-ia-gsoc_gb300")
 sys.path.insert(0, PKG)
 
 METRIC = "imreconstruct+bwlabel MPix/s, uint8 4096², plain vs batched GPU; % of HBM peak"
-# recon init + recon, fill (local, merge, flatten, border seeds, output; a batch: pack, flood seed,
-# flood seed finish, flood, output), label (local, merge, flatten), rank (mark, count, scan,
-# assign), label/area output: see csrc/ops.cu chain_impl.  A tuned schedule with streaming
-# passes replaces recon init by its passes and two seed kernels (tuned_passes below).
-KERNELS_PER_CHAIN = 15
+# One image: recon init + recon, the two-class labelling that fills and labels at once (local,
+# merge, border walk, parent join, flatten), rank (mark, count, scan, assign), label/area/fill
+# output.  A batch: recon init + recon, fill (pack, flood seed, flood seed finish, flood,
+# output), label (local, merge, flatten), rank (mark, count, scan, assign), label/area output.
+# See csrc/ops.cu chain_impl.  A tuned schedule with streaming passes replaces recon init by its
+# passes and two seed kernels (tuned_passes below).
+KERNELS_PER_CHAIN = 12
+KERNELS_PER_BATCH_CHAIN = 15
 E2E_LANES = 4  # streams the end-to-end steps rotate over
 
 
@@ -63,7 +66,7 @@ def tuned_passes(dtype, conn, batch, px):
 
 def chain_kernels(dtype, batch, px):
     p = tuned_passes(dtype, 8, batch, px)
-    return KERNELS_PER_CHAIN + (p + 1 if p > 0 else 0)
+    return (KERNELS_PER_BATCH_CHAIN if batch else KERNELS_PER_CHAIN) + (p + 1 if p > 0 else 0)
 RECON_BYTES_PER_PX = 3  # marker read + mask read + result write (u8)
 CHAIN_BYTES_PER_PX = 17  # recon 3 + threshold 2 + fill 2 + bwlabel 5 + bwareaopen 5
 
@@ -914,9 +917,10 @@ def bbox_section(args, dev, steps=20):
 
 
 # -- S1 after the colour steps: opening and nucleus-candidate stage ------------------------------
-# recon init + recon, fill (local, merge, flatten, border seeds, output), bw1 label (local, merge,
-# flatten) + kept count, bw2 label (local, merge, flatten), seeds, output: csrc/ops.cu candidates_impl
-CANDIDATE_KERNELS = 16
+# recon init + recon, bw1 filled and labelled at once (local, merge, border walk, parent join,
+# flatten) + kept count, bw2 label (local, merge, flatten), seeds, output: csrc/ops.cu
+# candidates_impl
+CANDIDATE_KERNELS = 13
 OPEN_KERNELS = 2  # erosion, dilation (csrc/morph.cu)
 
 

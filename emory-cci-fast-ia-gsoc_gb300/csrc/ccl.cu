@@ -16,7 +16,8 @@ constexpr int kRankThreads = 256;
 
 // Global roots among the local roots: set their bit, count them (and the kept ones) per image.
 __global__ void __launch_bounds__(kRankThreads) mark_roots(Imgs I, Forest f, int max_roots, int lo, int hi,
-                                                           unsigned* __restrict__ bits, int* __restrict__ counts) {
+                                                           unsigned* __restrict__ bits, int* __restrict__ counts,
+                                                           const unsigned* __restrict__ skip) {
   const int n = min(__ldcg(f.nroots), max_roots);
   const int lane = threadIdx.x & 31;
   for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -25,7 +26,7 @@ __global__ void __launch_bounds__(kRankThreads) mark_roots(Imgs I, Forest f, int
     bool keep = false;
     if (k < n) {
       const int lr = __ldcg(f.roots + k);
-      if (__ldcg(f.L + lr) == lr) {
+      if (__ldcg(f.L + lr) == lr && !(skip && test_bit(skip, lr))) {
         atomicOr(bits + (lr >> 5), 1u << (lr & 31));
         img = img_of(I, lr, PxBase());
         if (f.A) {
@@ -132,11 +133,12 @@ __global__ void __launch_bounds__(1024) scan_blocks(Imgs I, int* __restrict__ cn
 __global__ void __launch_bounds__(kRankThreads) assign_ranks(Imgs I, Forest f, int max_roots,
                                                              const unsigned* __restrict__ bits,
                                                              const int* __restrict__ off, const int* __restrict__ wpre,
-                                                             int* __restrict__ rank) {
+                                                             int* __restrict__ rank,
+                                                             const unsigned* __restrict__ skip) {
   const int n = min(__ldcg(f.nroots), max_roots);
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const int r = __ldcg(f.roots + k);
-    if (__ldcg(f.L + r) != r) continue;
+    if (__ldcg(f.L + r) != r || (skip && test_bit(skip, r))) continue;
     const Img m = img_at(I, img_of(I, r, PxBase()));
     const int local = r - m.px_base;
     const int b = m.blk_base + local / kBlockPx;
@@ -173,24 +175,25 @@ cudaError_t rank_bits(const Imgs& I, const BatchTotals& t, const unsigned* bits,
 }
 
 cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, int* rank,
-                       unsigned* bits, size_t bits_bytes, int* block_tmp, int* wpre, int* counts, cudaStream_t s) {
+                       unsigned* bits, size_t bits_bytes, int* block_tmp, int* wpre, int* counts, cudaStream_t s,
+                       const unsigned* skip) {
   cudaError_t e = cudaMemsetAsync(bits, 0, bits_bytes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, sizeof(int) * 2 * (size_t)t.n, s);
   if (e != cudaSuccess) return e;
   const int g = list_grid(t.px);
-  mark_roots<<<g, kRankThreads, 0, s>>>(I, f, (int)t.px, lo, hi, bits, counts);
+  mark_roots<<<g, kRankThreads, 0, s>>>(I, f, (int)t.px, lo, hi, bits, counts, skip);
   count_blocks<<<(t.blocks + kRankThreads / 32 - 1) / (kRankThreads / 32), kRankThreads, 0, s>>>(I, t.blocks, bits,
                                                                                                   block_tmp, wpre);
   scan_blocks<<<t.n, 1024, 0, s>>>(I, block_tmp);
-  assign_ranks<<<g, kRankThreads, 0, s>>>(I, f, (int)t.px, bits, block_tmp, wpre, rank);
+  assign_ranks<<<g, kRankThreads, 0, s>>>(I, f, (int)t.px, bits, block_tmp, wpre, rank, skip);
   return cudaGetLastError();
 }
 
 cudaError_t count_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, unsigned* bits,
-                        int* counts, cudaStream_t s) {
+                        int* counts, cudaStream_t s, const unsigned* skip) {
   cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * 2 * (size_t)t.n, s);
   if (e != cudaSuccess) return e;
-  mark_roots<<<list_grid(t.px), kRankThreads, 0, s>>>(I, f, (int)t.px, lo, hi, bits, counts);
+  mark_roots<<<list_grid(t.px), kRankThreads, 0, s>>>(I, f, (int)t.px, lo, hi, bits, counts, skip);
   return cudaGetLastError();
 }
 

@@ -33,6 +33,22 @@ namespace nsgb {
 namespace ccl {
 
 constexpr int kTile = 32;      // tile edge (pixels)
+
+// Connectivity codes.  4 and 8 join every class alike.  The two dual codes label two classes
+// in one forest: kConnFg8Bg4 joins class 1 with 8-connectivity and class 2 with 4-connectivity,
+// kConnFg4Bg8 the other way round (the pairs for which a binary image's components form a
+// tree by enclosure).
+constexpr int kConnFg8Bg4 = 84;
+constexpr int kConnFg4Bg8 = 48;
+
+// Whether pixels of class c join their diagonal neighbours of the same class.
+template <int CONN>
+__device__ __forceinline__ bool joins_diagonally(uint32_t c) {
+  if constexpr (CONN == 8) return true;
+  else if constexpr (CONN == 4) return false;
+  else if constexpr (CONN == kConnFg8Bg4) return c == 1u;
+  else return c == 2u;
+}
 constexpr int kThreads = 256;            // threads per labelling tile (32 columns x 8 warps)
 constexpr int kRows = kTile / (kThreads / 32);  // tile rows per thread (consecutive)
 
@@ -239,7 +255,7 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
     const CT up = s_c[u];
     const bool up_start = up != 0 && !(tx > 0 && s_c[u - 1] == up);
     if (up == v && (run_start || up_start)) s_union(s_lab, i, u);
-    if (CONN == 8) {
+    if (joins_diagonally<CONN>(v)) {
       if (run_start && tx > 0 && s_c[u - 1] == v) s_union(s_lab, i, u - 1);
       const bool run_end = (tx == kTile - 1) || s_c[i + 1] != v;
       if (run_end && tx < kTile - 1 && s_c[u + 1] == v) s_union(s_lab, i, u + 1);
@@ -337,7 +353,7 @@ __global__ void __launch_bounds__(64) ccl_merge(Cls cls, Imgs I, int* __restrict
   // the near pixel at this lane has the far run's class, the partner (its neighbour along the
   // edge) is joined to it by the near tile's own labelling or by the next tile's edge merge,
   // and the near pixel is joined to the far run here: the diagonal union adds nothing.
-  if (CONN == 8 && ca != cb) {
+  if (ca != cb && joins_diagonally<CONN>(cb)) {
     if (b_start) {
       const int dy = bottom ? ay : ay - 1, dx = bottom ? ax - 1 : ax;
       if (dy >= 0 && dx >= 0 && dy < H && dx < W && cls(T.m, dy, dx) == cb) g_union(L, qb, pb + dy * W + dx);
@@ -453,8 +469,25 @@ __global__ void ccl_seed_pixels(Imgs I, int total_rows, const int* __restrict__ 
   });
 }
 
-// Seed pixels on each image's border only: blockIdx.y = image, x walks its border (top row,
-// bottom row, left column, right column).
+// Border pixel k of an H x W image (top row, bottom row, left column, right column; 2W + 2H
+// positions, corners visited twice).
+__device__ __forceinline__ void border_pixel(int k, int H, int W, int& y, int& x) {
+  if (k < W) {
+    y = 0;
+    x = k;
+  } else if (k < 2 * W) {
+    y = H - 1;
+    x = k - W;
+  } else if (k < 2 * W + H) {
+    y = k - 2 * W;
+    x = 0;
+  } else {
+    y = k - 2 * W - H;
+    x = W - 1;
+  }
+}
+
+// Seed pixels on each image's border only: blockIdx.y = image, x walks its border.
 template <class Seed>
 __global__ void ccl_seed_border(Imgs I, const int* __restrict__ L, Seed seed, unsigned* __restrict__ bits) {
   const Img m = img_at(I, blockIdx.y);
@@ -462,21 +495,25 @@ __global__ void ccl_seed_border(Imgs I, const int* __restrict__ L, Seed seed, un
   const int per = 2 * W + 2 * H;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < per; k += gridDim.x * blockDim.x) {
     int y, x;
-    if (k < W) {
-      y = 0;
-      x = k;
-    } else if (k < 2 * W) {
-      y = H - 1;
-      x = k - W;
-    } else if (k < 2 * W + H) {
-      y = k - 2 * W;
-      x = 0;
-    } else {
-      y = k - 2 * W - H;
-      x = W - 1;
-    }
+    border_pixel(k, H, W, y, x);
     if (!seed(m, y, x)) continue;
     const int r = root_of(L, (int64_t)m.px_base + (int64_t)y * W + x);
+    if (r >= 0) set_root_bit(bits, r);
+  }
+}
+
+// The same before the roots are flattened (after ccl_merge): the root is found by walking the
+// forest.
+template <class Seed>
+__global__ void ccl_seed_border_walk(Imgs I, int* L, Seed seed, unsigned* __restrict__ bits) {
+  const Img m = img_at(I, blockIdx.y);
+  const int H = m.H, W = m.W;
+  const int per = 2 * W + 2 * H;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < per; k += gridDim.x * blockDim.x) {
+    int y, x;
+    border_pixel(k, H, W, y, x);
+    if (!seed(m, y, x)) continue;
+    const int r = g_find(L, m.px_base + y * W + x);
     if (r >= 0) set_root_bit(bits, r);
   }
 }
@@ -522,17 +559,75 @@ cudaError_t label(const Cls& cls, const Imgs& I, const BatchTotals& t, int conn,
   return cudaGetLastError();
 }
 
+// Enclosure tree of a two-class labelling (kConnFg8Bg4 / kConnFg4Bg8, before flattening):
+// with dual connectivities the components of the two classes form a tree by enclosure, the
+// image's outside (the components marked in `outside`, those of the outside class that touch
+// the border) at its top, and a component's parent is the component of the pixel directly
+// above its first pixel in raster order (its root).  Every component below the top joins its
+// parent, so each set that results is one component of "class 1 plus the class-2 components
+// it encloses" (class 1 with its holes filled).  One thread per listed local root; a global
+// root is hooked only by its own thread (its parent's root index is smaller than its own), so
+// the test for a global root at the start holds until the thread itself changes it.
+static __global__ void ccl_join_parents(Imgs I, Forest f, int max_roots, const unsigned* __restrict__ outside) {
+  const int n = min(__ldcg(f.nroots), max_roots);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int r = __ldcg(f.roots + k);
+    if (ld_relaxed(f.L + r) != r) continue;
+    if ((__ldcg(outside + (r >> 5)) >> (r & 31)) & 1u) continue;
+    const Img m = img_at(I, img_of(I, r, PxBase()));
+    if (r - m.px_base < m.W) continue;  // first row: its parent is the outside
+    const int p = g_find(f.L, r - m.W);
+    if (p < 0 || ((__ldcg(outside + (p >> 5)) >> (p & 31)) & 1u)) continue;
+    g_union(f.L, r, p);
+  }
+}
+
+// Seed test: pixels of class 2.
+template <class Cls>
+struct Class2 {
+  Cls cls;
+  __device__ bool operator()(const Img& m, int y, int x) const { return cls(m, y, x) == 2u; }
+};
+
+// Labels both classes of a two-class classifier (class 1 = the foreground, class 2 = the rest)
+// with dual connectivities and joins every component below the outside to its parent: the
+// sets are then the components of the foreground with its holes filled, each rooted at its
+// smallest raster index, and A holds their areas (holes included).  The border components of
+// class 2 are marked in `outside` (zeroed first; their roots stay roots and are not part of
+// the filled image).  Afterwards root(i) = L[L[i]].
+template <class Cls>
+cudaError_t label_filled(const Cls& cls, const Imgs& I, const BatchTotals& t, int conn, const Forest& f,
+                         unsigned* outside, size_t outside_bytes, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(f.nroots, 0, sizeof(int), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(outside, 0, outside_bytes, s);
+  if (e != cudaSuccess) return e;
+  if (conn == kConnFg8Bg4) {
+    ccl_local<Cls, kConnFg8Bg4><<<t.c_tiles, kThreads, 0, s>>>(cls, I, f);
+    ccl_merge<Cls, kConnFg8Bg4><<<t.c_tiles, 64, 0, s>>>(cls, I, f.L);
+  } else {
+    ccl_local<Cls, kConnFg4Bg8><<<t.c_tiles, kThreads, 0, s>>>(cls, I, f);
+    ccl_merge<Cls, kConnFg4Bg8><<<t.c_tiles, 64, 0, s>>>(cls, I, f.L);
+  }
+  const int gx = (t.perimeter_max + 255) / 256 > 64 ? 64 : (t.perimeter_max + 255) / 256;
+  ccl_seed_border_walk<Class2<Cls>><<<dim3(gx > 0 ? gx : 1, t.n), 256, 0, s>>>(I, f.L, Class2<Cls>{cls}, outside);
+  ccl_join_parents<<<list_grid(t.px), 256, 0, s>>>(I, f, (int)t.px, outside);
+  ccl_flatten_roots<<<list_grid(t.px), 256, 0, s>>>(f, (int)t.px);
+  return cudaGetLastError();
+}
+
 // Raster-order ranks of the global roots, from the list of local roots: rank[r] = number of
 // roots of r's image before r (written at roots only).  counts[2*i] = roots of image i,
 // counts[2*i+1] = roots whose area (A, if given) lies in [lo, hi).  `bits` (one bit per
 // pixel, px/32 + 2 words), `block_tmp` (one int per rank block) and `wpre` (32 ints per rank
 // block) are scratch.
+// Roots marked in `skip` (optional) are left out: not counted and not ranked.
 cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, int* rank,
-                       unsigned* bits, size_t bits_bytes, int* block_tmp, int* wpre, int* counts, cudaStream_t s);
+                       unsigned* bits, size_t bits_bytes, int* block_tmp, int* wpre, int* counts, cudaStream_t s,
+                       const unsigned* skip = nullptr);
 // The counts of rank_roots alone (no ranks).  `bits` receives the global roots' bits (scratch,
 // not cleared first).
 cudaError_t count_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, unsigned* bits,
-                        int* counts, cudaStream_t s);
+                        int* counts, cudaStream_t s, const unsigned* skip = nullptr);
 constexpr int kBlockPx = 1024;
 
 // The counting half of rank_roots for any bitmap of the images' pixels: per 1024-px block the

@@ -95,6 +95,13 @@ struct ClsNotMax {  // binary hole filling: pixels that are not foreground (max<
   }
 };
 template <typename T>
+struct ClsAboveOrNot {  // hole filling and labelling at once: 1 where R > thr, 2 elsewhere
+  GtThr<T> gt;
+  __device__ uint32_t operator()(const Img& m, int y, int x) const {
+    return gt(pxcg<T>(m.plane, m.pitch, y, x)) ? 1u : 2u;
+  }
+};
+template <typename T>
 struct ClsNotAbove {  // hole filling of (R > thr): the complement class !(R > thr); R = plane
   GtThr<T> gt;
   __device__ uint32_t operator()(const Img& m, int y, int x) const {
@@ -109,9 +116,9 @@ __device__ __forceinline__ uint8_t valley(const Img& m, int y, int x) {
   const int d = (int)px<uint8_t>(m.aux, m.pitch, y, x) - (int)pxcg<uint8_t>(m.plane, m.pitch, y, x);
   return (uint8_t)(d > 0 ? d : 0);
 }
-struct ClsValleyNotAbove {  // hole filling of (D > g1): the complement class !(D > g1)
+struct ClsValleyAboveOrNot {  // hole filling and labelling of (D > g1) at once: 1 where D > g1, 2 elsewhere
   GtThr<uint8_t> gt;
-  __device__ uint32_t operator()(const Img& m, int y, int x) const { return gt(valley(m, y, x)) ? 0u : 1u; }
+  __device__ uint32_t operator()(const Img& m, int y, int x) const { return gt(valley(m, y, x)) ? 1u : 2u; }
 };
 struct ClsValleyAbove {  // bwselect's image D > g2
   GtThr<uint8_t> gt;
@@ -141,10 +148,11 @@ struct SeedCandidate {
   const int* LF;
   const int* A;
   int lo, hi;
+  const unsigned* outside;  // roots of LF that are not part of the filled image (optional)
   __device__ bool operator()(const Img& m, int y, int x) const {
     if (!gt(valley(m, y, x))) return false;
     const int r = ccl::root_of_ro(LF, (int64_t)m.px_base + (int64_t)y * m.W + x);
-    if (r < 0) return false;
+    if (r < 0 || (outside && ccl::test_bit(outside, r))) return false;
     const int a = __ldg(A + r);
     return a >= lo && a < hi;
   }
@@ -295,14 +303,35 @@ __global__ void candidates_out_kernel(Imgs I, int total_rows, const int* __restr
 // loads, because a giant component's root is read by every one of its pixels.  Single image:
 // explicit output pointers / pitches; batch: Img::labels / Img::area (dense).
 // RELABEL: raster rank labels (else root indices); AREA: area-filter outputs (A non-null).
-template <bool RELABEL, bool AREA>
+// FILLED: the forest of ccl::label_filled, whose roots marked in `outside` are background; the
+// filled image (255 elsewhere) goes to `filled` (single image, optional) or Img::fill (batch).
+template <bool RELABEL, bool AREA, bool FILLED = false>
 __global__ void label_out_kernel(Imgs I, int total_rows, const int* __restrict__ L, const int* __restrict__ rank,
                                  int32_t* labels, int64_t pitch_labels, const int* __restrict__ A, int lo,
-                                 int hi, int32_t* kept_labels, int64_t pitch_kept, uint8_t* flat, int64_t pitch_flat) {
+                                 int hi, int32_t* kept_labels, int64_t pitch_kept, uint8_t* flat, int64_t pitch_flat,
+                                 const unsigned* __restrict__ outside = nullptr, uint8_t* filled = nullptr,
+                                 int64_t pitch_filled = 0) {
   ccl::for_batch_quads(I, total_rows, [&](const Img& m, int y, int x, int n) {
     int r[4], lab[4], kl[4];
     uint8_t fl[4];
     ccl::roots4_ro(L, (int64_t)m.px_base + (int64_t)y * m.W + x, n, r);
+    if (FILLED) {
+      bool out[4];
+      uint8_t fi[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        out[k] = (k > 0 && r[k] == r[k - 1]) ? out[k - 1] : (r[k] >= 0 && ccl::test_bit(outside, r[k]));
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (out[k]) r[k] = -1;
+        fi[k] = r[k] >= 0 ? 255 : 0;
+      }
+      if (!I.d) {
+        if (filled) store4_u8(pxp<uint8_t>(filled, pitch_filled, y, x), n, fi);
+      } else if (m.fill) {
+        store4_u8(m.fill + (int64_t)y * m.W + x, n, fi);
+      }
+    }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const bool same = k > 0 && r[k] == r[k - 1];
@@ -663,6 +692,34 @@ cudaError_t chain_impl(int dtype, const Plan& P, const Ws& w, int recon_conn, do
                        uint8_t* area_out, const nsgb_opts* opts, cudaStream_t s) {
   const BatchTotals& t = P.t;
   cudaError_t e = recon_timed(opts, dtype, P, recon_conn, false, dtype == NSGB_I32, w.recon, s);
+  const bool dual = (fill_conn == 4 && label_conn == 8) || (fill_conn == 8 && label_conn == 4);
+  if (e == cudaSuccess && dual && !(P.I.d && t.n > 1)) {
+    // (b)-(e) on one image with one labelling.  With dual connectivities (the not-above class
+    // flooded 4-connected, the filled image labelled 8-connected, or the other way round) the
+    // components of R > thr and of its complement form a tree by enclosure, and a component of
+    // the filled image is a top-level component of R > thr with everything it encloses: both
+    // classes are labelled in one forest, each component joined to its parent (the component
+    // above its first pixel) unless that is a complement component touching the border.  The
+    // bitmap of those outside components lives in F, which this path does not otherwise use.
+    unsigned* outside = (unsigned*)w.F;
+    const int code = label_conn == 8 ? ccl::kConnFg8Bg4 : ccl::kConnFg4Bg8;
+    e = dispatch_int(dtype, [&](auto* tag) -> cudaError_t {
+      using T = std::remove_pointer_t<decltype(tag)>;
+      return ccl::label_filled(ClsAboveOrNot<T>{GtThr<T>::make(thr)}, P.I, t, code, w.forest(true), outside,
+                               w.bits_bytes, s);
+    });
+    if (e == cudaSuccess)
+      e = ccl::rank_roots(P.I, t, w.forest(true), area_min, area_max, w.R, w.bits, w.bits_bytes, w.tmp, w.wpre,
+                          w.counts, s, outside);
+    if (e == cudaSuccess) {
+      const int64_t W1 = P.I.d ? 0 : P.I.one.W;
+      label_out_kernel<true, true, true><<<qrb(t), 256, 0, s>>>(P.I, t.rows, w.L, w.R, labels_out, W1 * 4, w.A,
+                                                                area_min, area_max, nullptr, 0, area_out, W1,
+                                                                outside, fill_out, W1);
+      e = cudaGetLastError();
+    }
+    return e;
+  }
   if (e == cudaSuccess && P.I.d && t.n > 1) {
     // (b)+(c) on a batch: the pixels not above the threshold as a bit plane, flooded from
     // outside each image (bitfill.cu); the fill is what the flood does not reach.  The label
@@ -716,33 +773,30 @@ cudaError_t chain_impl(int dtype, const Plan& P, const Ws& w, int recon_conn, do
 }
 
 // The nucleus-candidate stage on one image (plane = rc_open, reconstructed in place; aux = rc):
-// (a) R = recon(rc_open, rc, 8); (b) bw1 = imfillHoles(D > g1, 4) into F, the threshold fused
-// into the labelling's classifier; (c) bw1's 8-connected components and their areas, the kept
-// ones counted (w.counts[1]); (d) bwselect(D > g2, bw1_t, 8): D > g2 labelled into a second
+// (a) R = recon(rc_open, rc, 8); (b) bw1 = imfillHoles(D > g1, 4) and (c) bw1's 8-connected
+// components with their areas, from one labelling of D > g1 and its complement (the threshold
+// in the classifier), the kept ones counted (w.counts[1]); (d) bwselect(D > g2, bw1_t, 8): D > g2 labelled into a second
 // forest (the rank array R, unused here), its roots seeded straight from bw1's forest and
 // areas, so bw1_t is never written; (e) the output with rbc == 0 folded in.
 cudaError_t candidates_impl(const Plan& P, const Ws& w, double g1, double g2, int lo, int hi, const uint8_t* rbc,
                             uint8_t* out, const nsgb_opts* opts, cudaStream_t s) {
   const BatchTotals& t = P.t;
-  const ClsValleyNotAbove holes{GtThr<uint8_t>::make(g1)};
+  const GtThr<uint8_t> gt1 = GtThr<uint8_t>::make(g1);
   const GtThr<uint8_t> gt2 = GtThr<uint8_t>::make(g2);
   cudaError_t e = recon_timed(opts, NSGB_U8, P, 8, false, false, w.recon, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.bits, 0, w.bits_bytes, s);
-  if (e == cudaSuccess) e = ccl::label(holes, P.I, t, 4, w.forest(false), s);
-  if (e == cudaSuccess) {
-    const int gx = grid1d(t.perimeter_max) > 64 ? 64 : grid1d(t.perimeter_max);
-    ccl::ccl_seed_border<SeedBorder<ClsValleyNotAbove>><<<dim3(gx, t.n), 256, 0, s>>>(
-        P.I, w.L, SeedBorder<ClsValleyNotAbove>{holes}, w.bits);
-    fill_out_kernel<uint8_t><<<qrb(t), 256, 0, s>>>(P.I, t.rows, w.L, w.bits, w.F, nullptr, 0, (uint8_t)255);
-    e = cudaGetLastError();
-  }
-  if (e == cudaSuccess) e = ccl::label(ClsDenseU8{w.F}, P.I, t, 8, w.forest(true), s);
-  if (e == cudaSuccess) e = ccl::count_roots(P.I, t, w.forest(true), lo, hi, w.bits, w.counts, s);
+  // (b)+(c) as one labelling of D > g1 (8-connected) and its complement (4-connected), each
+  // component joined to the one enclosing it (ccl::label_filled); the complement components
+  // that touch the border are marked in F (used as a bitmap here) and are not part of bw1.
+  unsigned* outside = (unsigned*)w.F;
+  if (e == cudaSuccess)
+    e = ccl::label_filled(ClsValleyAboveOrNot{gt1}, P.I, t, ccl::kConnFg8Bg4, w.forest(true), outside,
+                          w.bits_bytes, s);
+  if (e == cudaSuccess) e = ccl::count_roots(P.I, t, w.forest(true), lo, hi, w.bits, w.counts, s, outside);
   if (e == cudaSuccess) e = cudaMemsetAsync(w.bits, 0, w.bits_bytes, s);
   const ccl::Forest sel{w.R, nullptr, w.roots, w.nroots};
   if (e == cudaSuccess) e = ccl::label(ClsValleyAbove{gt2}, P.I, t, 8, sel, s);
   if (e == cudaSuccess) {
-    ccl::ccl_seed_pixels<SeedCandidate><<<rcb(t), 256, 0, s>>>(P.I, t.rows, w.R, SeedCandidate{gt2, w.L, w.A, lo, hi},
+    ccl::ccl_seed_pixels<SeedCandidate><<<rcb(t), 256, 0, s>>>(P.I, t.rows, w.R, SeedCandidate{gt2, w.L, w.A, lo, hi, outside},
                                                                w.bits);
     candidates_out_kernel<<<qrb(t), 256, 0, s>>>(P.I, t.rows, w.R, w.bits, rbc, out);
     e = cudaGetLastError();
