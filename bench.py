@@ -499,6 +499,8 @@ def run_nsgb(args):
         if not torch.equal(ln["pin_labels"].to(dev), labels) or not torch.equal(ln["pin_area"].to(dev), area):
             raise RuntimeError("e2e outputs differ from the device-resident run")
 
+    link = host_link(dev, 2 * n_px, 5 * n_px, n_px)
+
     peak, peak_kind = read_peaks()
     achieved = RECON_BYTES_PER_PX * n_px / (rms / 1e3) / 1e9
     traffic, traffic_note = read_traffic(args.size)
@@ -548,6 +550,7 @@ def run_nsgb(args):
             "ms_per_step": e2e_ms,
             "path": f"nsgb_chain C ABI, pinned host marker/mask in, labels + area mask out; steps rotate over "
                     f"{E2E_LANES} streams with their own buffers, so some steps' copies overlap another's kernels",
+            "host_link": dict(link, frac=(world * n_px / 1e6 / (e2e_ms / 1e3)) / (world * link["bound_mpix_s"])),
         },
         "gpu_launches": chain_kernels("u8", False, args.size * args.size) * args.steps,
         "clocks": clk,
@@ -1140,6 +1143,48 @@ def large_section(args, dev, steps=3):
         del img, fill, fws_t
         torch.cuda.empty_cache()
     return res
+
+
+def host_link(dev, in_bytes, out_bytes, px, reps=5):
+    """The host link's own bound on an end-to-end step: pinned-memory copy bandwidth measured
+    in this process (device -> host alone, host -> device alone, and both directions at once on
+    two streams), and the time a step's copies need at those rates when its inputs go in while
+    its outputs come out (the directions share the link: the smaller transfer runs at the
+    concurrent rate, the rest of the larger one at its solo rate)."""
+    import torch
+
+    n = max(in_bytes, out_bytes)
+    d_out = torch.empty(n, dtype=torch.uint8, device=dev)
+    d_in = torch.empty(n, dtype=torch.uint8, device=dev)
+    h_out = torch.empty(n, dtype=torch.uint8).pin_memory()
+    h_in = torch.zeros(n, dtype=torch.uint8).pin_memory()
+    s1, s2 = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+
+    def timed(d2h, h2d):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        ev[0].record(s1)
+        s2.wait_event(ev[0])
+        for _ in range(reps):
+            if d2h:
+                with torch.cuda.stream(s1):
+                    h_out.copy_(d_out, non_blocking=True)
+            if h2d:
+                with torch.cuda.stream(s2):
+                    d_in.copy_(h_in, non_blocking=True)
+        s1.wait_stream(s2)
+        ev[1].record(s1)
+        torch.cuda.synchronize()
+        return n * reps / (ev[0].elapsed_time(ev[1]) / 1e3) / 1e9
+
+    timed(True, True)  # warm-up
+    d2h, h2d, both = timed(True, False), timed(False, True), timed(True, True)
+    lo, hi = min(in_bytes, out_bytes), max(in_bytes, out_bytes)
+    solo = d2h if out_bytes >= in_bytes else h2d
+    bound_s = lo / (both * 1e9) + (hi - lo) / (solo * 1e9)
+    return {"d2h_GBps": d2h, "h2d_GBps": h2d, "concurrent_GBps_per_direction": both,
+            "bound_ms_per_step": bound_s * 1e3, "bound_mpix_s": px / 1e6 / bound_s,
+            "note": "pinned-memory copies timed in this run; frac = e2e value / this bound"}
 
 
 def main():

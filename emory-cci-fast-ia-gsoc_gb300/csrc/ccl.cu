@@ -18,6 +18,8 @@ constexpr int kRankThreads = 256;
 __global__ void __launch_bounds__(kRankThreads) mark_roots(Imgs I, Forest f, int max_roots, int lo, int hi,
                                                            unsigned* __restrict__ bits, int* __restrict__ counts,
                                                            const unsigned* __restrict__ skip) {
+  pdl_wait();
+  pdl_release();
   const int n = min(__ldcg(f.nroots), max_roots);
   const int lane = threadIdx.x & 31;
   for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -49,6 +51,8 @@ __global__ void __launch_bounds__(kRankThreads) mark_roots(Imgs I, Forest f, int
 // number of roots before it in the block (wpre[32 * b + j]).
 __global__ void __launch_bounds__(kRankThreads) count_blocks(Imgs I, int nblocks, const unsigned* __restrict__ bits,
                                                              int* __restrict__ cnt, int* __restrict__ wpre) {
+  pdl_wait();
+  pdl_release();
   const int b = blockIdx.x * (kRankThreads / 32) + (threadIdx.x >> 5);
   if (b >= nblocks) return;
   const int lane = threadIdx.x & 31;
@@ -75,6 +79,8 @@ __global__ void __launch_bounds__(kRankThreads) count_blocks(Imgs I, int nblocks
 // taken in passes of 8 x 1024 (coalesced, all loads of a pass in flight at once); thread t
 // holds elements j * 1024 + t of the pass.
 __global__ void __launch_bounds__(1024) scan_blocks(Imgs I, int* __restrict__ cnt) {
+  pdl_wait();
+  pdl_release();
   constexpr int J = 8;
   __shared__ int s_tot[J][32];
   __shared__ int s_chunk[J + 1];
@@ -135,6 +141,8 @@ __global__ void __launch_bounds__(kRankThreads) assign_ranks(Imgs I, Forest f, i
                                                              const int* __restrict__ off, const int* __restrict__ wpre,
                                                              int* __restrict__ rank,
                                                              const unsigned* __restrict__ skip) {
+  pdl_wait();
+  pdl_release();
   const int n = min(__ldcg(f.nroots), max_roots);
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const int r = __ldcg(f.roots + k);
@@ -176,17 +184,27 @@ cudaError_t rank_bits(const Imgs& I, const BatchTotals& t, const unsigned* bits,
 
 cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, int* rank,
                        unsigned* bits, size_t bits_bytes, int* block_tmp, int* wpre, int* counts, cudaStream_t s,
-                       const unsigned* skip) {
-  cudaError_t e = cudaMemsetAsync(bits, 0, bits_bytes, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, sizeof(int) * 2 * (size_t)t.n, s);
+                       const unsigned* skip, bool pdl) {
+  cudaError_t e;
+  if (pdl) {
+    const int nb = (int)(bits_bytes / sizeof(unsigned));
+    e = launch_k(true, zero_words, dim3(flat_grid(nb + 2 * t.n)), dim3(256), s, bits, nb, (unsigned*)counts, 2 * t.n);
+  } else {
+    e = cudaMemsetAsync(bits, 0, bits_bytes, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, sizeof(int) * 2 * (size_t)t.n, s);
+  }
   if (e != cudaSuccess) return e;
   const int g = list_grid(t.px);
-  mark_roots<<<g, kRankThreads, 0, s>>>(I, f, (int)t.px, lo, hi, bits, counts, skip);
-  count_blocks<<<(t.blocks + kRankThreads / 32 - 1) / (kRankThreads / 32), kRankThreads, 0, s>>>(I, t.blocks, bits,
-                                                                                                  block_tmp, wpre);
-  scan_blocks<<<t.n, 1024, 0, s>>>(I, block_tmp);
-  assign_ranks<<<g, kRankThreads, 0, s>>>(I, f, (int)t.px, bits, block_tmp, wpre, rank, skip);
-  return cudaGetLastError();
+  const int cb = (t.blocks + kRankThreads / 32 - 1) / (kRankThreads / 32);
+  e = launch_k(pdl, mark_roots, dim3(g), dim3(kRankThreads), s, I, f, (int)t.px, lo, hi, bits, counts, skip);
+  if (e == cudaSuccess)
+    e = launch_k(pdl, count_blocks, dim3(cb), dim3(kRankThreads), s, I, t.blocks, (const unsigned*)bits, block_tmp,
+                 wpre);
+  if (e == cudaSuccess) e = launch_k(pdl, scan_blocks, dim3(t.n), dim3(1024), s, I, block_tmp);
+  if (e == cudaSuccess)
+    e = launch_k(pdl, assign_ranks, dim3(g), dim3(kRankThreads), s, I, f, (int)t.px, (const unsigned*)bits,
+                 (const int*)block_tmp, (const int*)wpre, rank, skip);
+  return e;
 }
 
 cudaError_t count_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, unsigned* bits,

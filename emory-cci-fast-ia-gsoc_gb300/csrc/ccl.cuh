@@ -178,6 +178,8 @@ struct class_type<Cls, std::void_t<typename Cls::class_t>> {
 // over the tiles of all images).
 template <class Cls, int CONN>
 __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f) {
+  pdl_wait();
+  pdl_release();
   using CT = typename class_type<Cls>::type;
   __shared__ int s_lab[kTile * kTile];
   __shared__ int s_cnt[kTile * kTile];
@@ -316,6 +318,8 @@ __global__ void __launch_bounds__(kThreads) ccl_local(Cls cls, Imgs I, Forest f)
 // plus the two diagonal ends of each far-side run for 8-connectivity.
 template <class Cls, int CONN>
 __global__ void __launch_bounds__(64) ccl_merge(Cls cls, Imgs I, int* __restrict__ L) {
+  pdl_wait();
+  pdl_release();
   const TileAt T = tile_at(I, blockIdx.x);
   const int x0 = T.x0, y0 = T.y0, H = T.m.H, W = T.m.W, pb = T.m.px_base;
   const int lane = threadIdx.x & 31;
@@ -367,11 +371,16 @@ __global__ void __launch_bounds__(64) ccl_merge(Cls cls, Imgs I, int* __restrict
 
 // Every local root points directly at its global root; local-root areas move into the root.
 // Four list entries per thread and iteration, their loads issued together: most local roots
-// are global roots already (one load to see it), so the kernel is load-latency bound.
+// are global roots already (one load to see it), so the kernel is load-latency bound.  The
+// area adds of a warp are summed per root first (one atomic per root and warp): the local
+// roots of a giant component, one per labelling tile, all add into the same word.
 static __global__ void ccl_flatten_roots(Forest f, int max_roots) {
+  pdl_wait();
+  pdl_release();
   const int n = min(__ldcg(f.nroots), max_roots);
   const int stride = gridDim.x * blockDim.x;
-  for (int k0 = blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += 4 * stride) {
+  const int lane = threadIdx.x & 31;
+  for (int k0 = blockIdx.x * blockDim.x + threadIdx.x; k0 - lane < n; k0 += 4 * stride) {
     int lr[4], p[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) lr[j] = k0 + j * stride < n ? __ldcg(f.roots + k0 + j * stride) : -1;
@@ -379,11 +388,20 @@ static __global__ void ccl_flatten_roots(Forest f, int max_roots) {
     for (int j = 0; j < 4; ++j) p[j] = lr[j] >= 0 ? __ldcg(f.L + lr[j]) : -1;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      if (lr[j] < 0 || p[j] == lr[j]) continue;
-      const int r = g_find(f.L, lr[j]);
-      if (r >= 0 && r != lr[j]) {
-        atomicMin(f.L + lr[j], r);
-        if (f.A) atomicAdd(f.A + r, __ldcg(f.A + lr[j]));
+      int r = -1, a = 0;
+      if (lr[j] >= 0 && p[j] != lr[j]) {
+        r = g_find(f.L, lr[j]);
+        if (r >= 0 && r != lr[j]) {
+          atomicMin(f.L + lr[j], r);
+          if (f.A) a = __ldcg(f.A + lr[j]);
+        } else {
+          r = -1;
+        }
+      }
+      if (f.A) {
+        const unsigned peers = __match_any_sync(NSGB_FULL, r);
+        const int sum = __reduce_add_sync(peers, a);
+        if (r >= 0 && (__ffs(peers) - 1) == lane) atomicAdd(f.A + r, sum);
       }
     }
   }
@@ -506,6 +524,8 @@ __global__ void ccl_seed_border(Imgs I, const int* __restrict__ L, Seed seed, un
 // forest.
 template <class Seed>
 __global__ void ccl_seed_border_walk(Imgs I, int* L, Seed seed, unsigned* __restrict__ bits) {
+  pdl_wait();
+  pdl_release();
   const Img m = img_at(I, blockIdx.y);
   const int H = m.H, W = m.W;
   const int per = 2 * W + 2 * H;
@@ -569,6 +589,8 @@ cudaError_t label(const Cls& cls, const Imgs& I, const BatchTotals& t, int conn,
 // root is hooked only by its own thread (its parent's root index is smaller than its own), so
 // the test for a global root at the start holds until the thread itself changes it.
 static __global__ void ccl_join_parents(Imgs I, Forest f, int max_roots, const unsigned* __restrict__ outside) {
+  pdl_wait();
+  pdl_release();
   const int n = min(__ldcg(f.nroots), max_roots);
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const int r = __ldcg(f.roots + k);
@@ -580,6 +602,26 @@ static __global__ void ccl_join_parents(Imgs I, Forest f, int max_roots, const u
     if (p < 0 || ((__ldcg(outside + (p >> 5)) >> (p & 31)) & 1u)) continue;
     g_union(f.L, r, p);
   }
+}
+
+// Zeroes words [0, na) of a and [0, nb) of b.
+static __global__ void zero_words(unsigned* a, int na, unsigned* b, int nb) {
+  pdl_wait();
+  pdl_release();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < na + nb; i += gridDim.x * blockDim.x) {
+    if (i < na) a[i] = 0u;
+    else b[i - na] = 0u;
+  }
+}
+
+// Launches `kernel` the ordinary way, or (pdl) as a programmatic dependent of the kernel before
+// it on the stream, which every kernel launched here waits for first thing.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s,
+                            Args&&... args) {
+  if (pdl) return launch_dependent(kernel, grid, block, s, std::forward<Args>(args)...);
+  kernel<<<grid, block, 0, s>>>(std::forward<Args>(args)...);
+  return cudaGetLastError();
 }
 
 // Seed test: pixels of class 2.
@@ -597,22 +639,28 @@ struct Class2 {
 // the filled image).  Afterwards root(i) = L[L[i]].
 template <class Cls>
 cudaError_t label_filled(const Cls& cls, const Imgs& I, const BatchTotals& t, int conn, const Forest& f,
-                         unsigned* outside, size_t outside_bytes, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(f.nroots, 0, sizeof(int), s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(outside, 0, outside_bytes, s);
+                         unsigned* outside, size_t outside_bytes, cudaStream_t s, bool pdl = false) {
+  // The first launch follows whatever the caller queued last, so it is an ordinary one; the
+  // rest may start while their predecessor drains.
+  const int zw = (int)(outside_bytes / sizeof(unsigned));
+  cudaError_t e = launch_k(false, zero_words, dim3(flat_grid(zw + 1)), dim3(256), s, (unsigned*)f.nroots, 1,
+                           outside, zw);
   if (e != cudaSuccess) return e;
   if (conn == kConnFg8Bg4) {
-    ccl_local<Cls, kConnFg8Bg4><<<t.c_tiles, kThreads, 0, s>>>(cls, I, f);
-    ccl_merge<Cls, kConnFg8Bg4><<<t.c_tiles, 64, 0, s>>>(cls, I, f.L);
+    e = launch_k(pdl, ccl_local<Cls, kConnFg8Bg4>, dim3(t.c_tiles), dim3(kThreads), s, cls, I, f);
+    if (e == cudaSuccess) e = launch_k(pdl, ccl_merge<Cls, kConnFg8Bg4>, dim3(t.c_tiles), dim3(64), s, cls, I, f.L);
   } else {
-    ccl_local<Cls, kConnFg4Bg8><<<t.c_tiles, kThreads, 0, s>>>(cls, I, f);
-    ccl_merge<Cls, kConnFg4Bg8><<<t.c_tiles, 64, 0, s>>>(cls, I, f.L);
+    e = launch_k(pdl, ccl_local<Cls, kConnFg4Bg8>, dim3(t.c_tiles), dim3(kThreads), s, cls, I, f);
+    if (e == cudaSuccess) e = launch_k(pdl, ccl_merge<Cls, kConnFg4Bg8>, dim3(t.c_tiles), dim3(64), s, cls, I, f.L);
   }
   const int gx = (t.perimeter_max + 255) / 256 > 64 ? 64 : (t.perimeter_max + 255) / 256;
-  ccl_seed_border_walk<Class2<Cls>><<<dim3(gx > 0 ? gx : 1, t.n), 256, 0, s>>>(I, f.L, Class2<Cls>{cls}, outside);
-  ccl_join_parents<<<list_grid(t.px), 256, 0, s>>>(I, f, (int)t.px, outside);
-  ccl_flatten_roots<<<list_grid(t.px), 256, 0, s>>>(f, (int)t.px);
-  return cudaGetLastError();
+  if (e == cudaSuccess)
+    e = launch_k(pdl, ccl_seed_border_walk<Class2<Cls>>, dim3(gx > 0 ? gx : 1, t.n), dim3(256), s, I, f.L,
+                 Class2<Cls>{cls}, outside);
+  if (e == cudaSuccess)
+    e = launch_k(pdl, ccl_join_parents, dim3(list_grid(t.px)), dim3(256), s, I, f, (int)t.px, (const unsigned*)outside);
+  if (e == cudaSuccess) e = launch_k(pdl, ccl_flatten_roots, dim3(list_grid(t.px)), dim3(256), s, f, (int)t.px);
+  return e;
 }
 
 // Raster-order ranks of the global roots, from the list of local roots: rank[r] = number of
@@ -621,9 +669,11 @@ cudaError_t label_filled(const Cls& cls, const Imgs& I, const BatchTotals& t, in
 // pixel, px/32 + 2 words), `block_tmp` (one int per rank block) and `wpre` (32 ints per rank
 // block) are scratch.
 // Roots marked in `skip` (optional) are left out: not counted and not ranked.
+// With pdl, every launch is a programmatic dependent of the kernel before it (the caller's last
+// launch must be a kernel).
 cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, int* rank,
                        unsigned* bits, size_t bits_bytes, int* block_tmp, int* wpre, int* counts, cudaStream_t s,
-                       const unsigned* skip = nullptr);
+                       const unsigned* skip = nullptr, bool pdl = false);
 // The counts of rank_roots alone (no ranks).  `bits` receives the global roots' bits (scratch,
 // not cleared first).
 cudaError_t count_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, unsigned* bits,

@@ -311,6 +311,8 @@ __global__ void label_out_kernel(Imgs I, int total_rows, const int* __restrict__
                                  int hi, int32_t* kept_labels, int64_t pitch_kept, uint8_t* flat, int64_t pitch_flat,
                                  const unsigned* __restrict__ outside = nullptr, uint8_t* filled = nullptr,
                                  int64_t pitch_filled = 0) {
+  pdl_wait();
+  pdl_release();
   ccl::for_batch_quads(I, total_rows, [&](const Img& m, int y, int x, int n) {
     int r[4], lab[4], kl[4];
     uint8_t fl[4];
@@ -706,17 +708,17 @@ cudaError_t chain_impl(int dtype, const Plan& P, const Ws& w, int recon_conn, do
     e = dispatch_int(dtype, [&](auto* tag) -> cudaError_t {
       using T = std::remove_pointer_t<decltype(tag)>;
       return ccl::label_filled(ClsAboveOrNot<T>{GtThr<T>::make(thr)}, P.I, t, code, w.forest(true), outside,
-                               w.bits_bytes, s);
+                               w.bits_bytes, s, true);
     });
+    // From the labelling on, every launch is a programmatic dependent of the one before it.
     if (e == cudaSuccess)
       e = ccl::rank_roots(P.I, t, w.forest(true), area_min, area_max, w.R, w.bits, w.bits_bytes, w.tmp, w.wpre,
-                          w.counts, s, outside);
+                          w.counts, s, outside, true);
     if (e == cudaSuccess) {
       const int64_t W1 = P.I.d ? 0 : P.I.one.W;
-      label_out_kernel<true, true, true><<<qrb(t), 256, 0, s>>>(P.I, t.rows, w.L, w.R, labels_out, W1 * 4, w.A,
-                                                                area_min, area_max, nullptr, 0, area_out, W1,
-                                                                outside, fill_out, W1);
-      e = cudaGetLastError();
+      e = launch_dependent(label_out_kernel<true, true, true>, qrb(t), dim3(256), s, P.I, t.rows, (const int*)w.L,
+                           (const int*)w.R, labels_out, W1 * 4, (const int*)w.A, area_min, area_max,
+                           (int32_t*)nullptr, (int64_t)0, area_out, W1, (const unsigned*)outside, fill_out, W1);
     }
     return e;
   }
@@ -790,7 +792,7 @@ cudaError_t candidates_impl(const Plan& P, const Ws& w, double g1, double g2, in
   unsigned* outside = (unsigned*)w.F;
   if (e == cudaSuccess)
     e = ccl::label_filled(ClsValleyAboveOrNot{gt1}, P.I, t, ccl::kConnFg8Bg4, w.forest(true), outside,
-                          w.bits_bytes, s);
+                          w.bits_bytes, s, true);
   if (e == cudaSuccess) e = ccl::count_roots(P.I, t, w.forest(true), lo, hi, w.bits, w.counts, s, outside);
   if (e == cudaSuccess) e = cudaMemsetAsync(w.bits, 0, w.bits_bytes, s);
   const ccl::Forest sel{w.R, nullptr, w.roots, w.nroots};
