@@ -28,6 +28,7 @@
 
 #include "batch.cuh"
 #include "common.cuh"
+#include "launch.cuh"
 
 namespace nsgb {
 namespace ccl {

@@ -5,8 +5,6 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <utility>
-
 #include "../../include/nsgb.h"
 
 #define NSGB_FULL 0xFFFFFFFFu
@@ -24,30 +22,6 @@ enum DevStatus : int {
 // Every device-side spin gives up after this many polls (each poll sleeps ~256 ns, so the
 // limit is roughly 2 s) and records kDevTimeout instead of waiting forever.
 constexpr long long kSpinLimit = 1ll << 23;
-
-// Programmatic dependent launch.  A kernel launched by launch_dependent() may be scheduled
-// while the kernel before it on the stream drains; pdl_wait() holds it until that kernel has
-// completed and its writes are visible, and pdl_release() lets the next such kernel be
-// scheduled once every CTA of this one has started.  Both are no-ops in a kernel launched the
-// ordinary way, so kernels shared with other paths call them unconditionally, first thing.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-
-template <typename... KArgs, typename... Args>
-inline cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s,
-                                    Args&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
-}
 
 __device__ __forceinline__ void set_status(int* status, int code) {
   atomicCAS(status, 0, code);
