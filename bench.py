@@ -38,13 +38,13 @@ PKG = os.path.join(ROOT, "emory-cci-fast-ia-gsoc_gb300")
 sys.path.insert(0, PKG)
 
 METRIC = "imreconstruct+bwlabel MPix/s, uint8 4096², plain vs batched GPU; % of HBM peak"
-# One image: recon init + recon, the two-class labelling that fills and labels at once (local,
-# merge, border walk, parent join, flatten), rank (mark, count, scan, assign), label/area/fill
-# output.  A batch: recon init + recon, fill (pack, flood seed, flood seed finish, flood,
+# One image: recon init + recon, the two-class labelling that fills and labels at once
+# (zeroing, local, merge, border walk, parent join, flatten), rank (zeroing, mark, count, scan,
+# assign), label/area/fill output.  A batch: recon init + recon, fill (pack, flood seed, flood seed finish, flood,
 # output), label (local, merge, flatten), rank (mark, count, scan, assign), label/area output.
 # See csrc/ops.cu chain_impl.  A tuned schedule with streaming passes replaces recon init by its
 # passes and two seed kernels (tuned_passes below).
-KERNELS_PER_CHAIN = 12
+KERNELS_PER_CHAIN = 14
 KERNELS_PER_BATCH_CHAIN = 15
 E2E_LANES = 4  # streams the end-to-end steps rotate over
 
@@ -920,10 +920,10 @@ def bbox_section(args, dev, steps=20):
 
 
 # -- S1 after the colour steps: opening and nucleus-candidate stage ------------------------------
-# recon init + recon, bw1 filled and labelled at once (local, merge, border walk, parent join,
-# flatten) + kept count, bw2 label (local, merge, flatten), seeds, output: csrc/ops.cu
-# candidates_impl
-CANDIDATE_KERNELS = 13
+# recon init + recon, bw1 filled and labelled at once (zeroing, local, merge, border walk,
+# parent join, flatten) + kept count, bw2 label (local, merge, flatten), seeds, output:
+# csrc/ops.cu candidates_impl
+CANDIDATE_KERNELS = 14
 OPEN_KERNELS = 2  # erosion, dilation (csrc/morph.cu)
 
 
