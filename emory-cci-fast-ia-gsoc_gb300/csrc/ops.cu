@@ -75,6 +75,13 @@ struct GtThr {
 struct ClsValueU8 {  // bwlabel: the pixel value
   __device__ uint32_t operator()(const Img& m, int y, int x) const { return px<uint8_t>(m.plane, m.pitch, y, x); }
 };
+struct ClsNotFlooded {  // a batch's filled image: the pixels the flood from outside did not reach
+  const uint32_t* flooded;  // bit plane, rows of bit_words(W) words from Img::b_base
+  __device__ uint32_t operator()(const Img& m, int y, int x) const {
+    const uint32_t w = __ldg(flooded + m.b_base + (int64_t)y * ((m.W + 31) / 32) + (x >> 5));
+    return ((w >> (x & 31)) & 1u) ^ 1u;
+  }
+};
 struct ClsDenseU8 {  // the chain's filled image F in the workspace (dense, at px_base)
   const uint8_t* F;
   __device__ uint32_t operator()(const Img& m, int y, int x) const {
@@ -205,54 +212,56 @@ __global__ void fill_out_kernel(Imgs I, int total_rows, const int* __restrict__ 
 }
 
 // Bit planes for the chain's hole fill (bitfill.cu): open = 1 where the reconstruction is not
-// above the threshold (the class the fill works on), flooded = 0.  One thread per 32-pixel word,
-// with vector loads where the word's pixels are 16-byte aligned.
+// above the threshold (the class the fill works on), flooded = 0.  One lane per 32-pixel word of
+// the planes of all images (a flat walk, so narrow images leave no lane idle).  Where every
+// lane's word starts on a 16-byte boundary the lanes load their own words with vector loads;
+// otherwise (rows of an odd width start anywhere) the warp loads each lane's word in turn, one
+// pixel per lane, and forms it with a ballot: every load then reads consecutive bytes, where
+// per-lane scalar loads would touch 32 sectors per instruction.
 template <typename T>
-__global__ void pack_open_kernel(Imgs I, int total_rows, GtThr<T> gt, uint32_t* __restrict__ open,
+__global__ void pack_open_kernel(Imgs I, int total_words, GtThr<T> gt, uint32_t* __restrict__ open,
                                  uint32_t* __restrict__ flooded) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  ccl::for_batch_rows(I, total_rows, [&](const Img& m, int y) {
-    const int nw = bit_words(m.W);
-    if (k >= nw) return;
-    const T* row = (const T*)((const char*)m.plane + (int64_t)y * m.pitch) + 32 * k;
-    const int n = min(32, m.W - 32 * k);
+  const int lane = threadIdx.x & 31;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x + threadIdx.x - lane; base < total_words; base += stride) {
+    const int wi = base + lane;
+    const T* row = nullptr;
+    int n = 0;
+    if (wi < total_words) {
+      const Img& m = I.d ? I.d[img_of(I, wi, BBase())] : I.one;
+      const int nw = bit_words(m.W);
+      const int rel = wi - m.b_base;
+      const int y = rel / nw, k = rel - y * nw;
+      row = (const T*)((const char*)m.plane + (int64_t)y * m.pitch) + 32 * k;
+      n = min(32, m.W - 32 * k);
+    }
     uint32_t bits = 0;
-    if (n == 32 && ((uintptr_t)row & 15) == 0) {
-      constexpr int V = 16 / sizeof(T);
+    if (__all_sync(NSGB_FULL, n == 0 || (n == 32 && ((uintptr_t)row & 15) == 0))) {
+      if (n == 32) {
+        constexpr int V = 16 / sizeof(T);
 #pragma unroll
-      for (int q = 0; q < 32 / V; ++q) {
-        const uint4 v = __ldcg((const uint4*)row + q);
-        T e[V];
-        memcpy(e, &v, 16);
+        for (int q = 0; q < 32 / V; ++q) {
+          const uint4 v = __ldg((const uint4*)row + q);
+          T e[V];
+          memcpy(e, &v, 16);
 #pragma unroll
-        for (int j = 0; j < V; ++j) bits |= (gt(e[j]) ? 0u : 1u) << (q * V + j);
+          for (int j = 0; j < V; ++j) bits |= (gt(e[j]) ? 0u : 1u) << (q * V + j);
+        }
       }
     } else {
-      for (int j = 0; j < n; ++j) bits |= (gt(__ldcg(row + j)) ? 0u : 1u) << j;
+#pragma unroll 8
+      for (int src = 0; src < 32; ++src) {
+        const T* r = (const T*)__shfl_sync(NSGB_FULL, (unsigned long long)row, src);
+        const int ns = __shfl_sync(NSGB_FULL, n, src);
+        const uint32_t b = __ballot_sync(NSGB_FULL, lane < ns && !gt(__ldg(r + lane)));
+        if (lane == src) bits = b;
+      }
     }
-    const int64_t o = (int64_t)m.b_base + (int64_t)y * nw + k;
-    open[o] = bits;
-    flooded[o] = 0u;
-  });
-}
-
-// The filled image from the flood: 255 where the flood did not reach (foreground and holes),
-// 0 where it did.  Writes the workspace plane F (dense) and the caller's output (single image:
-// `out` / `pitch_out`; batch: Img::fill, dense), four pixels per thread.
-__global__ void flood_out_kernel(Imgs I, int total_rows, const uint32_t* __restrict__ flooded, uint8_t* F,
-                                 uint8_t* out, int64_t pitch_out) {
-  ccl::for_batch_quads(I, total_rows, [&](const Img& m, int y, int x, int n) {
-    const uint32_t w = __ldg(flooded + m.b_base + (int64_t)y * bit_words(m.W) + (x >> 5)) >> (x & 31);
-    uint8_t f[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) f[k] = ((w >> k) & 1u) ? 0 : 255;
-    const int64_t gi = (int64_t)m.px_base + (int64_t)y * m.W + x;
-    if (F) store4_u8(F + gi, n, f);
-    uint8_t* o = nullptr;
-    if (!I.d) o = out ? pxp<uint8_t>(out, pitch_out, y, x) : nullptr;
-    else if (m.fill) o = m.fill + (int64_t)y * m.W + x;
-    if (o) store4_u8(o, n, f);
-  });
+    if (wi < total_words) {
+      open[wi] = bits;
+      flooded[wi] = 0u;
+    }
+  }
 }
 
 // Binary reconstruction output, in place on the marker (= plane).
@@ -303,8 +312,9 @@ __global__ void candidates_out_kernel(Imgs I, int total_rows, const int* __restr
 // loads, because a giant component's root is read by every one of its pixels.  Single image:
 // explicit output pointers / pitches; batch: Img::labels / Img::area (dense).
 // RELABEL: raster rank labels (else root indices); AREA: area-filter outputs (A non-null).
-// FILLED: the forest of ccl::label_filled, whose roots marked in `outside` are background; the
-// filled image (255 elsewhere) goes to `filled` (single image, optional) or Img::fill (batch).
+// FILLED: the labelled pixels are the filled image, written as 255 (0 elsewhere) to `filled`
+// (single image, optional) or Img::fill (batch); with `outside` (the forest of
+// ccl::label_filled) the roots it marks are background too.
 template <bool RELABEL, bool AREA, bool FILLED = false>
 __global__ void label_out_kernel(Imgs I, int total_rows, const int* __restrict__ L, const int* __restrict__ rank,
                                  int32_t* labels, int64_t pitch_labels, const int* __restrict__ A, int lo,
@@ -322,7 +332,7 @@ __global__ void label_out_kernel(Imgs I, int total_rows, const int* __restrict__
       uint8_t fi[4];
 #pragma unroll
       for (int k = 0; k < 4; ++k)
-        out[k] = (k > 0 && r[k] == r[k - 1]) ? out[k - 1] : (r[k] >= 0 && ccl::test_bit(outside, r[k]));
+        out[k] = (k > 0 && r[k] == r[k - 1]) ? out[k - 1] : (r[k] >= 0 && outside && ccl::test_bit(outside, r[k]));
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         if (out[k]) r[k] = -1;
@@ -723,27 +733,36 @@ cudaError_t chain_impl(int dtype, const Plan& P, const Ws& w, int recon_conn, do
     return e;
   }
   if (e == cudaSuccess && P.I.d && t.n > 1) {
-    // (b)+(c) on a batch: the pixels not above the threshold as a bit plane, flooded from
-    // outside each image (bitfill.cu); the fill is what the flood does not reach.  The label
-    // planes L and A hold the two bit planes until the labelling of step (d) overwrites them.
-    // A flood is a chain of dependent tile visits from the border inwards; many images flood at
-    // once, so the batch hides that latency, and it then costs a fraction of the labelling
-    // (pack, flood and output touch 1 bit per pixel where the labelling writes and reads an int).
+    // (b)-(e) on a batch: the pixels not above the threshold as a bit plane, flooded from
+    // outside each image (bitfill.cu); the filled image is what the flood does not reach, and
+    // it is labelled straight from the flooded plane, the label output writing it out.  The
+    // planes L and R hold the open and flooded bit planes until the labelling (L) and the rank
+    // (R) overwrite them.  A flood is a chain of dependent tile visits from the border inwards;
+    // many images flood at once, so the batch hides that latency, and it then costs a fraction
+    // of the labelling (pack and flood touch 1 bit per pixel where a labelling writes an int).
     uint32_t* open = (uint32_t*)w.L;
-    uint32_t* flooded = (uint32_t*)w.A;
+    uint32_t* flooded = (uint32_t*)w.R;
     e = dispatch_int(dtype, [&](auto* tag) -> cudaError_t {
       using T = std::remove_pointer_t<decltype(tag)>;
-      pack_open_kernel<T><<<ccl::rowcol_grid(t.rows, bit_words(t.max_w)), 256, 0, s>>>(P.I, t.rows, GtThr<T>::make(thr),
-                                                                                     open, flooded);
+      pack_open_kernel<T><<<ccl::flat_grid(t.b_words), 256, 0, s>>>(P.I, (int)t.b_words, GtThr<T>::make(thr), open,
+                                                                   flooded);
       return cudaGetLastError();
     });
     if (e == cudaSuccess)
       e = flood_launch(P.I, t.f_tiles, open, flooded, fill_conn, w.recon, s, opts ? opts->queue_poll_limit : 0);
+    if (e == cudaSuccess) e = ccl::label(ClsNotFlooded{flooded}, P.I, t, label_conn, w.forest(true), s);
+    if (e == cudaSuccess)
+      e = ccl::rank_roots(P.I, t, w.forest(true), area_min, area_max, w.R, w.bits, w.bits_bytes, w.tmp, w.wpre,
+                          w.counts, s);
     if (e == cudaSuccess) {
-      flood_out_kernel<<<qrb(t), 256, 0, s>>>(P.I, t.rows, flooded, w.F, fill_out, 0);
+      label_out_kernel<true, true, true><<<qrb(t), 256, 0, s>>>(P.I, t.rows, w.L, w.R, labels_out, 0, w.A, area_min,
+                                                                area_max, nullptr, 0, area_out, 0, nullptr, fill_out,
+                                                                0);
       e = cudaGetLastError();
     }
-  } else if (e == cudaSuccess) {
+    return e;
+  }
+  if (e == cudaSuccess) {
     // (b)+(c) on one image: the threshold fused into the labelling's classifier, components
     // touching the border seeded.  (One image's flood is a chain of dependent tile visits that
     // the labelling does not have: 0.58 against 0.49 ms for the 4096^2 chain.)
