@@ -39,12 +39,12 @@ sys.path.insert(0, PKG)
 
 METRIC = "imreconstruct+bwlabel MPix/s, uint8 4096², plain vs batched GPU; % of HBM peak"
 # One image: recon init + recon, the two-class labelling that fills and labels at once
-# (zeroing, local, merge, border walk, parent join, flatten), rank (zeroing, mark, count, scan,
-# assign), label/area/fill output.  A batch: recon init + recon, fill (pack, flood seed, flood
+# (zeroing, local, merge, border walk, parent join, flatten), rank (mark, count, scan, assign),
+# label/area/fill output.  A batch: recon init + recon, fill (pack, flood seed, flood
 # seed finish, flood), label of the flooded plane (local, merge, flatten), rank (mark, count,
 # scan, assign), label/area/fill output.  See csrc/ops.cu chain_impl.  A tuned schedule with
 # streaming passes replaces recon init by its passes and two seed kernels (tuned_passes below).
-KERNELS_PER_CHAIN = 14
+KERNELS_PER_CHAIN = 13
 KERNELS_PER_BATCH_CHAIN = 14
 E2E_LANES = 4  # streams the end-to-end steps rotate over
 

@@ -74,7 +74,6 @@ struct CTileBase { __device__ int operator()(const Img& m) const { return m.c_ti
 struct BlkBase { __device__ int operator()(const Img& m) const { return m.blk_base; } };
 struct RowBase { __device__ int operator()(const Img& m) const { return m.row_base; } };
 struct PxBase { __device__ int operator()(const Img& m) const { return m.px_base; } };
-struct BBase { __device__ int operator()(const Img& m) const { return m.b_base; } };
 struct FTileBase { __device__ int operator()(const Img& m) const { return m.f_tile_base; } };
 struct REvenBase { __device__ int operator()(const Img& m) const { return m.r_even_base; } };
 struct ROddBase { __device__ int operator()(const Img& m) const { return m.r_tile_base - m.r_even_base; } };

@@ -184,12 +184,12 @@ cudaError_t rank_bits(const Imgs& I, const BatchTotals& t, const unsigned* bits,
 
 cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, int* rank,
                        unsigned* bits, size_t bits_bytes, int* block_tmp, int* wpre, int* counts, cudaStream_t s,
-                       const unsigned* skip, bool pdl) {
-  cudaError_t e;
-  if (pdl) {
-    const int nb = (int)(bits_bytes / sizeof(unsigned));
-    e = launch_k(true, zero_words, dim3(flat_grid(nb + 2 * t.n)), dim3(256), s, bits, nb, (unsigned*)counts, 2 * t.n);
-  } else {
+                       const unsigned* skip, bool pdl, bool zeroed) {
+  cudaError_t e = cudaSuccess;
+  if (!zeroed && pdl) {
+    const ZeroSpans z{{bits, (unsigned*)counts, nullptr, nullptr}, {(int)(bits_bytes / sizeof(unsigned)), 2 * t.n, 0, 0}};
+    e = launch_k(true, zero_words, dim3(flat_grid(z.total())), dim3(256), s, z);
+  } else if (!zeroed) {
     e = cudaMemsetAsync(bits, 0, bits_bytes, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, sizeof(int) * 2 * (size_t)t.n, s);
   }

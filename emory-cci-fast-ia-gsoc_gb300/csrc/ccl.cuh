@@ -605,13 +605,21 @@ static __global__ void ccl_join_parents(Imgs I, Forest f, int max_roots, const u
   }
 }
 
-// Zeroes words [0, na) of a and [0, nb) of b.
-static __global__ void zero_words(unsigned* a, int na, unsigned* b, int nb) {
+// Up to four word ranges to clear in one launch (n[k] words from p[k]; unused ranges have n 0).
+struct ZeroSpans {
+  unsigned* p[4];
+  int n[4];
+  int total() const { return n[0] + n[1] + n[2] + n[3]; }
+};
+
+static __global__ void zero_words(ZeroSpans z) {
   pdl_wait();
   pdl_release();
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < na + nb; i += gridDim.x * blockDim.x) {
-    if (i < na) a[i] = 0u;
-    else b[i - na] = 0u;
+  const int total = z.n[0] + z.n[1] + z.n[2] + z.n[3];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    int j = i, r = 0;
+    while (j >= z.n[r]) j -= z.n[r++];
+    z.p[r][j] = 0u;
   }
 }
 
@@ -640,12 +648,17 @@ struct Class2 {
 // the filled image).  Afterwards root(i) = L[L[i]].
 template <class Cls>
 cudaError_t label_filled(const Cls& cls, const Imgs& I, const BatchTotals& t, int conn, const Forest& f,
-                         unsigned* outside, size_t outside_bytes, cudaStream_t s, bool pdl = false) {
+                         unsigned* outside, size_t outside_bytes, cudaStream_t s, bool pdl = false,
+                         ZeroSpans more = ZeroSpans{{nullptr, nullptr, nullptr, nullptr}, {0, 0, 0, 0}}) {
   // The first launch follows whatever the caller queued last, so it is an ordinary one; the
-  // rest may start while their predecessor drains.
-  const int zw = (int)(outside_bytes / sizeof(unsigned));
-  cudaError_t e = launch_k(false, zero_words, dim3(flat_grid(zw + 1)), dim3(256), s, (unsigned*)f.nroots, 1,
-                           outside, zw);
+  // rest may start while their predecessor drains.  It also clears the caller's ranges 2 and 3
+  // of `more` (for the ranking that follows, say).
+  ZeroSpans z = more;
+  z.p[0] = (unsigned*)f.nroots;
+  z.n[0] = 1;
+  z.p[1] = outside;
+  z.n[1] = (int)(outside_bytes / sizeof(unsigned));
+  cudaError_t e = launch_k(false, zero_words, dim3(flat_grid(z.total())), dim3(256), s, z);
   if (e != cudaSuccess) return e;
   if (conn == kConnFg8Bg4) {
     e = launch_k(pdl, ccl_local<Cls, kConnFg8Bg4>, dim3(t.c_tiles), dim3(kThreads), s, cls, I, f);
@@ -671,10 +684,10 @@ cudaError_t label_filled(const Cls& cls, const Imgs& I, const BatchTotals& t, in
 // block) are scratch.
 // Roots marked in `skip` (optional) are left out: not counted and not ranked.
 // With pdl, every launch is a programmatic dependent of the kernel before it (the caller's last
-// launch must be a kernel).
+// launch must be a kernel); with zeroed, `bits` and `counts` are already clear.
 cudaError_t rank_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, int* rank,
                        unsigned* bits, size_t bits_bytes, int* block_tmp, int* wpre, int* counts, cudaStream_t s,
-                       const unsigned* skip = nullptr, bool pdl = false);
+                       const unsigned* skip = nullptr, bool pdl = false, bool zeroed = false);
 // The counts of rank_roots alone (no ranks).  `bits` receives the global roots' bits (scratch,
 // not cleared first).
 cudaError_t count_roots(const Imgs& I, const BatchTotals& t, const Forest& f, int lo, int hi, unsigned* bits,

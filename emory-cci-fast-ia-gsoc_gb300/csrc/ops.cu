@@ -218,6 +218,8 @@ __global__ void fill_out_kernel(Imgs I, int total_rows, const int* __restrict__ 
 // otherwise (rows of an odd width start anywhere) the warp loads each lane's word in turn, one
 // pixel per lane, and forms it with a ballot: every load then reads consecutive bytes, where
 // per-lane scalar loads would touch 32 sectors per instruction.
+struct BBase { __device__ int operator()(const Img& m) const { return m.b_base; } };
+
 template <typename T>
 __global__ void pack_open_kernel(Imgs I, int total_words, GtThr<T> gt, uint32_t* __restrict__ open,
                                  uint32_t* __restrict__ flooded) {
@@ -717,13 +719,16 @@ cudaError_t chain_impl(int dtype, const Plan& P, const Ws& w, int recon_conn, do
     const int code = label_conn == 8 ? ccl::kConnFg8Bg4 : ccl::kConnFg4Bg8;
     e = dispatch_int(dtype, [&](auto* tag) -> cudaError_t {
       using T = std::remove_pointer_t<decltype(tag)>;
+      // the ranking's bitmap and counts are cleared by the labelling's first launch
+      const ccl::ZeroSpans rank_zero{{nullptr, nullptr, w.bits, (unsigned*)w.counts},
+                                     {0, 0, (int)(w.bits_bytes / sizeof(unsigned)), 2 * t.n}};
       return ccl::label_filled(ClsAboveOrNot<T>{GtThr<T>::make(thr)}, P.I, t, code, w.forest(true), outside,
-                               w.bits_bytes, s, true);
+                               w.bits_bytes, s, true, rank_zero);
     });
     // From the labelling on, every launch is a programmatic dependent of the one before it.
     if (e == cudaSuccess)
       e = ccl::rank_roots(P.I, t, w.forest(true), area_min, area_max, w.R, w.bits, w.bits_bytes, w.tmp, w.wpre,
-                          w.counts, s, outside, true);
+                          w.counts, s, outside, true, true);
     if (e == cudaSuccess) {
       const int64_t W1 = P.I.d ? 0 : P.I.one.W;
       e = launch_dependent(label_out_kernel<true, true, true>, qrb(t), dim3(256), s, P.I, t.rows, (const int*)w.L,
