@@ -251,7 +251,7 @@ __global__ void pack_open_kernel(Imgs I, int total_words, GtThr<T> gt, uint32_t*
         }
       }
     } else {
-#pragma unroll 8
+#pragma unroll 4
       for (int src = 0; src < 32; ++src) {
         const T* r = (const T*)__shfl_sync(NSGB_FULL, (unsigned long long)row, src);
         const int ns = __shfl_sync(NSGB_FULL, n, src);
