@@ -1002,7 +1002,9 @@ nsgb_status nsgb_imfill_holes(int dtype, const void* image, void* out, int64_t r
     case NSGB_F32: fill_marker_kernel<float><<<rc(rows, cols), 256, 0, s>>>((const float*)image, (float*)out, pitch, H, W); break;
   }
   const Plan R = single_plan(dtype, out, image, rows, cols, pitch);
-  e = recon_timed(opts, dtype, R, conn, true, false, ws, s, 2);  // front from the border: re-sweep
+  // front from the border: re-sweep a tile up to four times when a neighbour changed while it
+  // ran (16384^2 fills, 8-connected: 11.76 -> 11.53 ms u8, 18.48 -> 17.93 ms i32 against two)
+  e = recon_timed(opts, dtype, R, conn, true, false, ws, s, 4);
   if (e == cudaSuccess && dtype == NSGB_F32) {
     canon_zero_f32_kernel<<<quad_grid(rows, cols), 256, 0, s>>>((float*)out, pitch, H, W);
     e = cudaGetLastError();
