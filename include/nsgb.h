@@ -198,7 +198,10 @@ nsgb_status nsgb_invert(int dtype, const void* in, void* out, int64_t rows, int6
  * B = R > thr; F = imfillHoles(B, binary, fill_conn); L = bwlabel2(F, label_conn, relabel);
  * A = bwareaopen2(F, unlabeled, flatten, area_min, area_max, label_conn).  Outputs fill,
  * labels, area (each optional).  n_labels / n_kept: host pointers (optional; synchronize).
- * dtypes of marker/mask: u8, u16, i32 (threshold in the same units). */
+ * dtypes of marker/mask: u8, u16, i32 (threshold in the same units).  With n_labels = n_kept =
+ * NULL and opts->sync == 0 the call only enqueues work, so it can be captured into a CUDA graph;
+ * its launches after the reconstruction are programmatic dependents of one another, ordered
+ * after everything queued before the call. */
 nsgb_status nsgb_chain(int dtype, void* marker, const void* mask, int64_t rows, int64_t cols,
                        int64_t pitch, int recon_conn, double thr, int fill_conn, int label_conn,
                        int32_t area_min, int32_t area_max, uint8_t* fill_out, int32_t* labels_out,
