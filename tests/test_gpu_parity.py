@@ -387,6 +387,43 @@ def test_chain_in_cuda_graph_with_timing_events(nsgb, oracle):
     assert lib.nsgb_device_status(C.c_void_p(ws), None) == 0
 
 
+@pytest.mark.parametrize("fill_conn,label_conn", [(4, 8), (8, 4)])
+def test_chain_pitched_inputs(nsgb, oracle, fill_conn, label_conn):
+    """nsgb_chain through the C ABI on marker and mask rows with padding (pitch > cols, odd
+    sizes), the one-labelling fill of both dual connectivity pairs, against the oracle; the
+    padding bytes stay untouched and the counts come back through the host pointers."""
+    import ctypes as C
+
+    import torch
+    from nsgb import _ffi, synth
+
+    lib = _ffi.lib
+    H, W, pad = 157, 301, 19
+    mask_h, marker_h = synth.tile_u8(H, W, 25, 5)
+    exp = oracle.chain(marker_h, mask_h, fill_conn=fill_conn, label_conn=label_conn)
+    big_k = torch.full((H, W + pad), 7, dtype=torch.uint8, device="cuda")
+    big_m = torch.full((H, W + pad), 9, dtype=torch.uint8, device="cuda")
+    big_k[:, :W] = to_dev(marker_h)
+    big_m[:, :W] = to_dev(mask_h)
+    fill = torch.empty((H, W), dtype=torch.uint8, device="cuda")
+    labels = torch.empty((H, W), dtype=torch.int32, device="cuda")
+    area = torch.empty((H, W), dtype=torch.uint8, device="cuda")
+    nb = lib.nsgb_workspace_size(_ffi.OP_CHAIN, _ffi.U8, H, W)
+    wst = torch.empty(nb + 256, dtype=torch.uint8, device="cuda")
+    ws = (wst.data_ptr() + 255) & ~255
+    nl, nk = C.c_int32(-1), C.c_int32(-1)
+    st = lib.nsgb_chain(_ffi.U8, big_k.data_ptr(), big_m.data_ptr(), H, W, W + pad, 8, 128.0, fill_conn, label_conn,
+                        11, 1000, fill.data_ptr(), labels.data_ptr(), area.data_ptr(), C.byref(nl), C.byref(nk), ws,
+                        nb, C.c_void_p(torch.cuda.current_stream().cuda_stream), None)
+    assert st == 0
+    assert np.array_equal(to_np(big_k[:, :W]), exp["recon"])
+    assert np.array_equal(to_np(fill), exp["fill"])
+    assert np.array_equal(to_np(labels), exp["labels"])
+    assert np.array_equal(to_np(area), exp["area"])
+    assert nl.value == exp["n_labels"] and nk.value == exp["n_kept"]
+    assert (to_np(big_k[:, W:]) == 7).all() and (to_np(big_m[:, W:]) == 9).all()
+
+
 def _nested_rings(H, W, seed):
     """Concentric rectangular rings of alternating brightness around random centres, with random
     gaps cut into some rings: components enclosed by components several levels deep."""
