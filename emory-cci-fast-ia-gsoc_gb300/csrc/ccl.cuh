@@ -488,6 +488,28 @@ __global__ void ccl_seed_pixels(Imgs I, int total_rows, const int* __restrict__ 
   });
 }
 
+// The same with four consecutive pixels per thread: their roots come from one 16-byte label
+// load where aligned, and a root shared with the seed pixel before it is set once.
+template <class Seed>
+__global__ void ccl_seed_quads(Imgs I, int total_rows, const int* __restrict__ L, Seed seed,
+                               unsigned* __restrict__ bits) {
+  for_batch_quads(I, total_rows, [&](const Img& m, int y, int x, int n) {
+    bool sd[4];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      sd[k] = k < n && seed(m, y, x + k);
+      any = any || sd[k];
+    }
+    if (!any) return;
+    int r[4];
+    roots4_ro(L, (int64_t)m.px_base + (int64_t)y * m.W + x, n, r);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (sd[k] && r[k] >= 0 && !(k > 0 && sd[k - 1] && r[k - 1] == r[k])) set_root_bit(bits, r[k]);
+  });
+}
+
 // Border pixel k of an H x W image (top row, bottom row, left column, right column; 2W + 2H
 // positions, corners visited twice).
 __device__ __forceinline__ void border_pixel(int k, int H, int W, int& y, int& x) {

@@ -822,7 +822,7 @@ cudaError_t candidates_impl(const Plan& P, const Ws& w, double g1, double g2, in
   const ccl::Forest sel{w.R, nullptr, w.roots, w.nroots};
   if (e == cudaSuccess) e = ccl::label(ClsValleyAbove{gt2}, P.I, t, 8, sel, s);
   if (e == cudaSuccess) {
-    ccl::ccl_seed_pixels<SeedCandidate><<<rcb(t), 256, 0, s>>>(P.I, t.rows, w.R, SeedCandidate{gt2, w.L, w.A, lo, hi, outside},
+    ccl::ccl_seed_quads<SeedCandidate><<<qrb(t), 256, 0, s>>>(P.I, t.rows, w.R, SeedCandidate{gt2, w.L, w.A, lo, hi, outside},
                                                                w.bits);
     candidates_out_kernel<<<qrb(t), 256, 0, s>>>(P.I, t.rows, w.R, w.bits, rbc, out);
     e = cudaGetLastError();
