@@ -1145,6 +1145,15 @@ def large_section(args, dev, steps=3):
     return res
 
 
+def link_bound_s(in_bytes, out_bytes, d2h_gbps, h2d_gbps, both_gbps):
+    """Seconds a step's copies need on the host link: both directions start together at the
+    concurrent rate; once the smaller transfer is done the rest of the larger one runs at its
+    direction's solo rate."""
+    lo, hi = min(in_bytes, out_bytes), max(in_bytes, out_bytes)
+    solo = d2h_gbps if out_bytes >= in_bytes else h2d_gbps
+    return lo / (both_gbps * 1e9) + (hi - lo) / (solo * 1e9)
+
+
 def host_link(dev, in_bytes, out_bytes, px, reps=5):
     """The host link's own bound on an end-to-end step: pinned-memory copy bandwidth measured
     in this process (device -> host alone, host -> device alone, and both directions at once on
@@ -1179,9 +1188,7 @@ def host_link(dev, in_bytes, out_bytes, px, reps=5):
 
     timed(True, True)  # warm-up
     d2h, h2d, both = timed(True, False), timed(False, True), timed(True, True)
-    lo, hi = min(in_bytes, out_bytes), max(in_bytes, out_bytes)
-    solo = d2h if out_bytes >= in_bytes else h2d
-    bound_s = lo / (both * 1e9) + (hi - lo) / (solo * 1e9)
+    bound_s = link_bound_s(in_bytes, out_bytes, d2h, h2d, both)
     return {"d2h_GBps": d2h, "h2d_GBps": h2d, "concurrent_GBps_per_direction": both,
             "bound_ms_per_step": bound_s * 1e3, "bound_mpix_s": px / 1e6 / bound_s,
             "note": "pinned-memory copies timed in this run; frac = e2e value / this bound"}
